@@ -1,0 +1,4 @@
+"""GB300-native Barger propagation (CUDAProb3++ hot path) behind the reference's
+Propagator API.  Importing the package loads nothing; the CUDA library is loaded (and must
+exist) when a propagator is constructed."""
+from .types import Antineutrino, Mixing, Neutrino, NeutrinoType, ProbType  # noqa: F401

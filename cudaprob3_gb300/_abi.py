@@ -1,0 +1,98 @@
+"""ctypes binding of libcp3gb300.so (the C ABI in include/cudaprob3_gb300.h).
+
+The library is built in-tree by ``cudaprob3_gb300.build``.  There is no CPU fallback: if the
+library is missing or cannot be loaded, ``lib()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+# C ABI symbols, in header order; the CPU test-suite checks the library exports each one.
+EXPORTS = (
+    "cp3_atmos_create", "cp3_beam_create", "cp3_destroy", "cp3_last_error", "cp3_get_info",
+    "cp3_set_energies", "cp3_set_cosines", "cp3_set_mns", "cp3_set_masses", "cp3_set_layers",
+    "cp3_set_layers_poly", "cp3_set_density_file", "cp3_set_chemical_composition",
+    "cp3_set_production_height", "cp3_set_beam_density", "cp3_set_beam_path_length",
+    "cp3_set_production_height_averaging", "cp3_calculate", "cp3_calculate_async",
+    "cp3_synchronize", "cp3_get_probability", "cp3_get_probability_beam",
+    "cp3_get_probability_arr", "cp3_device_result", "cp3_copy_result_async",
+)
+
+CP3_OK = 0
+FP64 = 0
+MIXED = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_h = C.c_void_p
+
+_SIGS = {
+    "cp3_atmos_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_h)], C.c_int),
+    "cp3_beam_create": ([C.c_int, C.c_int, C.c_int, C.POINTER(_h)], C.c_int),
+    "cp3_destroy": ([_h], C.c_int),
+    "cp3_last_error": ([_h], C.c_char_p),
+    "cp3_get_info": ([_h, _ip, _ip, _ip, _ip], C.c_int),
+    "cp3_set_energies": ([_h, _dp, C.c_int], C.c_int),
+    "cp3_set_cosines": ([_h, _dp, C.c_int], C.c_int),
+    "cp3_set_mns": ([_h, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int], C.c_int),
+    "cp3_set_masses": ([_h, C.c_double, C.c_double], C.c_int),
+    "cp3_set_layers": ([_h, _dp, _dp, _dp, C.c_int], C.c_int),
+    "cp3_set_layers_poly": ([_h, _dp, _dp, _dp, _dp, _dp, C.c_int], C.c_int),
+    "cp3_set_density_file": ([_h, C.c_char_p, C.c_double, C.c_double], C.c_int),
+    "cp3_set_chemical_composition": ([_h, _dp, C.c_int], C.c_int),
+    "cp3_set_production_height": ([_h, C.c_double], C.c_int),
+    "cp3_set_beam_density": ([_h, C.c_double], C.c_int),
+    "cp3_set_beam_path_length": ([_h, C.c_double], C.c_int),
+    "cp3_set_production_height_averaging": ([_h, C.c_int, _dp, _dp], C.c_int),
+    "cp3_calculate": ([_h, C.c_int], C.c_int),
+    "cp3_calculate_async": ([_h, C.c_int, C.c_void_p], C.c_int),
+    "cp3_synchronize": ([_h], C.c_int),
+    "cp3_get_probability": ([_h, C.c_int, C.c_int, C.c_int, _dp], C.c_int),
+    "cp3_get_probability_beam": ([_h, C.c_int, C.c_int, _dp], C.c_int),
+    "cp3_get_probability_arr": ([_h, C.c_int, _dp], C.c_int),
+    "cp3_device_result": ([_h, C.POINTER(C.c_void_p), _ip, C.POINTER(C.c_size_t)], C.c_int),
+    "cp3_copy_result_async": ([_h, C.c_void_p, C.c_void_p], C.c_int),
+}
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = False):
+    """Load the library once.  Raises if it is missing (no fallback exists)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"libcp3gb300.so not built ({path}); run "
+                               "`python -m cudaprob3_gb300.build` or __graft_entry__.build()")
+        _build.build()
+    L = C.CDLL(path)
+    for name, (args, res) in _SIGS.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = L
+    return L
+
+
+class CP3Error(RuntimeError):
+    """A non-zero status of the C ABI; the message is cp3_last_error()."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+def check(rc: int, handle=None):
+    if rc != CP3_OK:
+        msg = lib().cp3_last_error(handle)
+        raise CP3Error(rc, msg.decode() if msg else f"status {rc}")

@@ -1,0 +1,84 @@
+"""Build libcp3gb300.so in-tree (cudaprob3_gb300/_lib/) with nvcc for sm_103a.
+
+Translation units compile in parallel; cp3_tables.cu (the FP64 eigen work that mirrors the
+reference's arithmetic) is compiled without FMA contraction, everything else with it.
+``python -m cudaprob3_gb300.build`` or ``cudaprob3_gb300.build.build()``.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+LIB = os.path.join(OUT, "libcp3gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# (source, extra flags)
+UNITS = [
+    ("cp3_host.cpp", []),
+    ("cp3_abi.cu", []),
+    ("cp3_tables.cu", ["-fmad=false"]),
+    ("cp3_atmos.cu", []),
+]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcp3gb300.so")
+
+
+def _sources_mtime() -> float:
+    newest = 0.0
+    for root in (SRC, os.path.join(os.path.dirname(HERE), "include")):
+        for f in os.listdir(root):
+            newest = max(newest, os.path.getmtime(os.path.join(root, f)))
+    return newest
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile (if stale) and return the path of the shared library."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+        return LIB
+    nvcc = _nvcc()
+    os.makedirs(OUT, exist_ok=True)
+    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC,
+              "-I", os.path.join(os.path.dirname(HERE), "include")]
+    if verbose:
+        common += ["-Xptxas", "-v"]
+
+    def compile_one(unit):
+        src, extra = unit
+        obj = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
+        cmd = [nvcc] + ARCH + common + extra + ["-c", os.path.join(SRC, src), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return obj, r, cmd
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        results = list(ex.map(compile_one, UNITS))
+    logs = []
+    for obj, r, cmd in results:
+        logs.append(r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    tmp = LIB + ".tmp"
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + [o for o, _, _ in results]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    with open(os.path.join(OUT, "build.log"), "w") as f:
+        f.write("\n".join(logs))
+    if verbose:
+        sys.stdout.write("\n".join(logs))
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,551 @@
+// cp3_abi.cu -- the C ABI (include/cudaprob3_gb300.h): handle state, validation, device
+// buffers, launches and result access.
+//
+// State that the reference keeps in process globals and __constant__ symbols
+// (physics.hpp:115-125) is per handle here: the oscillation block travels by value as a
+// kernel parameter and everything else lives in the handle's own device buffers, so handles
+// never interfere.  Uploads happen lazily at compute time and only for what changed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cudaprob3_gb300.h"
+#include "cp3_host.hpp"
+#include "cp3_kernels.hpp"
+
+using namespace cp3;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+template <class T>
+struct DevBuf {
+    T* ptr = nullptr;
+    size_t count = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    // Grows to at least n elements (contents not kept).
+    cudaError_t reserve(size_t n) {
+        if (n <= count && ptr) return cudaSuccess;
+        release();
+        const cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return e;
+        }
+        count = n;
+        return cudaSuccess;
+    }
+};
+
+}  // namespace
+
+struct cp3_propagator {
+    int kind = 0;  // 0 atmospheric, 1 beam
+    int device = 0, nc = 0, ne = 0, precision = CP3_FP64;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    MixingInput mix;
+    bool mns_set = false, masses_set = false;
+    std::vector<double> energies, cosines;
+    bool energies_set = false, cosines_set = false;
+    EarthModel model;
+    bool model_set = false;
+    double height_cm = 0.0;
+    bool height_set = false;
+    double beam_rho = 0.0, beam_L = 0.0;
+    bool beam_rho_set = false, beam_L_set = false;
+    int avg_bins = 0;
+    std::vector<double> avg_prob, avg_edges;
+
+    TrajectoryTable traj;
+    bool traj_dirty = true;
+    int ncls_used = 0;
+
+    DevBuf<double> d_energies;
+    DevBuf<int> d_seg_off, d_seg_cls;
+    DevBuf<double> d_seg_len, d_cls_rho;
+    DevBuf<float2> d_seg_len_df;
+    DevBuf<double> d_table64;
+    DevBuf<float> d_table32;
+    DevBuf<char> d_result;
+    size_t result_bytes = 0;
+
+    double* h_result = nullptr;  // pinned, lazily allocated
+    bool result_on_host = false;
+    bool computed = false;
+
+    ~cp3_propagator() {
+        if (h_result) cudaFreeHost(h_result);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int fail(cp3_propagator* h, int code, const std::string& msg) {
+    if (h)
+        h->err = msg;
+    else
+        g_create_error = msg;
+    return code;
+}
+
+int cuda_fail(cp3_propagator* h, cudaError_t e, const char* where) {
+    cudaGetLastError();  // clear a sticky-free error so the handle stays usable
+    return fail(h, e == cudaErrorMemoryAllocation ? CP3_ERR_OOM : CP3_ERR_CUDA,
+                std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CP3_CUDA(h, call, where)                            \
+    do {                                                    \
+        const cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, where); \
+    } while (0)
+
+int check_handle(cp3_propagator* h) {
+    if (!h) return fail(nullptr, CP3_ERR_BAD_ARGUMENT, "null propagator handle");
+    return CP3_OK;
+}
+
+int create(int kind, int device, int nc, int ne, int precision, cp3_propagator** out) {
+    if (!out) return fail(nullptr, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (precision != CP3_FP64 && precision != CP3_MIXED)
+        return fail(nullptr, CP3_ERR_BAD_ARGUMENT, "unknown precision");
+    if (ne <= 0 || (kind == 0 && nc <= 0))
+        return fail(nullptr, CP3_ERR_BAD_SIZE, "grid sizes must be positive");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, CP3_ERR_CUDA, "No GPU found");
+    }
+    if (device < 0 || device >= ndev)
+        return fail(nullptr, CP3_ERR_BAD_ARGUMENT,
+                    "The requested GPU Id " + std::to_string(device) + " is not available.");
+    cp3_propagator* h = new cp3_propagator();
+    h->kind = kind;
+    h->device = device;
+    h->nc = kind == 0 ? nc : 1;
+    h->ne = ne;
+    h->precision = precision;
+    h->energies.assign(ne, 0.0);
+    if (kind == 0) h->cosines.assign(nc, 0.0);
+    const size_t elems = (size_t)9 * h->nc * ne;
+    h->result_bytes = elems * (precision == CP3_FP64 ? sizeof(double) : sizeof(float));
+    if ((e = cudaSetDevice(device)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = h->d_energies.reserve(ne)) != cudaSuccess ||
+        (e = h->d_result.reserve(h->result_bytes)) != cudaSuccess) {
+        cudaGetLastError();
+        const std::string msg = std::string("propagator creation failed: ") + cudaGetErrorString(e);
+        delete h;
+        return fail(nullptr, e == cudaErrorMemoryAllocation ? CP3_ERR_OOM : CP3_ERR_CUDA, msg);
+    }
+    *out = h;
+    return CP3_OK;
+}
+
+// Uploads the trajectory table and density classes if any of their inputs changed.
+int prepare_atmos(cp3_propagator* h) {
+    if (!h->traj_dirty) return CP3_OK;
+    std::string msg;
+    int rc = build_trajectories(h->model, h->cosines.data(), h->nc, h->height_cm, &h->traj, &msg);
+    if (rc) return fail(h, rc, msg);
+    const TrajectoryTable& t = h->traj;
+    const size_t nseg = t.len_km.size();
+    CP3_CUDA(h, h->d_seg_off.reserve(t.offset.size()), "allocate trajectories");
+    CP3_CUDA(h, h->d_seg_cls.reserve(nseg), "allocate trajectories");
+    CP3_CUDA(h, cudaMemcpy(h->d_seg_off.ptr, t.offset.data(), sizeof(int) * t.offset.size(),
+                           cudaMemcpyHostToDevice), "upload trajectories");
+    CP3_CUDA(h, cudaMemcpy(h->d_seg_cls.ptr, t.cls.data(), sizeof(int) * nseg,
+                           cudaMemcpyHostToDevice), "upload trajectories");
+    if (h->precision == CP3_FP64) {
+        CP3_CUDA(h, h->d_seg_len.reserve(nseg), "allocate trajectories");
+        CP3_CUDA(h, cudaMemcpy(h->d_seg_len.ptr, t.len_km.data(), sizeof(double) * nseg,
+                               cudaMemcpyHostToDevice), "upload trajectories");
+    } else {
+        std::vector<float2> df(nseg);
+        for (size_t i = 0; i < nseg; i++) {
+            const float hi = (float)t.len_km[i];
+            df[i] = make_float2(hi, (float)(t.len_km[i] - (double)hi));
+        }
+        CP3_CUDA(h, h->d_seg_len_df.reserve(nseg), "allocate trajectories");
+        CP3_CUDA(h, cudaMemcpy(h->d_seg_len_df.ptr, df.data(), sizeof(float2) * nseg,
+                               cudaMemcpyHostToDevice), "upload trajectories");
+    }
+    // density classes: 0 = air, 1 + i = shell i (getDensityOfLayer: rhos[i] * yps[i])
+    h->ncls_used = 1 + *std::max_element(t.maxlayers.begin(), t.maxlayers.end());
+    std::vector<double> cls_rho(h->ncls_used, 0.0);
+    for (int c = 1; c < h->ncls_used; c++) cls_rho[c] = h->model.rho[c - 1] * h->model.ye[c - 1];
+    CP3_CUDA(h, h->d_cls_rho.reserve(cls_rho.size()), "allocate classes");
+    CP3_CUDA(h, cudaMemcpy(h->d_cls_rho.ptr, cls_rho.data(), sizeof(double) * cls_rho.size(),
+                           cudaMemcpyHostToDevice), "upload classes");
+    const size_t cells = (size_t)h->ncls_used * pad_energies(h->ne);
+    if (h->precision == CP3_FP64)
+        CP3_CUDA(h, h->d_table64.reserve(cells * kF64Fields), "allocate eigen table");
+    else
+        CP3_CUDA(h, h->d_table32.reserve(cells * kMixFields), "allocate eigen table");
+    h->traj_dirty = false;
+    return CP3_OK;
+}
+
+int launch(cp3_propagator* h, int type, cudaStream_t s) {
+    if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
+        return fail(h, CP3_ERR_BAD_ARGUMENT, "neutrino type must be Neutrino or Antineutrino");
+    if (!h->energies_set) return fail(h, CP3_ERR_NOT_SET, "energy list was not set");
+    if (!h->mns_set) return fail(h, CP3_ERR_NOT_SET, "mixing matrix was not set (setMNSMatrix)");
+    if (!h->masses_set)
+        return fail(h, CP3_ERR_NOT_SET, "mass differences were not set (setNeutrinoMasses)");
+    CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    OscParams p;
+    build_osc_params(h->mix, type == CP3_ANTINEUTRINO, &p);
+    cudaError_t e = cudaSuccess;
+    if (h->kind == 0) {
+        if (!h->model_set) return fail(h, CP3_ERR_NOT_SET, "density model was not set");
+        if (!h->height_set)
+            return fail(h, CP3_ERR_NOT_SET,
+                        "CudaPropagatorSingle::calculateProbabilities. production height was not set");
+        if (h->avg_bins > 0)
+            return fail(h, CP3_ERR_UNSUPPORTED,
+                        "production-height averaging is computed by the oracle only in this build");
+        if (h->model.poly)
+            return fail(h, CP3_ERR_UNSUPPORTED, "polynomial density model not yet on the GPU path");
+        int rc = prepare_atmos(h);
+        if (rc) return rc;
+        if (h->precision == CP3_FP64) {
+            e = launch_table_f64(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
+                                 h->d_table64.ptr, s);
+            if (e == cudaSuccess)
+                e = launch_atmos_f64(p, h->d_energies.ptr, h->ne, h->d_table64.ptr,
+                                     h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
+                                     (double*)h->d_result.ptr, s);
+        } else {
+            e = launch_table_mixed(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
+                                   h->d_table32.ptr, s);
+            if (e == cudaSuccess)
+                e = launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
+                                       h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc,
+                                       (float*)h->d_result.ptr, s);
+        }
+    } else {
+        if (!h->beam_rho_set) return fail(h, CP3_ERR_NOT_SET, "beam density was not set");
+        if (!h->beam_L_set) return fail(h, CP3_ERR_NOT_SET, "beam path length was not set");
+        // calculate_beam passes density * density_convert() (physics.hpp:1217-1223)
+        const double rho_e = h->beam_rho * kDensityConvert;
+        if (h->precision == CP3_FP64)
+            e = launch_beam_f64(p, h->d_energies.ptr, h->ne, rho_e, h->beam_L,
+                                (double*)h->d_result.ptr, s);
+        else
+            e = launch_beam_mixed(p, h->d_energies.ptr, h->ne, rho_e, h->beam_L,
+                                  (float*)h->d_result.ptr, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
+    h->result_on_host = false;
+    h->computed = true;
+    return CP3_OK;
+}
+
+int fetch_result(cp3_propagator* h) {
+    if (!h->computed) return fail(h, CP3_ERR_NOT_SET, "no probabilities computed yet");
+    if (h->result_on_host) return CP3_OK;
+    const size_t n = h->result_bytes / (h->precision == CP3_FP64 ? 8 : 4);
+    if (!h->h_result) CP3_CUDA(h, cudaMallocHost(&h->h_result, n * sizeof(double)), "pinned result");
+    CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    CP3_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
+    if (h->precision == CP3_FP64) {
+        CP3_CUDA(h, cudaMemcpy(h->h_result, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost),
+                 "copy result");
+    } else {
+        // floats land in the second half of the pinned buffer, then widen in place (forward
+        // order never overwrites an unread float: float i sits at byte 4*(n+i) >= 8*i).
+        float* f = reinterpret_cast<float*>(h->h_result) + n;
+        CP3_CUDA(h, cudaMemcpy(f, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost),
+                 "copy result");
+        for (size_t i = 0; i < n; i++) h->h_result[i] = (double)f[i];
+    }
+    h->result_on_host = true;
+    return CP3_OK;
+}
+
+int check_type(cp3_propagator* h, int t) {
+    if (t < 0 || t > 8) return fail(h, CP3_ERR_BAD_ARGUMENT, "ProbType must be in 0..8");
+    return CP3_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp3_atmos_create(int device, int n_cosines, int n_energies, int precision, cp3_propagator** out) {
+    return create(0, device, n_cosines, n_energies, precision, out);
+}
+
+int cp3_beam_create(int device, int n_energies, int precision, cp3_propagator** out) {
+    return create(1, device, 1, n_energies, precision, out);
+}
+
+int cp3_destroy(cp3_propagator* h) {
+    if (!h) return CP3_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+    return CP3_OK;
+}
+
+const char* cp3_last_error(const cp3_propagator* h) {
+    return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int cp3_get_info(const cp3_propagator* h, int* kind, int* precision, int* n_cosines, int* n_energies) {
+    if (!h) return fail(nullptr, CP3_ERR_BAD_ARGUMENT, "null propagator handle");
+    if (kind) *kind = h->kind;
+    if (precision) *precision = h->precision;
+    if (n_cosines) *n_cosines = h->kind == 0 ? h->nc : 0;
+    if (n_energies) *n_energies = h->ne;
+    return CP3_OK;
+}
+
+int cp3_set_energies(cp3_propagator* h, const double* energies, int n) {
+    if (int rc = check_handle(h)) return rc;
+    if (n != h->ne || !energies)
+        return fail(h, CP3_ERR_BAD_SIZE,
+                    "Propagator::setEnergyList. Propagator was not created for this number of energy nodes");
+    h->energies.assign(energies, energies + n);
+    CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    CP3_CUDA(h, cudaMemcpy(h->d_energies.ptr, energies, sizeof(double) * n, cudaMemcpyHostToDevice),
+             "upload energies");
+    h->energies_set = true;
+    return CP3_OK;
+}
+
+int cp3_set_cosines(cp3_propagator* h, const double* cosines, int n) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 0) return fail(h, CP3_ERR_UNSUPPORTED, "beam propagators have no cosine list");
+    if (n != h->nc || !cosines)
+        return fail(h, CP3_ERR_BAD_SIZE,
+                    "Propagator::setCosineList. Propagator was not created for this number of cosine nodes");
+    if (h->model_set) {  // setMaxlayers runs on every cosine change (atmoscpupropagator.hpp:378)
+        for (int i = 0; i < n; i++)
+            if (count_shells(h->model, cosines[i]) > kMaxShells)
+                return fail(h, CP3_ERR_LAYER_LIMIT, "setMaxlayers : invalid number of maxLayer");
+    }
+    h->cosines.assign(cosines, cosines + n);
+    h->cosines_set = true;
+    h->traj_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_mns(cp3_propagator* h, double t12, double t13, double t23, double dcp, int knutype) {
+    if (int rc = check_handle(h)) return rc;
+    h->mix.theta12 = t12;
+    h->mix.theta13 = t13;
+    h->mix.theta23 = t23;
+    h->mix.dcp = dcp;
+    h->mix.knutype = knutype;
+    h->mns_set = true;
+    return CP3_OK;
+}
+
+int cp3_set_masses(cp3_propagator* h, double dm12sq, double dm23sq) {
+    if (int rc = check_handle(h)) return rc;
+    h->mix.dm12sq = dm12sq;
+    h->mix.dm23sq = dm23sq;
+    h->masses_set = true;
+    return CP3_OK;
+}
+
+static int set_model(cp3_propagator* h, const double* radii, const double* c1, const double* c2,
+                     const double* c3, const double* ye, int n, bool poly) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 0)
+        return fail(h, CP3_ERR_UNSUPPORTED,
+                    "beam propagators take setDensity(rho) and setPathLength(L)");
+    EarthModel m;
+    std::string msg;
+    int rc = make_earth_model(radii, c1, c2, c3, ye, n, poly, &m, &msg);
+    if (rc) return fail(h, rc, msg);
+    if (h->cosines_set)
+        for (double c : h->cosines)
+            if (count_shells(m, c) > kMaxShells)
+                return fail(h, CP3_ERR_LAYER_LIMIT, "setMaxlayers : invalid number of maxLayer");
+    h->model = std::move(m);
+    h->model_set = true;
+    h->traj_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_layers(cp3_propagator* h, const double* radii, const double* rho, const double* ye, int n) {
+    return set_model(h, radii, rho, nullptr, nullptr, ye, n, false);
+}
+
+int cp3_set_layers_poly(cp3_propagator* h, const double* radii, const double* a, const double* b,
+                        const double* c, const double* ye, int n) {
+    return set_model(h, radii, a, b, c, ye, n, true);
+}
+
+int cp3_set_density_file(cp3_propagator* h, const char* path, double ye_core, double ye_mantle) {
+    if (int rc = check_handle(h)) return rc;
+    if (!path) return fail(h, CP3_ERR_BAD_ARGUMENT, "null path");
+    int ncols = 0;
+    std::vector<std::vector<double>> cols;
+    std::string msg;
+    int rc = parse_model_file(path, &ncols, &cols, &msg);
+    if (rc) return fail(h, rc, msg);
+    const int n = (int)cols[0].size();
+    if (ncols == 2) {
+        std::vector<double> ye(n);
+        for (int i = 0; i < n; i++) ye[i] = cols[0][i] <= 3480.0 ? ye_core : ye_mantle;
+        return set_model(h, cols[0].data(), cols[1].data(), nullptr, nullptr, ye.data(), n, false);
+    }
+    if (ncols == 3) return set_model(h, cols[0].data(), cols[1].data(), nullptr, nullptr, cols[2].data(), n, false);
+    return set_model(h, cols[0].data(), cols[1].data(), cols[2].data(), cols[3].data(), cols[4].data(), n, true);
+}
+
+int cp3_set_chemical_composition(cp3_propagator* h, const double* ye, int n) {
+    if (int rc = check_handle(h)) return rc;
+    if (!h->model_set || !ye || (size_t)n != h->model.ye.size())
+        return fail(h, CP3_ERR_BAD_SIZE,
+                    "CpuPropagator::setChemicalComposition. Size of input list not equal to expectation.");
+    // The reference overwrites yps in its internal (descending) order.
+    h->model.ye.assign(ye, ye + n);
+    h->traj_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_production_height(cp3_propagator* h, double km) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 0) return fail(h, CP3_ERR_UNSUPPORTED, "beam propagators have no production height");
+    if (!h->cosines_set) return fail(h, CP3_ERR_NOT_SET, "must set cosine list before production height");
+    h->height_cm = km * 100000.0;
+    h->height_set = true;
+    h->traj_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_beam_density(cp3_propagator* h, double rho) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 1) {
+        // AtmosCpuPropagator::setDensity(rho) is a printing dummy (atmoscpupropagator.hpp:347-358)
+        return fail(h, CP3_ERR_UNSUPPORTED,
+                    "DUMMY FUNCTION: ATMOS class uses setDensity(radii, rhos, yps) or setDensityFromFile");
+    }
+    h->beam_rho = rho;
+    h->beam_rho_set = true;
+    return CP3_OK;
+}
+
+int cp3_set_beam_path_length(cp3_propagator* h, double km) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 1)
+        return fail(h, CP3_ERR_UNSUPPORTED, "DUMMY FUNCTION - ATMOS class calculates PATH LENGTH");
+    h->beam_L = km;
+    h->beam_L_set = true;
+    return CP3_OK;
+}
+
+int cp3_set_production_height_averaging(cp3_propagator* h, int n_bins, const double* prob,
+                                        const double* edges_km) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 0) return fail(h, CP3_ERR_UNSUPPORTED, "beam propagators have no production height");
+    if (n_bins < 0 || n_bins > kMaxProdHeightBins)
+        return fail(h, CP3_ERR_BAD_ARGUMENT,
+                    "SetNumberOfProductionHeightBinsForAveraging : invalid number of production height bins");
+    if (n_bins == 0) {
+        h->avg_bins = 0;
+        return CP3_OK;
+    }
+    if (!prob || !edges_km) return fail(h, CP3_ERR_BAD_ARGUMENT, "null production-height arrays");
+    const size_t np = (size_t)n_bins * 2 * 3 * h->ne * h->nc;
+    h->avg_prob.assign(prob, prob + np);
+    h->avg_edges.assign(edges_km, edges_km + n_bins + 1);
+    h->avg_bins = n_bins;
+    return CP3_OK;
+}
+
+int cp3_calculate(cp3_propagator* h, int type) {
+    if (int rc = check_handle(h)) return rc;
+    int rc = launch(h, type, h->stream);
+    if (rc) return rc;
+    CP3_CUDA(h, cudaStreamSynchronize(h->stream), "waitForCompletion");
+    return CP3_OK;
+}
+
+int cp3_calculate_async(cp3_propagator* h, int type, void* stream) {
+    if (int rc = check_handle(h)) return rc;
+    return launch(h, type, stream ? (cudaStream_t)stream : h->stream);
+}
+
+int cp3_synchronize(cp3_propagator* h) {
+    if (int rc = check_handle(h)) return rc;
+    CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    CP3_CUDA(h, cudaStreamSynchronize(h->stream), "waitForCompletion");
+    return CP3_OK;
+}
+
+int cp3_get_probability(cp3_propagator* h, int ic, int ie, int t, double* out) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 0) return fail(h, CP3_ERR_UNSUPPORTED, "use cp3_get_probability_beam for beam propagators");
+    if (int rc = check_type(h, t)) return rc;
+    if (ic < 0 || ie < 0 || ic >= h->nc || ie >= h->ne)
+        return fail(h, CP3_ERR_INDEX, "CudaPropagatorSingle::getProbability. Invalid indices");
+    if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    if (int rc = fetch_result(h)) return rc;
+    *out = h->h_result[((size_t)t * h->nc + ic) * h->ne + ie];
+    return CP3_OK;
+}
+
+int cp3_get_probability_beam(cp3_propagator* h, int ie, int t, double* out) {
+    if (int rc = check_handle(h)) return rc;
+    if (h->kind != 1) return fail(h, CP3_ERR_UNSUPPORTED, "use cp3_get_probability for atmospheric propagators");
+    if (int rc = check_type(h, t)) return rc;
+    if (ie < 0 || ie >= h->ne)
+        return fail(h, CP3_ERR_INDEX, "CudaPropagatorSingle::getProbability. Invalid indices");
+    if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    if (int rc = fetch_result(h)) return rc;
+    *out = h->h_result[(size_t)t * h->ne + ie];
+    return CP3_OK;
+}
+
+int cp3_get_probability_arr(cp3_propagator* h, int t, double* out) {
+    if (int rc = check_handle(h)) return rc;
+    if (int rc = check_type(h, t)) return rc;
+    if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    if (int rc = fetch_result(h)) return rc;
+    const double* plane = h->h_result + (size_t)t * h->nc * h->ne;
+    size_t it = 0;
+    for (int ie = 0; ie < h->ne; ie++)
+        for (int ic = 0; ic < h->nc; ic++) out[it++] = plane[(size_t)ic * h->ne + ie];
+    return CP3_OK;
+}
+
+int cp3_device_result(cp3_propagator* h, const void** ptr, int* is_float, size_t* bytes) {
+    if (int rc = check_handle(h)) return rc;
+    if (ptr) *ptr = h->d_result.ptr;
+    if (is_float) *is_float = h->precision == CP3_MIXED;
+    if (bytes) *bytes = h->result_bytes;
+    return CP3_OK;
+}
+
+int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream) {
+    if (int rc = check_handle(h)) return rc;
+    if (!dst) return fail(h, CP3_ERR_BAD_ARGUMENT, "null destination");
+    CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    CP3_CUDA(h, cudaMemcpyAsync(dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost,
+                                stream ? (cudaStream_t)stream : h->stream),
+             "copy result");
+    return CP3_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,391 @@
+// cp3_atmos.cu -- per-bin kernels: atmospheric FP64 and mixed, beam mixed.
+//
+// Mapping: one CTA = one cosine row x a tile of kBlock consecutive energies, one thread =
+// one (cosine, energy) bin.  The row's trajectory (segment lengths and density classes,
+// a few hundred bytes) is staged in shared memory; every thread of the CTA then walks the
+// same segment list, so control flow is uniform.  The per-(class, energy) eigen tables are
+// read with unit stride across a warp (SoA layout) and stay L2-resident.  The result
+// [9][n_cosines][n_energies] is written one channel plane at a time: each warp store is
+// 32 consecutive elements (128 B in FP32, 256 B in FP64).
+#include "cp3_device.cuh"
+#include "cp3_kernels.hpp"
+
+namespace cp3 {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kMaxGridY = 65535;
+
+// ------------------------------------------------------------------------------------
+// FP64: physics::calculate_atmos (physics.hpp:789-1150) for the fixed production height.
+
+struct cm3 {
+    cd a[3][3];
+};
+
+__device__ __forceinline__ void mul3(const cm3& A, const cm3& B, cm3& R) {
+    // math::multiply_complex_matrix (math.hpp:84-96): R = A . B, summed over k in order.
+    cm3 t;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            double re = 0.0, im = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                re += A.a[i][k].re * B.a[k][j].re - A.a[i][k].im * B.a[k][j].im;
+                im += A.a[i][k].im * B.a[k][j].re + A.a[i][k].re * B.a[k][j].im;
+            }
+            t.a[i][j] = cd{re, im};
+        }
+    R = t;
+}
+
+// T = sum_k e^{i arg_k} C_k for one segment (multiply_phase_matrix, math.hpp:59-75), with
+// arg_k = -2.534 dmMatVac[k][0] L / E evaluated as in getArg (physics.hpp:439-450).
+__device__ __forceinline__ void segment_matrix_f64(const double* __restrict__ t, int ne_pad,
+                                                   double L, double E, cm3& T) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) T.a[i][j] = cd{0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double dmv = __ldg(t + (size_t)(54 + k) * ne_pad);
+        double s, c;
+        sincos(-kLoEFac * dmv * L / E, &s, &c);
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const double re = __ldg(t + (size_t)((k * 9 + q) * 2) * ne_pad);
+            const double im = __ldg(t + (size_t)((k * 9 + q) * 2 + 1) * ne_pad);
+            T.a[q / 3][q % 3].re += c * re - s * im;
+            T.a[q / 3][q % 3].im += c * im + s * re;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    atmos_f64_kernel(const double* __restrict__ energies, int ne, int ne_pad,
+                     const double* __restrict__ table, const int* __restrict__ seg_off,
+                     const double* __restrict__ seg_len, const int* __restrict__ seg_cls,
+                     int ic0, int nc, double* __restrict__ out) {
+    __shared__ double s_len[kMaxSegments];
+    __shared__ int s_cls[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) {
+        s_len[i] = seg_len[s0 + i];
+        s_cls[i] = seg_cls[s0 + i];
+    }
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const double E = energies[ie];
+    const size_t cls_stride = (size_t)kF64Fields * ne_pad;
+    const double* tab = table + ie;
+    const int M = nseg - 1;
+
+    cm3 fin, mantle, T;
+    segment_matrix_f64(tab + s_cls[0] * cls_stride, ne_pad, s_len[0], E, fin);
+    for (int l = 1; l <= M; l++) {
+        segment_matrix_f64(tab + s_cls[l] * cls_stride, ne_pad, s_len[l], E, T);
+        mul3(T, fin, fin);
+        if (l < M) {
+            if (l == 1)
+                mantle = T;  // identity . T is exact
+            else
+                mul3(mantle, T, mantle);
+        }
+    }
+    if (M >= 2) mul3(mantle, fin, fin);
+
+    // Probabilities as physics.hpp:1102-1130 with no averaging: Product_k = fin . C_atm[k],
+    // Prob = sum_k |Product_k|^2 + 2 sum_{q<k} Re(Product_q conj Product_k).
+    const double* ta = tab + s_cls[0] * cls_stride;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            cd P[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                double re = 0.0, im = 0.0;
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    const double cre = __ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2) * ne_pad);
+                    const double cim = __ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2 + 1) * ne_pad);
+                    re += fin.a[i][q].re * cre - fin.a[i][q].im * cim;
+                    im += fin.a[i][q].im * cre + fin.a[i][q].re * cim;
+                }
+                P[k] = cd{re, im};
+            }
+            double prob = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                prob += P[k].re * P[k].re + P[k].im * P[k].im;
+#pragma unroll
+                for (int q = 0; q < k; q++)
+                    prob += 2. * P[q].re * P[k].re + 2. * P[q].im * P[k].im;  // shift = 1 + 0i
+            }
+            // Prob[i][j] (i final, j initial) is P(j -> i): channel j*3+i.
+            out[((size_t)(j * 3 + i) * nc + ic) * ne + ie] = prob;
+        }
+}
+
+// ------------------------------------------------------------------------------------
+// Mixed: the same physics, rearranged for FP32.
+//   T_l = W S_l W^+,  S_l = 1 + z1 P1 + z2 P2,  z_k = e^{-i omega_k L_l} - 1   (symmetric)
+//   A   = W (S_1..S_{M-1}) S_M (S_{M-1}..S_1) S_0 W^+ = W (B^T S_M B) S_0 W^+,
+// with B = S_{M-1}..S_1, because S_l^T = S_l.  That is M+1 complex 3x3 products per bin
+// instead of the reference's 2M-1, on symmetric factors.
+
+struct cs6 {  // complex symmetric 3x3
+    cf a[6];
+};
+struct cg9 {  // complex general 3x3
+    cf a[3][3];
+};
+
+__device__ __forceinline__ void segment_matrix_mixed(const float* __restrict__ t, int ne_pad,
+                                                     float2 L, cs6& S) {
+    float z[2][2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float wh = __ldg(t + (size_t)(12 + 2 * k) * ne_pad);
+        const float wl = __ldg(t + (size_t)(13 + 2 * k) * ne_pad);
+        const float r = reduced_phase(wh, wl, L.x, L.y);
+        float sh, ch;
+        sincosf(0.5f * r, &sh, &ch);
+        z[k][0] = -2.0f * sh * sh;  // cos r - 1
+        z[k][1] = -2.0f * sh * ch;  // -sin r
+    }
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const float p1 = __ldg(t + (size_t)q * ne_pad);
+        const float p2 = __ldg(t + (size_t)(6 + q) * ne_pad);
+        const float one = (q == 0 || q == 3 || q == 5) ? 1.0f : 0.0f;
+        S.a[q].re = fmaf(z[1][0], p2, fmaf(z[0][0], p1, one));
+        S.a[q].im = fmaf(z[1][1], p2, z[0][1] * p1);
+    }
+}
+
+// R = S . G (S symmetric)
+__device__ __forceinline__ void mul_sg(const cs6& S, const cg9& G, cg9& R) {
+    cg9 t;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            cf acc = cmulf(S.a[sidx(i, 0)], G.a[0][j]);
+#pragma unroll
+            for (int k = 1; k < 3; k++) {
+                const cf s = S.a[sidx(i, k)], g = G.a[k][j];
+                acc.re = fmaf(s.re, g.re, fmaf(-s.im, g.im, acc.re));
+                acc.im = fmaf(s.re, g.im, fmaf(s.im, g.re, acc.im));
+            }
+            t.a[i][j] = acc;
+        }
+    R = t;
+}
+
+// R = G . S (S symmetric)
+__device__ __forceinline__ void mul_gs(const cg9& G, const cs6& S, cg9& R) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            cf acc = cmulf(G.a[i][0], S.a[sidx(0, j)]);
+#pragma unroll
+            for (int k = 1; k < 3; k++) {
+                const cf g = G.a[i][k], s = S.a[sidx(k, j)];
+                acc.re = fmaf(g.re, s.re, fmaf(-g.im, s.im, acc.re));
+                acc.im = fmaf(g.re, s.im, fmaf(g.im, s.re, acc.im));
+            }
+            R.a[i][j] = acc;
+        }
+}
+
+__device__ __forceinline__ void sym_to_gen(const cs6& S, cg9& G) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) G.a[i][j] = S.a[sidx(i, j)];
+}
+
+// Probabilities of A = W A2 W^+, W = [[1,0,0],[0,c,s e],[0,-s,c e]], e = e^{i d}; stores
+// channel a*3+b = |A[b][a]|^2 at out[ch * plane].
+__device__ __forceinline__ void store_probabilities(const cg9& A2, float c, float s, float ed_re,
+                                                    float ed_im, float* __restrict__ out,
+                                                    size_t plane) {
+    cg9 Y;  // Y = A2 W^+ : columns 1, 2 mix through (c, -s) and e* (s, c)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const cf a1 = A2.a[i][1], a2 = A2.a[i][2];
+        const cf f{a2.re * ed_re + a2.im * ed_im, a2.im * ed_re - a2.re * ed_im};  // e* a2
+        Y.a[i][0] = A2.a[i][0];
+        Y.a[i][1] = cf{fmaf(c, a1.re, s * f.re), fmaf(c, a1.im, s * f.im)};
+        Y.a[i][2] = cf{fmaf(-s, a1.re, c * f.re), fmaf(-s, a1.im, c * f.im)};
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const cf y1 = Y.a[1][j], y2 = Y.a[2][j];
+        const cf g{y2.re * ed_re - y2.im * ed_im, y2.re * ed_im + y2.im * ed_re};  // e y2
+        const cf r0 = Y.a[0][j];
+        const cf r1{fmaf(c, y1.re, s * g.re), fmaf(c, y1.im, s * g.im)};
+        const cf r2{fmaf(-s, y1.re, c * g.re), fmaf(-s, y1.im, c * g.im)};
+        // column j = initial flavour j; rows 0..2 = final flavours
+        out[(size_t)(j * 3 + 0) * plane] = fmaf(r0.re, r0.re, r0.im * r0.im);
+        out[(size_t)(j * 3 + 1) * plane] = fmaf(r1.re, r1.re, r1.im * r1.im);
+        out[(size_t)(j * 3 + 2) * plane] = fmaf(r2.re, r2.re, r2.im * r2.im);
+    }
+}
+
+struct WParams {
+    float c, s, er, ei;
+};
+
+__global__ void __launch_bounds__(kBlock)
+    atmos_mixed_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
+                       const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
+                       const int* __restrict__ seg_cls, int ic0, int nc, float* __restrict__ out) {
+    __shared__ float2 s_len[kMaxSegments];
+    __shared__ int s_cls[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) {
+        s_len[i] = seg_len[s0 + i];
+        s_cls[i] = seg_cls[s0 + i];
+    }
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const size_t cls_stride = (size_t)kMixFields * ne_pad;
+    const float* tab = table + ie;
+    const int M = nseg - 1;
+
+    cs6 S0;
+    segment_matrix_mixed(tab + s_cls[0] * cls_stride, ne_pad, s_len[0], S0);
+    cg9 A2;
+    if (M == 0) {
+        sym_to_gen(S0, A2);
+    } else {
+        cs6 S;
+        cg9 B;
+        if (M == 1) {
+            segment_matrix_mixed(tab + s_cls[1] * cls_stride, ne_pad, s_len[1], S);
+            sym_to_gen(S, B);  // B = S_1, Q = S_1
+            mul_gs(B, S0, A2);
+        } else {
+            segment_matrix_mixed(tab + s_cls[1] * cls_stride, ne_pad, s_len[1], S);
+            sym_to_gen(S, B);
+            for (int l = 2; l < M; l++) {
+                segment_matrix_mixed(tab + s_cls[l] * cls_stride, ne_pad, s_len[l], S);
+                mul_sg(S, B, B);
+            }
+            segment_matrix_mixed(tab + s_cls[M] * cls_stride, ne_pad, s_len[M], S);
+            cg9 X;
+            mul_sg(S, B, X);  // X = S_M B
+            cs6 Q;            // Q = B^T X (symmetric)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = i; j < 3; j++) {
+                    cf acc = cmulf(B.a[0][i], X.a[0][j]);
+#pragma unroll
+                    for (int k = 1; k < 3; k++) {
+                        const cf b = B.a[k][i], x = X.a[k][j];
+                        acc.re = fmaf(b.re, x.re, fmaf(-b.im, x.im, acc.re));
+                        acc.im = fmaf(b.re, x.im, fmaf(b.im, x.re, acc.im));
+                    }
+                    Q.a[sidx(i, j)] = acc;
+                }
+            sym_to_gen(Q, B);
+            mul_gs(B, S0, A2);
+        }
+    }
+    const size_t plane = (size_t)nc * ne;
+    store_probabilities(A2, w.c, w.s, w.er, w.ei, out + (size_t)ic * ne + ie, plane);
+}
+
+// Beam, mixed: per-bin FP64 eigen-decomposition, FP64 phase reduction, FP32 matrix work.
+__global__ void __launch_bounds__(kBlock)
+    beam_mixed_kernel(const __grid_constant__ OscParams p, WParams w,
+                      const double* __restrict__ energies, int ne, double rho_e, double L,
+                      float* __restrict__ out) {
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    double P[2][6], om[2];
+    rotated_eigen_f64(&p, energies[ie], rho_e, P, om);
+    float z[2][2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const double x = om[k] * L;
+        const double n = rint(x * (1.0 / (2.0 * M_PI)));
+        // 2 pi = 6.283185307179586 + 2.4492935982947064e-16 (double-double)
+        const float r = (float)fma(-n, 2.4492935982947064e-16, fma(-n, 6.283185307179586, x));
+        float sh, ch;
+        sincosf(0.5f * r, &sh, &ch);
+        z[k][0] = -2.0f * sh * sh;
+        z[k][1] = -2.0f * sh * ch;
+    }
+    cs6 S;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const float p1 = (float)P[0][q], p2 = (float)P[1][q];
+        const float one = (q == 0 || q == 3 || q == 5) ? 1.0f : 0.0f;
+        S.a[q].re = fmaf(z[1][0], p2, fmaf(z[0][0], p1, one));
+        S.a[q].im = fmaf(z[1][1], p2, z[0][1] * p1);
+    }
+    cg9 A2;
+    sym_to_gen(S, A2);
+    store_probabilities(A2, w.c, w.s, w.er, w.ei, out + ie, (size_t)ne);
+}
+
+WParams wparams(const OscParams& p) {
+    return WParams{(float)p.w[0], (float)p.w[1], (float)p.w[2], (float)p.w[3]};
+}
+
+}  // namespace
+
+cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
+                             const double* table, const int* seg_off, const double* seg_len,
+                             const int* seg_cls, int n_cosines, double* out, cudaStream_t s) {
+    (void)p;
+    if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
+    const int ne_pad = pad_energies(ne);
+    for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
+        const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
+        dim3 grid((ne + kBlock - 1) / kBlock, rows);
+        atmos_f64_kernel<<<grid, kBlock, 0, s>>>(energies, ne, ne_pad, table, seg_off, seg_len,
+                                                 seg_cls, ic0, n_cosines, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
+                               const int* seg_off, const float2* seg_len, const int* seg_cls,
+                               int n_cosines, float* out, cudaStream_t s) {
+    if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
+    const int ne_pad = pad_energies(ne);
+    const WParams w = wparams(p);
+    for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
+        const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
+        dim3 grid((ne + kBlock - 1) / kBlock, rows);
+        atmos_mixed_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
+                                                   seg_cls, ic0, n_cosines, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_beam_mixed(const OscParams& p, const double* energies, int ne, double rho_e,
+                              double L_km, float* out, cudaStream_t s) {
+    if (ne <= 0) return cudaSuccess;
+    beam_mixed_kernel<<<(ne + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, wparams(p), energies, ne,
+                                                                    rho_e, L_km, out);
+    return cudaGetLastError();
+}
+
+}  // namespace cp3

@@ -1,0 +1,320 @@
+// cp3_device.cuh -- device building blocks shared by the kernels.
+//
+// Part 1 (FP64, reference-faithful): the matter eigenvalues, spectral products and
+// flavour-basis projectors of physics.hpp, in the reference's evaluation order.  Used by
+// the FP64 tables/kernels and by the FP64 eigen-decomposition of the mixed tables.
+// Part 2 (mixed): double-float phase products and range reduction, complex float helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "cp3_types.h"
+
+namespace cp3 {
+
+struct cd {
+    double re, im;
+};
+struct cf {
+    float re, im;
+};
+
+#define CP3_U(p, i, j) (cd{(p)->U[((i)*3 + (j)) * 2], (p)->U[((i)*3 + (j)) * 2 + 1]})
+#define CP3_DM(p, i, j) ((p)->dm[(i)*3 + (j)])
+
+// physics::getMfast (physics.hpp:267-340): matter eigenvalues of 2E.H (eV^2), ordered by the
+// vacuum root order.  Returns mm[i]; the reference's dmMatVac[i][j] = mm[i] - DM(j,0) and
+// dmMatMat[i][j] = mm[i] - mm[j].
+__device__ __forceinline__ void matter_masses_f64(const OscParams* __restrict__ p, double E,
+                                                  double rho, double mm[3]) {
+    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
+    const double d01 = CP3_DM(p, 0, 1), d02 = CP3_DM(p, 0, 2);
+    const cd u00 = CP3_U(p, 0, 0), u01 = CP3_U(p, 0, 1), u02 = CP3_U(p, 0, 2);
+    const double alpha = fac + d01 + d02;
+    const double beta = d01 * d02 + fac * (d01 * (1.0 - u01.re * u01.re - u01.im * u01.im) +
+                                           d02 * (1.0 - u02.re * u02.re - u02.im * u02.im));
+    const double gamma = fac * d01 * d02 * (u00.re * u00.re + u00.im * u00.im);
+    const double tmp = alpha * alpha - 3.0 * beta < 0 ? 0 : alpha * alpha - 3.0 * beta;
+    const double argtmp = (2.0 * alpha * alpha * alpha - 9.0 * alpha * beta + 27.0 * gamma) /
+                          (2.0 * sqrt(tmp * tmp * tmp));
+    const double arg = fabs(argtmp) > 1.0 ? argtmp / fabs(argtmp) : argtmp;
+    const double th0 = acos(arg) / 3.0;
+    const double th1 = th0 - (2.0 * M_PI / 3.0);
+    const double th2 = th0 + (2.0 * M_PI / 3.0);
+    double r[3];
+    r[0] = -(2.0 / 3.0) * sqrt(tmp);
+    r[1] = -(2.0 / 3.0) * sqrt(tmp);
+    r[2] = -(2.0 / 3.0) * sqrt(tmp);
+    r[0] *= cos(th0);
+    r[1] *= cos(th1);
+    r[2] *= cos(th2);
+    const double shift = CP3_DM(p, 0, 0) - alpha / 3.0;
+    r[0] += shift;
+    r[1] += shift;
+    r[2] += shift;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int o = p->order[i];
+        mm[i] = o == 0 ? r[0] : (o == 1 ? r[1] : r[2]);
+    }
+}
+
+// physics::get_product (physics.hpp:345-430) + getC (:459-514): the flavour-basis projectors
+// C[k][a][b] of the expansion T = sum_k C_k exp(i arg_k).
+__device__ __forceinline__ void flavour_projectors_f64(const OscParams* __restrict__ p, double E,
+                                                       double rho, const double mm[3],
+                                                       cd C[3][3][3]) {
+    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
+    double dMV[3][3], dMM[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            dMM[i][j] = mm[i] - mm[j];
+            dMV[i][j] = mm[i] - CP3_DM(p, j, 0);
+        }
+    cd h[3][3][3];
+#pragma unroll
+    for (int n = 0; n < 3; n++)
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            const cd a = CP3_U(p, 0, n), b = CP3_U(p, 0, m);
+            const double re = -fac * (a.re * b.re + a.im * b.im);
+            const double im = -fac * (a.re * b.im - a.im * b.re);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                h[n][m][j].re = re;
+                h[n][m][j].im = im;
+            }
+        }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        h[0][0][j].re -= dMV[j][0];
+        h[1][1][j].re -= dMV[j][1];
+        h[2][2][j].re -= dMV[j][2];
+    }
+    const double den[3] = {dMM[0][1] * dMM[0][2], dMM[1][2] * dMM[1][0], dMM[2][0] * dMM[2][1]};
+    cd prod[3][3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) prod[i][j][k] = cd{0.0, 0.0};
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const int f = (k + 1) % 3, s = (k + 2) % 3;
+                    const cd x = h[i][q][f], y = h[q][j][s];
+                    prod[i][j][k].re += x.re * y.re - x.im * y.im;
+                    prod[i][j][k].im += x.re * y.im + x.im * y.re;
+                }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                prod[i][j][k].re /= den[k];
+                prod[i][j][k].im /= den[k];
+            }
+        }
+    // getC: C_k = U . prod_k . U^dagger, accumulated as RR/RI/IR/II partial sums.
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            double RR[3] = {0, 0, 0}, RI[3] = {0, 0, 0}, IR[3] = {0, 0, 0}, II[3] = {0, 0, 0};
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const cd u = CP3_U(p, a, i);
+                    RR[j] += u.re * prod[i][j][k].re;
+                    RI[j] += u.re * prod[i][j][k].im;
+                    IR[j] += u.im * prod[i][j][k].re;
+                    II[j] += u.im * prod[i][j][k].im;
+                }
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                double re = 0., im = 0.;
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const cd u = CP3_U(p, b, j);
+                    re += RR[j] * u.re;
+                    re += RI[j] * u.im;
+                    re += IR[j] * u.im;
+                    re -= II[j] * u.re;
+                    im += II[j] * u.im;
+                    im += IR[j] * u.re;
+                    im += RI[j] * u.re;
+                    im -= RR[j] * u.im;
+                }
+                C[k][a][b] = cd{re, im};
+            }
+        }
+}
+
+// physics::get_product + getA (physics.hpp:345-430, 516-598): the beam amplitude
+// A = U (sum_k e^{i arg_k} prod_k) U^dagger through AXFAC.  A[n][m]: row = final flavour.
+__device__ __forceinline__ void beam_amplitude_f64(const OscParams* __restrict__ p, double E,
+                                                   double rho, double L, cd A[3][3]) {
+    double mm[3];
+    matter_masses_f64(p, E, rho, mm);
+    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
+    double dMV[3][3], dMM[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            dMM[i][j] = mm[i] - mm[j];
+            dMV[i][j] = mm[i] - CP3_DM(p, j, 0);
+        }
+    cd h[3][3][3];
+#pragma unroll
+    for (int n = 0; n < 3; n++)
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            const cd a = CP3_U(p, 0, n), b = CP3_U(p, 0, m);
+            const double re = -fac * (a.re * b.re + a.im * b.im);
+            const double im = -fac * (a.re * b.im - a.im * b.re);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                h[n][m][j].re = re;
+                h[n][m][j].im = im;
+            }
+        }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        h[0][0][j].re -= dMV[j][0];
+        h[1][1][j].re -= dMV[j][1];
+        h[2][2][j].re -= dMV[j][2];
+    }
+    const double den[3] = {dMM[0][1] * dMM[0][2], dMM[1][2] * dMM[1][0], dMM[2][0] * dMM[2][1]};
+    double sn[3], cs[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) sincos(-kLoEFac * dMV[k][0] * L / E, &sn[k], &cs[k]);
+    cd X[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            cd pr[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) pr[k] = cd{0.0, 0.0};
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const int f = (k + 1) % 3, s = (k + 2) % 3;
+                    const cd x = h[i][q][f], y = h[q][j][s];
+                    pr[k].re += x.re * y.re - x.im * y.im;
+                    pr[k].im += x.re * y.im + x.im * y.re;
+                }
+            cd acc{0.0, 0.0};
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const double pre = pr[k].re / den[k], pim = pr[k].im / den[k];
+                acc.re += cs[k] * pre - sn[k] * pim;
+                acc.im += cs[k] * pim + sn[k] * pre;
+            }
+            X[i][j] = acc;
+        }
+#pragma unroll
+    for (int n = 0; n < 3; n++)
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            double re = 0, im = 0;
+            const double* f = &p->axfac[(n * 3 + m) * 36];
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const double* g = f + (i * 3 + j) * 4;
+                    re += g[0] * X[i][j].re + g[1] * X[i][j].im;
+                    im += g[2] * X[i][j].im + g[3] * X[i][j].re;
+                }
+            A[n][m] = cd{re, im};
+        }
+}
+
+// Index of (i, j), i <= j, in the 6-entry storage of a symmetric 3x3 matrix.
+__host__ __device__ constexpr int sidx(int i, int j) {
+    return i <= j ? (i == 0 ? j : (i == 1 ? 2 + j : 5)) : (j == 0 ? i : (j == 1 ? 2 + i : 5));
+}
+
+// Eigen-decomposition used by the mixed kernels, in FP64.  In the basis rotated by
+// W = R23 . diag(1,1,e^{i d}) the Hamiltonian 2E.H is the real symmetric H0 + V e0 e0^T
+// (V = -fac of getMfast).  Eigenvalues come from the reference cubic (matter_masses_f64,
+// same spectrum); the projectors onto the eigenvalues k = 1, 2 are
+//   P_k = (H - m_a)(H - m_b) / ((m_k - m_a)(m_k - m_b)),  {a, b} = the other two,
+// (P_0 = 1 - P_1 - P_2), and the phase rates relative to eigenvalue 0 are
+//   omega_k = 2.534 (m_k - m_0) / E   [rad / km].
+__device__ __forceinline__ void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
+                                                  double rho, double P[2][6], double om[2]) {
+    double mm[3];
+    matter_masses_f64(p, E, rho, mm);
+    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
+    double h[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) h[q] = p->h0[q];
+    h[0] -= fac;
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++) {
+        const int k = kk + 1;
+        const int a = k == 1 ? 0 : 0;
+        const int b = k == 1 ? 2 : 1;
+        double A[6], B[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            A[q] = h[q];
+            B[q] = h[q];
+        }
+        A[0] -= mm[a];
+        A[3] -= mm[a];
+        A[5] -= mm[a];
+        B[0] -= mm[b];
+        B[3] -= mm[b];
+        B[5] -= mm[b];
+        const double inv = 1.0 / ((mm[k] - mm[a]) * (mm[k] - mm[b]));
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = i; j < 3; j++) {
+                double s = 0.0;
+#pragma unroll
+                for (int m = 0; m < 3; m++) s += A[sidx(i, m)] * B[sidx(m, j)];
+                P[kk][sidx(i, j)] = s * inv;
+            }
+        om[kk] = kLoEFac * (mm[k] - mm[0]) / E;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Mixed-precision helpers.
+
+// 2*pi in three float parts: kTwoPiA has 8 significant bits so n*kTwoPiA is exact for
+// |n| < 2^16; the sum of the three equals 2*pi to ~1e-17.
+constexpr float kTwoPiA = 6.28125f;
+constexpr float kTwoPiB = 1.9353071693331003e-3f;   // float(2pi - A)
+constexpr float kTwoPiC = 1.0253376273028358e-11f;  // float(2pi - A - B)
+constexpr float kInvTwoPi = 0.15915494309189535f;
+
+// Double-float product x = (ah + al)(bh + bl) reduced to [-pi, pi] (error ~1e-9 rad for
+// |x| < 1e4).  The exact product of the leading parts comes from an FMA (Dekker/Ogita
+// TwoProduct), the cross terms are added to the error word, then Cody-Waite reduction.
+__device__ __forceinline__ float reduced_phase(float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    const float n = rintf(p * kInvTwoPi);
+    float r = fmaf(-n, kTwoPiA, p);
+    r = fmaf(-n, kTwoPiB, r);
+    r = fmaf(-n, kTwoPiC, r);
+    return r + e;
+}
+
+__device__ __forceinline__ cf cmulf(cf a, cf b) {
+    return cf{fmaf(a.re, b.re, -a.im * b.im), fmaf(a.re, b.im, a.im * b.re)};
+}
+
+}  // namespace cp3

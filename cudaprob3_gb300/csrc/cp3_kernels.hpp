@@ -1,0 +1,38 @@
+// cp3_kernels.hpp -- launch wrappers of the kernels (host-callable, no CUDA types beyond
+// cudaStream_t), shared by the C ABI and the batched driver.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cp3_types.h"
+
+namespace cp3 {
+
+// Fields of one (density class, energy) entry of the eigen tables.
+constexpr int kF64Fields = 57;  // C_k[a][b] re/im (54) + dmMatVac[k][0] (3)
+constexpr int kMixFields = 16;  // P1 (6), P2 (6) real symmetric; omega_1, omega_2 double-float
+
+inline int pad_energies(int ne) { return (ne + 31) / 32 * 32; }
+
+// Eigen tables over (class, energy): FP64 flavour projectors (reference expansion), or the
+// rotated-basis real projectors + double-float phase rates of the mixed kernels.
+cudaError_t launch_table_f64(const OscParams& p, const double* energies, int ne,
+                             const double* cls_rho, int ncls, double* table, cudaStream_t s);
+cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int ne,
+                               const double* cls_rho, int ncls, float* table, cudaStream_t s);
+
+// Atmospheric bins over a cosine range [ic0, ic0 + nrows) of an n_cosines-row result.
+cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
+                             const double* table, const int* seg_off, const double* seg_len,
+                             const int* seg_cls, int n_cosines, double* out, cudaStream_t s);
+cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
+                               const int* seg_off, const float2* seg_len, const int* seg_cls,
+                               int n_cosines, float* out, cudaStream_t s);
+
+// Beam bins: rho_e = rho * 0.5 (electron density), L in km.
+cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,
+                            double L_km, double* out, cudaStream_t s);
+cudaError_t launch_beam_mixed(const OscParams& p, const double* energies, int ne, double rho_e,
+                              double L_km, float* out, cudaStream_t s);
+
+}  // namespace cp3

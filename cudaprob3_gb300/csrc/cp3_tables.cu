@@ -1,0 +1,110 @@
+// cp3_tables.cu -- FP64 eigen work: the per-(density class, energy) tables of the
+// atmospheric kernels and the per-bin FP64 beam kernel.
+//
+// This translation unit is compiled with -fmad=false: its arithmetic is the reference's
+// (physics.hpp getMfast / get_product / getC / getA) in the reference's order, and keeping
+// multiply and add separately rounded reproduces the reference's x86 results to the last
+// bits where the eigen-system is ill-conditioned.  The table work is O(classes x energies),
+// amortised over every cosine, so the missing contraction costs nothing that matters.
+#include "cp3_device.cuh"
+#include "cp3_kernels.hpp"
+
+namespace cp3 {
+
+namespace {
+
+constexpr int kTableBlock = 128;
+
+// FP64 table: C_k (flavour basis) and dmMatVac[k][0] for T = sum_k C_k e^{i arg_k}
+// (physics.hpp:620-629 without the L-dependent phase).  SoA: field f of (class c, energy e)
+// at table[(c * kF64Fields + f) * ne_pad + e].
+__global__ void __launch_bounds__(kTableBlock)
+    table_f64_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
+                     int ne, int ne_pad, const double* __restrict__ cls_rho,
+                     double* __restrict__ table) {
+    const int ie = blockIdx.x * kTableBlock + threadIdx.x;
+    const int c = blockIdx.y;
+    if (ie >= ne) return;
+    const double E = energies[ie];
+    const double rho = cls_rho[c];
+    double mm[3];
+    matter_masses_f64(&p, E, rho, mm);
+    cd C[3][3][3];
+    flavour_projectors_f64(&p, E, rho, mm, C);
+    double* t = table + (size_t)c * kF64Fields * ne_pad + ie;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            t[(size_t)((k * 9 + q) * 2) * ne_pad] = C[k][q / 3][q % 3].re;
+            t[(size_t)((k * 9 + q) * 2 + 1) * ne_pad] = C[k][q / 3][q % 3].im;
+        }
+#pragma unroll
+    for (int k = 0; k < 3; k++) t[(size_t)(54 + k) * ne_pad] = mm[k] - p.dm[0];
+}
+
+// Mixed table: real projectors P1, P2 of H0 + V e0 e0^T and the phase rates
+// omega_k = 2.534 (m_k - m_0) / E split into float pairs.  Field layout as above with
+// kMixFields: 0-5 P1, 6-11 P2 (00,01,02,11,12,22), 12/13 omega_1 hi/lo, 14/15 omega_2.
+__global__ void __launch_bounds__(kTableBlock)
+    table_mixed_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
+                       int ne, int ne_pad, const double* __restrict__ cls_rho,
+                       float* __restrict__ table) {
+    const int ie = blockIdx.x * kTableBlock + threadIdx.x;
+    const int c = blockIdx.y;
+    if (ie >= ne) return;
+    double P[2][6], om[2];
+    rotated_eigen_f64(&p, energies[ie], cls_rho[c], P, om);
+    float* t = table + (size_t)c * kMixFields * ne_pad + ie;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+#pragma unroll
+        for (int q = 0; q < 6; q++) t[(size_t)(k * 6 + q) * ne_pad] = (float)P[k][q];
+        const float hi = (float)om[k];
+        t[(size_t)(12 + 2 * k) * ne_pad] = hi;
+        t[(size_t)(13 + 2 * k) * ne_pad] = (float)(om[k] - (double)hi);
+    }
+}
+
+// physics::calculate_beam (physics.hpp:1153-1260), one thread per energy; result [9][ne].
+__global__ void __launch_bounds__(kTableBlock)
+    beam_f64_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
+                    int ne, double rho_e, double L, double* __restrict__ out) {
+    const int ie = blockIdx.x * kTableBlock + threadIdx.x;
+    if (ie >= ne) return;
+    cd A[3][3];
+    beam_amplitude_f64(&p, energies[ie], rho_e, L, A);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            out[(size_t)(i * 3 + j) * ne + ie] = A[j][i].re * A[j][i].re + A[j][i].im * A[j][i].im;
+}
+
+}  // namespace
+
+cudaError_t launch_table_f64(const OscParams& p, const double* energies, int ne,
+                             const double* cls_rho, int ncls, double* table, cudaStream_t s) {
+    if (ne <= 0 || ncls <= 0) return cudaSuccess;
+    dim3 grid((ne + kTableBlock - 1) / kTableBlock, ncls);
+    table_f64_kernel<<<grid, kTableBlock, 0, s>>>(p, energies, ne, pad_energies(ne), cls_rho, table);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int ne,
+                               const double* cls_rho, int ncls, float* table, cudaStream_t s) {
+    if (ne <= 0 || ncls <= 0) return cudaSuccess;
+    dim3 grid((ne + kTableBlock - 1) / kTableBlock, ncls);
+    table_mixed_kernel<<<grid, kTableBlock, 0, s>>>(p, energies, ne, pad_energies(ne), cls_rho, table);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,
+                            double L_km, double* out, cudaStream_t s) {
+    if (ne <= 0) return cudaSuccess;
+    beam_f64_kernel<<<(ne + kTableBlock - 1) / kTableBlock, kTableBlock, 0, s>>>(p, energies, ne,
+                                                                                rho_e, L_km, out);
+    return cudaGetLastError();
+}
+
+}  // namespace cp3

@@ -1,0 +1,35 @@
+// cp3_types.h -- plain-old-data blocks shared by the host layer and the kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace cp3 {
+
+// Constants of the reference (constants.hpp:26-50, physics.hpp:443): same values.
+constexpr double kTwoRtTwoGf = 1.52588e-4;   // 2*sqrt(2)*G_F in the reference's units
+constexpr double kKm2Cm = 1.0e5;
+constexpr double kREarthKm = 6371.0;
+constexpr double kREarthCm = kREarthKm * kKm2Cm;
+constexpr double kDensityConvert = 0.5;       // beam Z/A
+constexpr double kLoEFac = 2.534;             // (1/2)(1/(hbar c)) in GeV/(eV^2 km)
+constexpr int kMaxProdHeightBins = 20;
+constexpr int kMaxShells = 128;               // CP3_MAX_SHELLS
+constexpr int kMaxSegments = kMaxShells + 1;  // air segment + crossed shells
+
+// One oscillation-parameter set for one neutrino type, as the kernels read it.
+// Built on the host from the user's angles and splittings (cp3_host.cpp).
+struct alignas(16) OscParams {
+    // Reference-faithful data (FP64 kernels): Propagator::Mix_U, DM, mass order, AXFAC.
+    double U[18];        // U(i,j) re/im at [(i*3+j)*2 + {0,1}]
+    double dm[9];        // DM(i,j) = m_i^2 - m_j^2 with the degeneracy break
+    double axfac[324];   // AXFAC(n,m,i,j,e) at [(((n*3+m)*3+i)*3+j)*4+e]
+    // Rotated real basis of the mixed kernels: U = W . O . diag(1,1,e^{-i d}) with
+    // W = R23 . diag(1,1,e^{i d}) and O = R13 . R12 real, so 2E.H = W (H0 + V e0 e0^T) W^+.
+    double h0[6];        // H0 = O . diag(DM(k,0)) . O^T : 00,01,02,11,12,22 (eV^2)
+    double w[4];         // c23, s23, cos d, sin d (d = the dcp actually used in U)
+    int order[3];        // root order from the vacuum cubic (prepare_getMfast)
+    int anti;            // 1: antineutrino sign of the matter potential
+    int pad[4];
+};
+
+}  // namespace cp3

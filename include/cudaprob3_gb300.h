@@ -1,0 +1,179 @@
+/*
+ * cudaprob3_gb300.h -- C ABI of the GB300 Barger propagator (libcp3gb300.so).
+ *
+ * Plain pointers and sizes only.  Each entry point names the reference interface it
+ * replaces (CUDAProb3++ "linear" fork: AtmosCudaPropagatorSingle / BeamCudaPropagatorSingle,
+ * which derive from AtmosCpuPropagator<double> / BeamCpuPropagator<double> and
+ * Propagator<double>).  The C++ facade cudaprob3_gb300.hpp wraps this ABI in classes with the
+ * reference's names and turns non-zero statuses into std::runtime_error.
+ *
+ * Handles are independent: every parameter lives in the handle (host) and in per-handle
+ * device buffers, never in process-global or __constant__ state, so two handles may compute
+ * concurrently on different streams.  A single handle is not thread-safe.
+ *
+ * Result layouts (device and the bulk-copy calls):
+ *   atmospheric  [9][n_cosines][n_energies]    (channel t = a*3+b is P(a -> b))
+ *   beam         [9][n_energies]
+ * FP64 handles hold doubles, MIXED handles hold floats.
+ */
+#ifndef CUDAPROB3_GB300_H
+#define CUDAPROB3_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cp3_propagator cp3_propagator;
+
+/* Status codes.  The reference throws std::runtime_error (input errors) or prints and calls
+ * exit(1) (CUDA errors, hpc_helpers.cuh:71-78); here every call returns one of these and
+ * cp3_last_error() holds the message. */
+enum cp3_status {
+    CP3_OK = 0,
+    CP3_ERR_BAD_SIZE = 1,      /* vector size differs from the handle's grid / empty model */
+    CP3_ERR_NOT_SET = 2,       /* a required setter was not called (e.g. production height) */
+    CP3_ERR_LAYER_LIMIT = 3,   /* a trajectory crosses more shells than CP3_MAX_SHELLS */
+    CP3_ERR_CUDA = 4,          /* CUDA runtime error (message has the CUDA error string) */
+    CP3_ERR_OOM = 5,           /* device allocation failed */
+    CP3_ERR_BAD_ARGUMENT = 6,  /* invalid enum / pointer / device id */
+    CP3_ERR_INDEX = 7,         /* getProbability index out of range */
+    CP3_ERR_ORDER = 8,         /* radii not monotone ("radii order messed up") */
+    CP3_ERR_FILE = 9,          /* density model file missing or malformed */
+    CP3_ERR_UNSUPPORTED = 10   /* feature not available for this handle kind / precision */
+};
+
+/* Arithmetic of a handle. */
+enum cp3_precision {
+    CP3_FP64 = 0,  /* plain FP64 throughout: the drop-in for the reference's FP64 kernels */
+    CP3_MIXED = 1  /* FP32 transition matrices, layer products and probabilities; FP64
+                      eigen-decomposition; double-float phase reduction */
+};
+
+/* NeutrinoType (types.hpp:29). */
+enum cp3_neutrino { CP3_NEUTRINO = 0, CP3_ANTINEUTRINO = 1 };
+
+/* Most shells one trajectory may cross (the reference's compile-time MaxNLayers()==10,
+ * constants.hpp:46, is a runtime check against this value here). */
+#define CP3_MAX_SHELLS 128
+
+/* ---- lifetime ------------------------------------------------------------------------ */
+
+/* AtmosCudaPropagatorSingle(int id, int n_cosines, int n_energies)
+ * (atmoscudapropagator.cuh:52, atmoscudapropagator.cu:30-57). */
+int cp3_atmos_create(int device, int n_cosines, int n_energies, int precision,
+                     cp3_propagator** out);
+
+/* BeamCudaPropagatorSingle(int id, int n_energies, int n_threads)
+ * (beamcudapropagator.cuh:52, beamcudapropagator.cu:29-54). */
+int cp3_beam_create(int device, int n_energies, int precision, cp3_propagator** out);
+
+/* ~AtmosCudaPropagatorSingle / ~BeamCudaPropagatorSingle (atmoscudapropagator.cu:64-67). */
+int cp3_destroy(cp3_propagator* h);
+
+/* Message of the last failed call on h (h == NULL: last failed create on this thread). */
+const char* cp3_last_error(const cp3_propagator* h);
+
+/* Queries: kind (0 atmospheric, 1 beam), precision, grid sizes. */
+int cp3_get_info(const cp3_propagator* h, int* kind, int* precision, int* n_cosines,
+                 int* n_energies);
+
+/* ---- setters (Propagator / AtmosCpuPropagator / BeamCpuPropagator) ----------------------- */
+
+/* Propagator::setEnergyList (propagator.hpp:213-218) + device copy
+ * (atmoscudapropagator.cu:181-186).  n must equal the handle's n_energies.  GeV. */
+int cp3_set_energies(cp3_propagator* h, const double* energies, int n);
+
+/* AtmosCpuPropagator::setCosineList (atmoscpupropagator.hpp:368-381) + device copy
+ * (atmoscudapropagator.cu:188-191).  Recomputes the per-cosine shell counts. */
+int cp3_set_cosines(cp3_propagator* h, const double* cosines, int n);
+
+/* Propagator::setMNSMatrix (propagator.hpp:148-183): radians; knutype < 0 flips dcp. */
+int cp3_set_mns(cp3_propagator* h, double theta12, double theta13, double theta23, double dcp,
+                int knutype);
+
+/* Propagator::setNeutrinoMasses (propagator.hpp:188-209): eV^2, dm23sq = m3^2 - m2^2. */
+int cp3_set_masses(cp3_propagator* h, double dm12sq, double dm23sq);
+
+/* AtmosCpuPropagator::setDensity(radii, rhos, yps) (atmoscpupropagator.hpp:116-170) and its
+ * device copy (atmoscudapropagator.cu:121-140).  Radii in km, ascending or descending,
+ * including the r = 0 row; rho in g/cm^3; ye = Z/A. */
+int cp3_set_layers(cp3_propagator* h, const double* radii, const double* rho, const double* ye,
+                   int n);
+
+/* AtmosCpuPropagator::setDensity(radii, a, b, c, yps) (atmoscpupropagator.hpp:181-242):
+ * rho(r) = a r^2 + b r + c per shell, averaged along each trajectory segment
+ * (physics::getDensityOfLayerPoly, physics.hpp:651-739). */
+int cp3_set_layers_poly(cp3_propagator* h, const double* radii, const double* a,
+                        const double* b, const double* c, const double* ye, int n);
+
+/* AtmosCpuPropagator::setDensityFromFile (atmoscpupropagator.hpp:250-344): 3-column
+ * (r rho ye) or 5-column (r a b c ye) text, '#' comments.  Two-column files (r rho), which
+ * the reference rejects with std::terminate, are accepted with ye from default_ye_core for
+ * r <= 3480 km and default_ye_mantle outside. */
+int cp3_set_density_file(cp3_propagator* h, const char* path, double default_ye_core,
+                         double default_ye_mantle);
+
+/* AtmosCpuPropagator::setChemicalComposition (atmoscpupropagator.hpp:481-491,
+ * atmoscudapropagator.cu:207-220): n must equal the number of model rows. */
+int cp3_set_chemical_composition(cp3_propagator* h, const double* ye, int n);
+
+/* AtmosCpuPropagator::setProductionHeight (atmoscpupropagator.hpp:386-393): km; the cosine
+ * list must be set first ("must set cosine list before production height"). */
+int cp3_set_production_height(cp3_propagator* h, double height_km);
+
+/* BeamCpuPropagator::setDensity(rho) / setPathLength(L) (beamcpupropagator.hpp:84-91;
+ * device copies beamcudapropagator.cu:83-101).  g/cm^3 (Ye = 0.5 implied) and km. */
+int cp3_set_beam_density(cp3_propagator* h, double rho);
+int cp3_set_beam_path_length(cp3_propagator* h, double path_km);
+
+/* ---- production-height averaging (physics.hpp:997-1067) ---------------------------------- */
+
+/* AtmosCpuPropagator::SetNumberOfProductionHeightBinsForAveraging +
+ * setProductionHeightList (atmoscpupropagator.hpp:85-110, 395-427).  The reference's
+ * switch never turns averaging on (:97-99); here n_bins >= 1 turns it on explicitly and
+ * n_bins == 0 turns it off.  prob: [2][3][n_energies][n_cosines][n_bins];
+ * edges_km: n_bins + 1 entries.  n_bins <= 20. */
+int cp3_set_production_height_averaging(cp3_propagator* h, int n_bins, const double* prob,
+                                        const double* edges_km);
+
+/* ---- compute ----------------------------------------------------------------------------- */
+
+/* calculateProbabilities(NeutrinoType) (atmoscudapropagator.cu:202-205, 266-310;
+ * beamcudapropagator.cu:103-106, 162-186): launch and wait. */
+int cp3_calculate(cp3_propagator* h, int neutrino_type);
+
+/* Launch on `stream` (a cudaStream_t; NULL = the handle's own stream) and return. */
+int cp3_calculate_async(cp3_propagator* h, int neutrino_type, void* stream);
+
+/* waitForCompletion (atmoscudapropagator.cu:313-316). */
+int cp3_synchronize(cp3_propagator* h);
+
+/* ---- results ----------------------------------------------------------------------------- */
+
+/* AtmosCudaPropagatorSingle::getProbability(ic, ie, t) (atmoscudapropagator.cu:222-235).
+ * The first call after a compute copies the whole result to the host. */
+int cp3_get_probability(cp3_propagator* h, int index_cosine, int index_energy, int prob_type,
+                        double* out);
+
+/* BeamCudaPropagatorSingle::getProbability(ie, t) (beamcudapropagator.cu:146-160). */
+int cp3_get_probability_beam(cp3_propagator* h, int index_energy, int prob_type, double* out);
+
+/* getProbabilityArr(out, t) (atmoscudapropagator.cu:238-257): atmospheric order is
+ * energy-major, cosine-minor (out[ie * n_cosines + ic]); beam out[ie]. */
+int cp3_get_probability_arr(cp3_propagator* h, int prob_type, double* out);
+
+/* No reference counterpart (zero-copy access): device pointer of the result in the layout
+ * above; *is_float = 1 for MIXED handles.  Valid until the next compute or destroy. */
+int cp3_device_result(cp3_propagator* h, const void** ptr, int* is_float, size_t* bytes);
+
+/* No reference counterpart: asynchronous copy of the whole result, native element type and
+ * device layout, into dst (bytes as reported by cp3_device_result) on `stream`
+ * (NULL = handle stream). */
+int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

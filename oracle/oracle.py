@@ -65,10 +65,23 @@ def _f64(a):
 
 
 def build(quiet: bool = True) -> None:
-    """Compile the C restatement (both variants) with the committed Makefile."""
-    out = subprocess.run(["make", "-s", "-C", HERE, "all"], capture_output=True, text=True)
-    if out.returncode != 0:
-        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    """Compile the C restatement (both variants) with the committed Makefile, or with the
+    same gcc commands directly where make is absent."""
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "all"], capture_output=True, text=True)
+        if out.returncode == 0:
+            return
+        msg = out.stdout + out.stderr
+    except FileNotFoundError:
+        msg = "make not found"
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "cp3_oracle.c")
+    base = ["gcc", "-std=c11", "-D_DEFAULT_SOURCE", "-O3", "-fopenmp", "-fPIC", "-shared"]
+    for extra, name in ((["-ffp-contract=off"], "libcp3oracle.so"), ([], "libcp3oracle_fast.so")):
+        r = subprocess.run(base + extra + ["-o", os.path.join(BUILD, name), src, "-lm"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + msg + "\n" + r.stdout + r.stderr)
 
 
 class OracleError(RuntimeError):

@@ -1,0 +1,138 @@
+"""Drop-in behaviour of the propagator classes on the GPU: setter checks and messages,
+result access paths, handle independence."""
+import numpy as np
+import pytest
+
+from cudaprob3_gb300 import (AtmosCudaPropagatorSingle, BeamCudaPropagatorSingle,
+                             CudaPropagatorSingle, NeutrinoType, ProbType, earth)
+
+pytestmark = pytest.mark.gpu
+
+NOM = earth.NOMINAL
+
+
+def configured(nc=6, ne=5, prec="fp64"):
+    p = AtmosCudaPropagatorSingle(0, nc, ne, precision=prec)
+    p.setEnergyList(earth.log_energy_grid(ne))
+    p.setCosineList(earth.cosine_grid(nc))
+    p.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, 1)
+    p.setNeutrinoMasses(NOM.dm12sq, NOM.dm23sq)
+    p.setDensity(*earth.PREM_4LAYER)
+    p.setProductionHeight(22.0)
+    return p
+
+
+def test_size_checks():
+    p = AtmosCudaPropagatorSingle(0, 6, 5)
+    with pytest.raises(RuntimeError, match="number of energy nodes"):
+        p.setEnergyList(np.ones(4))
+    with pytest.raises(RuntimeError, match="number of cosine nodes"):
+        p.setCosineList(np.ones(7))
+    with pytest.raises(RuntimeError, match="rhos.size"):
+        p.setDensity([0, 1000, 6371], [1, 2], [0.5, 0.5, 0.5])
+    with pytest.raises(RuntimeError, match="radii order"):
+        p.setDensity([0, 3000, 2000, 6371], [1, 2, 3, 4], [0.5] * 4)
+
+
+def test_production_height_order_and_required():
+    p = AtmosCudaPropagatorSingle(0, 6, 5)
+    with pytest.raises(RuntimeError, match="must set cosine list before production height"):
+        p.setProductionHeight(22.0)
+    p.setEnergyList(earth.log_energy_grid(5))
+    p.setCosineList(earth.cosine_grid(6))
+    p.setMNSMatrix(0.5, 0.1, 0.7, 0.0, 1)
+    p.setNeutrinoMasses(7.5e-5, 2.5e-3)
+    p.setDensity(*earth.PREM_4LAYER)
+    with pytest.raises(RuntimeError, match="production height was not set"):
+        p.calculateProbabilities(NeutrinoType.Neutrino)
+
+
+def test_layer_limit():
+    r = np.linspace(0, 6371, 140)
+    p = AtmosCudaPropagatorSingle(0, 3, 2)
+    p.setCosineList([-1.0, -0.5, 0.5])
+    with pytest.raises(RuntimeError, match="invalid number of maxLayer"):
+        p.setDensity(r, np.full(140, 5.0), np.full(140, 0.5))
+
+
+def test_get_probability_paths_agree():
+    p = configured()
+    p.calculateProbabilities(NeutrinoType.Neutrino)
+    res = p.result()
+    arr = p.getProbabilityArr(ProbType.m_e)
+    for ic in range(6):
+        for ie in range(5):
+            v = p.getProbability(ic, ie, ProbType.m_e)
+            assert v == res[ProbType.m_e, ic, ie]
+            assert arr[ie * 6 + ic] == v
+    with pytest.raises(RuntimeError, match="Invalid indices"):
+        p.getProbability(6, 0, ProbType.e_e)
+
+
+def test_second_compute_overwrites():
+    p = configured()
+    p.calculateProbabilities(NeutrinoType.Neutrino)
+    a = p.getProbability(0, 0, ProbType.m_m)
+    p.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, -1)
+    p.calculateProbabilities(NeutrinoType.Antineutrino)
+    b = p.getProbability(0, 0, ProbType.m_m)
+    assert a != b
+
+
+def test_handles_are_independent():
+    a = configured(prec="mixed")
+    b = configured(prec="mixed")
+    b.setNeutrinoMasses(NOM.dm12sq, -2.5e-3)
+    a.calculate_async(NeutrinoType.Neutrino)
+    b.calculate_async(NeutrinoType.Neutrino)
+    a.synchronize()
+    b.synchronize()
+    ra, rb = a.result(), b.result()
+    a.calculateProbabilities(NeutrinoType.Neutrino)
+    assert np.array_equal(a.result(), ra)
+    assert not np.array_equal(ra, rb)
+
+
+def test_density_file_formats(tmp_path, oracle):
+    r, rho, ye = earth.PREM_4LAYER
+    f3 = tmp_path / "prem3.dat"
+    f3.write_text("# radius rho ye\n" + "".join(f"{a} {b} {c}\n" for a, b, c in zip(r, rho, ye)))
+    f2 = tmp_path / "prem2.dat"
+    f2.write_text("".join(f"{a}\t{b}\n" for a, b in zip(r, rho)))
+    outs = []
+    for f in (f3, f2):
+        p = configured()
+        p.setDensityFromFile(str(f))
+        p.calculateProbabilities(NeutrinoType.Neutrino)
+        outs.append(p.result())
+    ref = configured()
+    ref.calculateProbabilities(NeutrinoType.Neutrino)
+    assert np.array_equal(outs[0], ref.result())
+    assert np.array_equal(outs[1], ref.result())  # Ye rule reproduces PREM_4layer's column
+    bad = tmp_path / "bad.dat"
+    bad.write_text("0 1 2 3\n")
+    with pytest.raises(RuntimeError, match="Unsupported"):
+        configured().setDensityFromFile(str(bad))
+
+
+def test_beam_api_and_legacy_template_name():
+    b = BeamCudaPropagatorSingle(0, 100, 1)
+    b.setEnergyList(earth.lin_energy_grid(100))
+    b.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, 1)
+    b.setNeutrinoMasses(NOM.dm12sq, NOM.dm23sq)
+    with pytest.raises(RuntimeError, match="density was not set"):
+        b.calculateProbabilities(NeutrinoType.Neutrino)
+    b.setDensity(2.6)
+    b.setPathLength(1300.0)
+    b.calculateProbabilities(NeutrinoType.Neutrino)
+    assert abs(b.getProbabilityArr(ProbType.m_m)[50] - b.getProbability(50, ProbType.m_m)) == 0
+    t = CudaPropagatorSingle(0, 4, 4, float_type=np.float32)
+    assert t.precision == 1
+
+
+def test_unitarity_mixed_large():
+    p = configured(nc=300, ne=200, prec="mixed")
+    p.calculateProbabilities(NeutrinoType.Neutrino)
+    P = p.result().astype(np.float64).reshape(3, 3, 300, 200)  # [a][b][ic][ie]
+    assert np.abs(P.sum(axis=1) - 1).max() < 1e-5
+    assert np.abs(P.sum(axis=0) - 1).max() < 1e-5

@@ -1,0 +1,427 @@
+"""Benchmark of the Barger propagation hot path on GB300.
+
+Default workload (the precision-study configuration): atmospheric propagation through a
+59-shell synthetic Earth (equal-thickness shells, seeded monotone density 13.1 -> 2.6 g/cm^3
+with a step at 3480 km), 2000 cos(zenith) x 2000 log-spaced energies (0.1-100 GeV), production
+height 22 km, neutrino and antineutrino, nominal oscillation parameters, mixed-precision
+kernels.  One step = both neutrino types over the full grid = 72e6 probabilities.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload atmos59|prem4|beam]
+
+Prints one JSON line.  ``value`` is probabilities/s with inputs resident on the device
+(CUDA events on the launching stream, max over ranks); ``e2e`` is the same metric through the
+public API with host buffers (grid upload and full result download in the timed region);
+``roofline`` reports the per-bin kernel against the live-measured FP32 FMA peak.
+``--impl reference`` times the CPU oracle (C restatement of the reference's CPU
+propagator, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TYPES = 2  # neutrino + antineutrino per step
+
+
+def f_bin(M):
+    """Canonical algorithmic flops of one (cos, E) bin crossing M shells: eigen-solve 40 +
+    phase 7 + 3-term transition matrix 183 per distinct segment (M+1), 216 per layer product
+    (2M-1 of them), 27 for the nine |A|^2."""
+    M = np.asarray(M, dtype=np.float64)
+    return 27.0 + 230.0 * (M + 1) + 216.0 * np.maximum(2 * M - 1, 0)
+
+
+def workload(name):
+    from cudaprob3_gb300 import earth
+    if name == "atmos59":
+        r, rho, ye = earth.synthetic_shells(59)
+        return dict(kind="atmos", model=(r, rho, ye), cz=earth.cosine_grid(2000),
+                    en=earth.log_energy_grid(2000), h=22.0,
+                    desc="atmospheric, 59 equal shells (seeded monotone profile), 2000 cos x "
+                         "2000 log-E (0.1-100 GeV), h=22 km, nu+nubar")
+    if name == "prem4":
+        return dict(kind="atmos", model=earth.PREM_4LAYER, cz=earth.cosine_grid(400),
+                    en=earth.log_energy_grid(400), h=22.0,
+                    desc="atmospheric, PREM 4-layer, 400 cos x 400 log-E (0.1-100 GeV), "
+                         "h=22 km, nu+nubar")
+    if name == "beam":
+        return dict(kind="beam", en=earth.lin_energy_grid(100000), rho=2.6, L=1300.0,
+                    desc="beam, rho=2.6 g/cm^3, L=1300 km, 1e5 E (0.1-10 GeV), nu+nubar")
+    raise SystemExit(f"unknown workload {name}")
+
+
+def shells_crossed(w):
+    from cudaprob3_gb300 import earth  # noqa: F401
+    r = np.asarray(w["model"][0], dtype=np.float64)
+    rd = np.sort(r)[::-1]
+    lim = -np.sqrt(1 - rd ** 2 / 6371.0 ** 2)
+    lim[0] = 0.0
+    return (w["cz"][:, None] < lim[None, :]).sum(axis=1)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path).read().splitlines()[1:]:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax = float(parts[2].split()[0])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fma_peaks(device):
+    from cudaprob3_gb300 import build
+    L = C.CDLL(build.PEAKS_LIB)
+    L.cp3peaks_fma_tflops.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
+    out = {}
+    for name, fp64, iters in (("fp32", 0, 8192), ("fp64", 1, 512)):
+        t, ms = C.c_double(), C.c_double()
+        rc = L.cp3peaks_fma_tflops(fp64, device, iters, C.byref(t), C.byref(ms))
+        out[name] = t.value if rc == 0 else None
+    return out
+
+
+def make_propagator(w, prec):
+    from cudaprob3_gb300 import AtmosCudaPropagatorSingle, BeamCudaPropagatorSingle
+    if w["kind"] == "atmos":
+        p = AtmosCudaPropagatorSingle(0, len(w["cz"]), len(w["en"]), precision=prec)
+        p.setEnergyList(w["en"])
+        p.setCosineList(w["cz"])
+        p.setDensity(*w["model"])
+        p.setProductionHeight(w["h"])
+    else:
+        p = BeamCudaPropagatorSingle(0, len(w["en"]), 1, precision=prec)
+        p.setEnergyList(w["en"])
+        p.setDensity(w["rho"])
+        p.setPathLength(w["L"])
+    return p
+
+
+def set_params(p, m, knu):
+    p.setMNSMatrix(m.theta12, m.theta13, m.theta23, m.dcp, knu)
+    p.setNeutrinoMasses(m.dm12sq, m.dm23sq)
+
+
+def run_ours(args, rank, world):
+    import torch
+    from cudaprob3_gb300 import earth
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    w = workload(args.workload)
+    prec = args.precision
+    # weak scaling: each rank propagates its own parameter set over the full grid
+    m = earth.NOMINAL if rank == 0 else earth.gaussian_sets(world, seed=77)[rank]
+    props = []
+    for knu in (1, -1):
+        p = make_propagator(w, prec)
+        set_params(p, m, knu)
+        p.set_profiling(True)
+        props.append(p)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        for t, p in enumerate(props):
+            p.calculate_async(t, sptr)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    if w["kind"] == "atmos":
+        nbins = len(w["cz"]) * len(w["en"])
+        M = shells_crossed(w)
+        flops_launch = float(f_bin(M).sum()) * len(w["en"])
+    else:
+        nbins = len(w["en"])
+        flops_launch = float(f_bin(0)) * nbins
+    probs_step = 9 * nbins * N_TYPES
+    bytes_out_launch = 9 * nbins * (4 if prec == "mixed" else 8)
+
+    # device-resident timed region: K steps, L2 flushed (untimed) between steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    bins_ms, eig_ms = [], []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        for k in range(args.steps):
+            flush.add_(1.0)
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            for p in props:
+                a, b = p.kernel_times()
+                eig_ms.append(a)
+                bins_ms.append(b)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_ms = float(np.mean(step_ms))
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        t_ms = float(tt.item())
+    value = world * probs_step / (t_ms * 1e-3)
+    kernel_ms = float(np.mean(bins_ms))
+
+    # end to end through the public API: grid H2D from pinned memory, compute, full D2H
+    is_float = prec == "mixed"
+    host_out = [torch.empty(bytes_out_launch // (4 if is_float else 8),
+                            dtype=torch.float32 if is_float else torch.float64, pin_memory=True)
+                for _ in props]
+    en_pinned = torch.from_numpy(np.asarray(w["en"], dtype=np.float64)).pin_memory()
+    cz_pinned = (torch.from_numpy(np.asarray(w["cz"], dtype=np.float64)).pin_memory()
+                 if w["kind"] == "atmos" else None)
+
+    def e2e_step():
+        for t, p in enumerate(props):
+            p.setEnergyList(en_pinned.numpy())
+            if cz_pinned is not None:
+                p.setCosineList(cz_pinned.numpy())
+            p.calculate_async(t, sptr)
+            p.copy_result_async(host_out[t].data_ptr(), sptr)
+        stream.synchronize()
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    h2d = (len(w["en"]) + (len(w["cz"]) if w["kind"] == "atmos" else 0)) * 8 * len(props)
+    d2h = bytes_out_launch * len(props)
+
+    peaks = fma_peaks(dev)
+    achieved = flops_launch / (kernel_ms * 1e-3) / 1e12
+    peak32 = peaks.get("fp32")
+    roofline = {
+        "bound": "fp32" if prec == "mixed" else "fp64",
+        "achieved": round(achieved, 3),
+        "peak": round(peak32 if prec == "mixed" else peaks.get("fp64"), 3),
+        "unit": "TFLOP/s",
+        "frac": round(achieved / (peak32 if prec == "mixed" else peaks.get("fp64")), 4),
+        "traffic": None,
+        "peak_source": "live FMA-chain microbenchmark in this run (cp3_peaks.cu); the pool's "
+                       "measured HBM/bf16 peaks do not apply to scalar FP pipes",
+        "kernel": "atmos_mixed_kernel" if (w["kind"] == "atmos" and prec == "mixed") else
+                  ("atmos_f64_kernel" if w["kind"] == "atmos" else
+                   ("beam_mixed_kernel" if prec == "mixed" else "beam_f64_kernel")),
+        "kernel_ms": round(kernel_ms, 4),
+        "eigen_table_ms": round(float(np.mean(eig_ms)), 4),
+        "flops_per_launch": flops_launch,
+        "hbm_gbs_output": round(bytes_out_launch / (kernel_ms * 1e-3) / 1e9, 1),
+    }
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        roofline["hbm_frac_of_measured"] = round(roofline["hbm_gbs_output"] / mp["hbm_gbs"], 4)
+    except (OSError, KeyError, ValueError):
+        pass
+
+    line = {
+        "metric": "oscillation probabilities/s (mixed precision, max err <= 1e-5 vs FP64 oracle)",
+        "value": value,
+        "unit": "probabilities/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64" if prec == "mixed" else "f64",
+        "data": "synthetic (seeded Earth model and parameters; no dataset involved)",
+        "config": {"workload": args.workload, "description": w["desc"], "precision": prec,
+                   "probabilities_per_step": probs_step,
+                   "l2": "256 MB buffer written between timed steps (untimed); per-step output "
+                         f"{d2h / 1e6:.0f} MB exceeds L2"},
+        "e2e": {"value": world * probs_step / (e2e_ms * 1e-3), "unit": "probabilities/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": args.steps * len(props) * (2 if w["kind"] == "atmos" else 1),
+        "roofline": roofline,
+        "peaks_tflops": peaks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
+    line["clocks"] = clk.summary()
+    return line
+
+
+def cpu_sample(w, seconds, orc=None, nthreads=1):
+    """A bounded slice of the workload for the CPU, sized from a short probe run to take
+    about ``seconds`` of wall time: every k-th cosine row (keeps the distribution of shells
+    crossed) or a contiguous block of beam energies."""
+    if w["kind"] == "atmos":
+        stride = max(1, len(w["cz"]) // 8)
+        if orc is not None:
+            probe = dict(w, cz=w["cz"][::stride])
+            t0 = time.perf_counter()
+            cpu_run(probe, orc, nthreads)
+            per_row = (time.perf_counter() - t0) / len(probe["cz"])
+            rows = max(8, min(len(w["cz"]), int(seconds / max(per_row, 1e-9))))
+            stride = max(1, len(w["cz"]) // rows)
+        sub = w["cz"][::stride]
+        return dict(w, cz=sub), f"every {stride}th cosine row ({len(sub)} x {len(w['en'])} bins), nu+nubar"
+    n = len(w["en"])
+    if orc is not None:
+        probe = dict(w, en=w["en"][:20000])
+        t0 = time.perf_counter()
+        cpu_run(probe, orc, nthreads)
+        n = max(20000, min(n, int(seconds / max((time.perf_counter() - t0) / 20000, 1e-12))))
+    return dict(w, en=w["en"][:n]), f"{n} energies, nu+nubar"
+
+
+def cpu_run(w, orc, nthreads):
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix
+    m = earth.NOMINAL
+    t0 = time.perf_counter()
+    nbins = 0
+    for anti, knu in ((False, 1), (True, -1)):
+        mix = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
+        if w["kind"] == "atmos":
+            r, rho, ye = w["model"]
+            orc.atmos(mix, anti, w["cz"], w["en"], r, rho, ye, w["h"], nthreads=nthreads)
+            nbins += len(w["cz"]) * len(w["en"])
+        else:
+            orc.beam(mix, anti, w["en"], w["rho"], w["L"], nthreads=nthreads)
+            nbins += len(w["en"])
+    return 9 * nbins / (time.perf_counter() - t0)
+
+
+def cpu_baseline(w, seconds=2.0):
+    from oracle.oracle import Oracle
+    orc = Oracle(fast=True)
+    cores = os.cpu_count() or 1
+    sample_w, desc = cpu_sample(w, seconds, orc, cores)  # the probe run also warms up
+    rate = cpu_run(sample_w, orc, cores)
+    return {"value": rate, "unit": "probabilities/s", "cores": cores, "kind": "port",
+            "sample": desc + "; C restatement of the reference CpuPropagator<double> "
+                             "(OpenMP over cosines, -O3), all host threads"}
+
+
+def run_reference(args):
+    """The reference arm: the reference's CPU algorithm (C restatement) on the host cores."""
+    from oracle.oracle import Oracle
+    w = workload(args.workload)
+    orc = Oracle(fast=True)
+    cores = os.cpu_count() or 1
+    sample_w, desc = cpu_sample(w, args.cpu_seconds / 4.0, orc, cores)
+    for _ in range(args.warmup):
+        cpu_run(sample_w, orc, cores)
+    rates = [cpu_run(sample_w, orc, cores) for _ in range(args.steps)]
+    value = float(np.median(rates))
+    return {
+        "impl": "reference",
+        "metric": "oscillation probabilities/s (mixed precision, max err <= 1e-5 vs FP64 oracle)",
+        "value": value, "unit": "probabilities/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 9 * N_TYPES * (len(sample_w["cz"]) * len(sample_w["en"]) if w["kind"] == "atmos" else len(sample_w["en"])) / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"],
+                                        "sample": desc},
+        "cpu_baseline": {"value": value, "unit": "probabilities/s", "cores": cores,
+                         "kind": "port",
+                         "sample": desc + "; reference CPU algorithm restated in C "
+                                          "(oracle/cp3_oracle.c), the reference's own build "
+                                          "needs its source tree, absent on this host"},
+        "e2e": {"value": value, "unit": "probabilities/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="atmos59", choices=["atmos59", "prem4", "beam"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=2.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    import __graft_entry__
+    __graft_entry__.build()
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    line = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

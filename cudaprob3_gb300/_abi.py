@@ -19,6 +19,7 @@ EXPORTS = (
     "cp3_set_production_height_averaging", "cp3_calculate", "cp3_calculate_async",
     "cp3_synchronize", "cp3_get_probability", "cp3_get_probability_beam",
     "cp3_get_probability_arr", "cp3_device_result", "cp3_copy_result_async",
+    "cp3_set_profiling", "cp3_kernel_times",
 )
 
 CP3_OK = 0
@@ -55,6 +56,8 @@ _SIGS = {
     "cp3_get_probability_arr": ([_h, C.c_int, _dp], C.c_int),
     "cp3_device_result": ([_h, C.POINTER(C.c_void_p), _ip, C.POINTER(C.c_size_t)], C.c_int),
     "cp3_copy_result_async": ([_h, C.c_void_p, C.c_void_p], C.c_int),
+    "cp3_set_profiling": ([_h, C.c_int], C.c_int),
+    "cp3_kernel_times": ([_h, _dp, _dp], C.c_int),
 }
 
 _LIB = None

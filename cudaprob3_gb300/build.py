@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcp3gb300.so")
+PEAKS_LIB = os.path.join(OUT, "libcp3peaks.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra flags)
@@ -73,6 +74,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
+    # bench support: scalar FMA peaks (separate library, not part of the C ABI)
+    cmd = [nvcc] + ARCH + common + ["-shared", os.path.join(SRC, "cp3_peaks.cu"), "-o", PEAKS_LIB]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     with open(os.path.join(OUT, "build.log"), "w") as f:
         f.write("\n".join(logs))
     if verbose:

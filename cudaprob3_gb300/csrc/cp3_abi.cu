@@ -85,7 +85,14 @@ struct cp3_propagator {
     bool result_on_host = false;
     bool computed = false;
 
+    bool profiling = false;
+    bool timed = false;
+    bool timed_table = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
     ~cp3_propagator() {
+        for (cudaEvent_t& e : ev)
+            if (e) cudaEventDestroy(e);
         if (h_result) cudaFreeHost(h_result);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -212,6 +219,10 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
     OscParams p;
     build_osc_params(h->mix, type == CP3_ANTINEUTRINO, &p);
     cudaError_t e = cudaSuccess;
+    h->timed = false;
+    auto mark = [&](int i) {
+        if (h->profiling && e == cudaSuccess) e = cudaEventRecord(h->ev[i], s);
+    };
     if (h->kind == 0) {
         if (!h->model_set) return fail(h, CP3_ERR_NOT_SET, "density model was not set");
         if (!h->height_set)
@@ -224,9 +235,11 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
             return fail(h, CP3_ERR_UNSUPPORTED, "polynomial density model not yet on the GPU path");
         int rc = prepare_atmos(h);
         if (rc) return rc;
+        mark(0);
         if (h->precision == CP3_FP64) {
             e = launch_table_f64(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
                                  h->d_table64.ptr, s);
+            mark(1);
             if (e == cudaSuccess)
                 e = launch_atmos_f64(p, h->d_energies.ptr, h->ne, h->d_table64.ptr,
                                      h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
@@ -234,26 +247,33 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
         } else {
             e = launch_table_mixed(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
                                    h->d_table32.ptr, s);
+            mark(1);
             if (e == cudaSuccess)
                 e = launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
                                        h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc,
                                        (float*)h->d_result.ptr, s);
         }
+        mark(2);
+        h->timed_table = true;
     } else {
         if (!h->beam_rho_set) return fail(h, CP3_ERR_NOT_SET, "beam density was not set");
         if (!h->beam_L_set) return fail(h, CP3_ERR_NOT_SET, "beam path length was not set");
         // calculate_beam passes density * density_convert() (physics.hpp:1217-1223)
         const double rho_e = h->beam_rho * kDensityConvert;
+        mark(1);
         if (h->precision == CP3_FP64)
             e = launch_beam_f64(p, h->d_energies.ptr, h->ne, rho_e, h->beam_L,
                                 (double*)h->d_result.ptr, s);
         else
             e = launch_beam_mixed(p, h->d_energies.ptr, h->ne, rho_e, h->beam_L,
                                   (float*)h->d_result.ptr, s);
+        mark(2);
+        h->timed_table = false;
     }
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     h->result_on_host = false;
     h->computed = true;
+    h->timed = h->profiling;
     return CP3_OK;
 }
 
@@ -545,6 +565,29 @@ int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream) {
     CP3_CUDA(h, cudaMemcpyAsync(dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost,
                                 stream ? (cudaStream_t)stream : h->stream),
              "copy result");
+    return CP3_OK;
+}
+
+int cp3_set_profiling(cp3_propagator* h, int enable) {
+    if (int rc = check_handle(h)) return rc;
+    CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    if (enable)
+        for (cudaEvent_t& e : h->ev)
+            if (!e) CP3_CUDA(h, cudaEventCreate(&e), "cudaEventCreate");
+    h->profiling = enable != 0;
+    h->timed = false;
+    return CP3_OK;
+}
+
+int cp3_kernel_times(cp3_propagator* h, double* eigen_ms, double* bins_ms) {
+    if (int rc = check_handle(h)) return rc;
+    if (!h->timed) return fail(h, CP3_ERR_NOT_SET, "no profiled compute (cp3_set_profiling first)");
+    CP3_CUDA(h, cudaEventSynchronize(h->ev[2]), "cudaEventSynchronize");
+    float a = 0.f, b = 0.f;
+    if (h->timed_table) CP3_CUDA(h, cudaEventElapsedTime(&a, h->ev[0], h->ev[1]), "elapsed");
+    CP3_CUDA(h, cudaEventElapsedTime(&b, h->ev[1], h->ev[2]), "elapsed");
+    if (eigen_ms) *eigen_ms = a;
+    if (bins_ms) *bins_ms = b;
     return CP3_OK;
 }
 

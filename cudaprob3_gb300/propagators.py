@@ -78,6 +78,15 @@ class Propagator:
         self._check(self._lib.cp3_device_result(self._h, C.byref(ptr), C.byref(isf), C.byref(nb)))
         return ptr.value, bool(isf.value), nb.value
 
+    def set_profiling(self, enable: bool = True):
+        self._check(self._lib.cp3_set_profiling(self._h, int(bool(enable))))
+
+    def kernel_times(self):
+        """(eigen-table ms, per-bin kernel ms) of the last compute (needs set_profiling)."""
+        a, b = C.c_double(), C.c_double()
+        self._check(self._lib.cp3_kernel_times(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def copy_result_async(self, dst_ptr: int, stream=None):
         self._check(self._lib.cp3_copy_result_async(self._h, C.c_void_p(dst_ptr),
                                                     C.c_void_p(stream) if stream else None))

@@ -173,6 +173,15 @@ int cp3_device_result(cp3_propagator* h, const void** ptr, int* is_float, size_t
  * (NULL = handle stream). */
 int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream);
 
+/* ---- profiling (the reference's TIMERSTART/TIMERSTOP macros, hpc_helpers.cuh:29-67) ------- */
+
+/* enable != 0: record CUDA events around each kernel of every following compute. */
+int cp3_set_profiling(cp3_propagator* h, int enable);
+
+/* Device time of the last compute's kernels (waits for them): the eigen-table kernel and the
+ * per-bin kernel, milliseconds.  eigen_ms is 0 where no table kernel runs (beam). */
+int cp3_kernel_times(cp3_propagator* h, double* eigen_ms, double* bins_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,7 @@ EXPORTS = (
     "cp3_set_production_height_averaging", "cp3_calculate", "cp3_calculate_async",
     "cp3_synchronize", "cp3_get_probability", "cp3_get_probability_beam",
     "cp3_get_probability_arr", "cp3_device_result", "cp3_copy_result_async",
-    "cp3_set_profiling", "cp3_kernel_times",
+    "cp3_trajectory_table", "cp3_set_profiling", "cp3_kernel_times",
 )
 
 CP3_OK = 0
@@ -56,6 +56,8 @@ _SIGS = {
     "cp3_get_probability_arr": ([_h, C.c_int, _dp], C.c_int),
     "cp3_device_result": ([_h, C.POINTER(C.c_void_p), _ip, C.POINTER(C.c_size_t)], C.c_int),
     "cp3_copy_result_async": ([_h, C.c_void_p, C.c_void_p], C.c_int),
+    "cp3_trajectory_table": ([_dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, C.c_int, C.c_double,
+                              _ip, _ip, _ip, _dp, _dp, _ip, _dp], C.c_int),
     "cp3_set_profiling": ([_h, C.c_int], C.c_int),
     "cp3_kernel_times": ([_h, _dp, _dp], C.c_int),
 }
@@ -93,6 +95,29 @@ class CP3Error(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(message)
         self.code = code
+
+
+def trajectory_table(radii, c1, ye, cosines, height_km, c2=None, c3=None, poly=False):
+    """Host-side geometry of the atmospheric kernels (no GPU needed): returns a dict with
+    seg_offset, seg_len_km, seg_rho_e, seg_class, class_rho_e."""
+    import numpy as np
+
+    L = lib()
+    f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    r, a1, a2, a3, y, cz = f(radii), f(c1), f(c2), f(c3), f(ye), f(cosines)
+    p = lambda a: None if a is None else a.ctypes.data_as(_dp)  # noqa: E731
+    ns, ncl = C.c_int(), C.c_int()
+    args = (p(r), p(a1), p(a2), p(a3), p(y), len(r), int(poly), p(cz), len(cz), float(height_km))
+    check(L.cp3_trajectory_table(*args, C.byref(ns), C.byref(ncl), None, None, None, None, None))
+    off = np.empty(len(cz) + 1, dtype=np.int32)
+    ln, rho = np.empty(ns.value), np.empty(ns.value)
+    cls = np.empty(ns.value, dtype=np.int32)
+    crho = np.empty(max(ncl.value, 1))
+    ip = lambda a: a.ctypes.data_as(_ip)  # noqa: E731
+    check(L.cp3_trajectory_table(*args, C.byref(ns), C.byref(ncl), ip(off), p(ln), p(rho),
+                                 ip(cls), p(crho)))
+    return dict(seg_offset=off, seg_len_km=ln, seg_rho_e=rho, seg_class=cls,
+                class_rho_e=crho[:ncl.value])
 
 
 def check(rc: int, handle=None):

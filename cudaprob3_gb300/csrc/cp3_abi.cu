@@ -53,6 +53,7 @@ struct cp3_propagator {
     int kind = 0;  // 0 atmospheric, 1 beam
     int device = 0, nc = 0, ne = 0, precision = CP3_FP64;
     cudaStream_t stream = nullptr;
+    cudaStream_t last_stream = nullptr;  // stream of the last compute: results are read after it
     std::string err;
 
     MixingInput mix;
@@ -273,6 +274,7 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     h->result_on_host = false;
     h->computed = true;
+    h->last_stream = s;
     h->timed = h->profiling;
     return CP3_OK;
 }
@@ -283,7 +285,7 @@ int fetch_result(cp3_propagator* h) {
     const size_t n = h->result_bytes / (h->precision == CP3_FP64 ? 8 : 4);
     if (!h->h_result) CP3_CUDA(h, cudaMallocHost(&h->h_result, n * sizeof(double)), "pinned result");
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    CP3_CUDA(h, cudaStreamSynchronize(h->stream), "synchronize");
+    CP3_CUDA(h, cudaStreamSynchronize(h->last_stream ? h->last_stream : h->stream), "synchronize");
     if (h->precision == CP3_FP64) {
         CP3_CUDA(h, cudaMemcpy(h->h_result, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost),
                  "copy result");
@@ -320,6 +322,7 @@ int cp3_destroy(cp3_propagator* h) {
     if (!h) return CP3_OK;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->last_stream && h->last_stream != h->stream) cudaStreamSynchronize(h->last_stream);
     delete h;
     return CP3_OK;
 }
@@ -511,6 +514,8 @@ int cp3_synchronize(cp3_propagator* h) {
     if (int rc = check_handle(h)) return rc;
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     CP3_CUDA(h, cudaStreamSynchronize(h->stream), "waitForCompletion");
+    if (h->last_stream && h->last_stream != h->stream)
+        CP3_CUDA(h, cudaStreamSynchronize(h->last_stream), "waitForCompletion");
     return CP3_OK;
 }
 
@@ -562,9 +567,37 @@ int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream) {
     if (int rc = check_handle(h)) return rc;
     if (!dst) return fail(h, CP3_ERR_BAD_ARGUMENT, "null destination");
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    CP3_CUDA(h, cudaMemcpyAsync(dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost,
-                                stream ? (cudaStream_t)stream : h->stream),
+    cudaStream_t s = stream ? (cudaStream_t)stream : (h->last_stream ? h->last_stream : h->stream);
+    CP3_CUDA(h, cudaMemcpyAsync(dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost, s),
              "copy result");
+    return CP3_OK;
+}
+
+int cp3_trajectory_table(const double* radii, const double* c1, const double* c2,
+                         const double* c3, const double* ye, int n_radii, int poly,
+                         const double* cosines, int n_cosines, double height_km,
+                         int* n_segments, int* n_classes, int* seg_offset, double* seg_len_km,
+                         double* seg_rho_e, int* seg_class, double* class_rho_e) {
+    if (!n_segments || !n_classes || (n_cosines > 0 && !cosines) || n_cosines < 0)
+        return fail(nullptr, CP3_ERR_BAD_ARGUMENT, "null size outputs or cosines");
+    EarthModel m;
+    std::string msg;
+    int rc = make_earth_model(radii, c1, c2, c3, ye, n_radii, poly != 0, &m, &msg);
+    if (rc) return fail(nullptr, rc, msg);
+    TrajectoryTable t;
+    rc = build_trajectories(m, cosines, n_cosines, height_km * 100000.0, &t, &msg);
+    if (rc) return fail(nullptr, rc, msg);
+    const int maxm = n_cosines > 0 ? *std::max_element(t.maxlayers.begin(), t.maxlayers.end()) : 0;
+    *n_segments = (int)t.len_km.size();
+    *n_classes = poly ? 0 : 1 + maxm;
+    if (seg_offset) std::copy(t.offset.begin(), t.offset.end(), seg_offset);
+    if (seg_len_km) std::copy(t.len_km.begin(), t.len_km.end(), seg_len_km);
+    if (seg_rho_e) std::copy(t.rho_e.begin(), t.rho_e.end(), seg_rho_e);
+    if (seg_class) std::copy(t.cls.begin(), t.cls.end(), seg_class);
+    if (class_rho_e && !poly) {
+        class_rho_e[0] = 0.0;
+        for (int c = 1; c <= maxm; c++) class_rho_e[c] = m.rho[c - 1] * m.ye[c - 1];
+    }
     return CP3_OK;
 }
 

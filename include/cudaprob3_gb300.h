@@ -144,7 +144,8 @@ int cp3_set_production_height_averaging(cp3_propagator* h, int n_bins, const dou
  * beamcudapropagator.cu:103-106, 162-186): launch and wait. */
 int cp3_calculate(cp3_propagator* h, int neutrino_type);
 
-/* Launch on `stream` (a cudaStream_t; NULL = the handle's own stream) and return. */
+/* Launch on `stream` (a cudaStream_t; NULL = the handle's own stream) and return.  Later
+ * result reads and cp3_synchronize order themselves after this stream. */
 int cp3_calculate_async(cp3_propagator* h, int neutrino_type, void* stream);
 
 /* waitForCompletion (atmoscudapropagator.cu:313-316). */
@@ -170,8 +171,24 @@ int cp3_device_result(cp3_propagator* h, const void** ptr, int* is_float, size_t
 
 /* No reference counterpart: asynchronous copy of the whole result, native element type and
  * device layout, into dst (bytes as reported by cp3_device_result) on `stream`
- * (NULL = handle stream). */
+ * (NULL = the stream of the last compute). */
 int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream);
+
+/* ---- trajectory geometry (host only, no GPU) --------------------------------------------- */
+
+/* No reference counterpart (inspection of what the atmospheric kernels walk; the geometry is
+ * that of physics::calculate_atmos, getTraversedDistanceOfLayer, getDensityOfLayer[Poly],
+ * physics.hpp:634-898).  Model as for cp3_set_layers (poly = 0: c1 = rho) or
+ * cp3_set_layers_poly (poly = 1: c1, c2, c3 = a, b, c).  Call once with NULL outputs to get
+ * *n_segments and *n_classes, then with arrays of those sizes: seg_offset[n_cosines + 1],
+ * seg_len_km / seg_rho_e / seg_class[*n_segments] (segments l = 0..M of each cosine: air,
+ * then shells inwards), class_rho_e[*n_classes] (class 0 = air; class 1 + i = shell i of the
+ * constant model; poly segments have class -1). */
+int cp3_trajectory_table(const double* radii, const double* c1, const double* c2,
+                         const double* c3, const double* ye, int n_radii, int poly,
+                         const double* cosines, int n_cosines, double production_height_km,
+                         int* n_segments, int* n_classes, int* seg_offset, double* seg_len_km,
+                         double* seg_rho_e, int* seg_class, double* class_rho_e);
 
 /* ---- profiling (the reference's TIMERSTART/TIMERSTOP macros, hpc_helpers.cuh:29-67) ------- */
 

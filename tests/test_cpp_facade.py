@@ -1,0 +1,60 @@
+"""The C++ facade (include/cudaprob3_gb300.hpp): compiles against the header with the
+reference's call order (CPU), and on the GPU reproduces the oracle through it."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+SRC = os.path.join(ROOT, "tests", "cpp", "drop_in.cpp")
+
+
+def build_program(tmp_path):
+    from cudaprob3_gb300 import build
+    lib = build.build()
+    exe = str(tmp_path / "drop_in")
+    cmd = ["g++", "-std=c++14", "-O2", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe,
+           lib, "-Wl,-rpath," + os.path.dirname(lib)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_facade_compiles_and_links(tmp_path):
+    exe = build_program(tmp_path)
+    assert os.path.exists(exe)
+
+
+@pytest.mark.gpu
+def test_facade_matches_oracle(tmp_path, oracle):
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix
+    exe = build_program(tmp_path)
+    model = tmp_path / "prem4.dat"
+    r, rho, ye = earth.PREM_4LAYER
+    model.write_text("".join(f"{a} {b} {c}\n" for a, b, c in zip(r, rho, ye)))
+    for args in ([exe], [exe, str(model)]):
+        out = subprocess.run(args, capture_output=True, text=True, timeout=120)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "caught: CudaPropagatorSingle::getProbability. Invalid indices" in out.stdout
+        nc, ne = 20, 16
+        cz = -1.0 + 2.0 * np.arange(nc) / (nc - 1)
+        en = 10 ** (-1.0 + 3.0 * np.arange(ne) / (ne - 1))
+        m = OMix(0.5843, 0.1496, 0.7365, -1.601, 7.53e-5, 2.49e-3, 1)
+        ref = oracle.atmos(m, False, cz, en, r, rho, ye, 22.0)
+        eb = 0.1 + 9.9 * np.arange(1000) / 999.0
+        refb = oracle.beam(m, False, eb, 2.6, 1300.0)
+        n = 0
+        for line in out.stdout.splitlines():
+            f = line.split()
+            if f[0] == "atmos":
+                ic, ie, t, v = int(f[1]), int(f[2]), int(f[3]), float(f[4])
+                assert abs(v - ref[ic, ie, t]) <= 1e-12
+                n += 1
+            elif f[0] == "beam":
+                ie, t, v = int(f[1]), int(f[2]), float(f[3])
+                assert abs(v - refb[ie, t]) <= 1e-12
+                n += 1
+        assert n > 100

@@ -347,7 +347,8 @@ def cpu_sample(w, seconds, orc=None, nthreads=1):
             t0 = time.perf_counter()
             cpu_run(probe, orc, nthreads)
             per_row = (time.perf_counter() - t0) / len(probe["cz"])
-            rows = max(8, min(len(w["cz"]), int(seconds / max(per_row, 1e-9))))
+            # enough rows that the dynamic schedule keeps every thread busy
+            rows = max(8 * nthreads, min(len(w["cz"]), int(seconds / max(per_row, 1e-9))))
             stride = max(1, len(w["cz"]) // rows)
         sub = w["cz"][::stride]
         return dict(w, cz=sub), f"every {stride}th cosine row ({len(sub)} x {len(w['en'])} bins), nu+nubar"
@@ -395,7 +396,7 @@ def run_reference(args):
     w = workload(args.workload)
     orc = Oracle(fast=True)
     cores = os.cpu_count() or 1
-    sample_w, desc = cpu_sample(w, args.cpu_seconds / 4.0, orc, cores)
+    sample_w, desc = cpu_sample(w, args.cpu_seconds, orc, cores)
     for _ in range(args.warmup):
         cpu_run(sample_w, orc, cores)
     rates = [cpu_run(sample_w, orc, cores) for _ in range(args.steps)]

@@ -298,10 +298,11 @@ constexpr float kTwoPiB = 1.9353071693331003e-3f;   // float(2pi - A)
 constexpr float kTwoPiC = 1.0253376273028358e-11f;  // float(2pi - A - B)
 constexpr float kInvTwoPi = 0.15915494309189535f;
 
-// Double-float product x = (ah + al)(bh + bl) reduced to [-pi, pi] (error ~1e-9 rad for
-// |x| < 1e4).  The exact product of the leading parts comes from an FMA (Dekker/Ogita
-// TwoProduct), the cross terms are added to the error word, then Cody-Waite reduction.
-__device__ __forceinline__ float reduced_phase(float ah, float al, float bh, float bl) {
+// Double-float product x = (ah + al)(bh + bl) reduced to [-pi, pi], returned as r + lo with
+// |lo| <= ulp(r)/2 (error of the pair ~1e-9 rad for |x| < 1e4).  The exact product of the
+// leading parts comes from an FMA (Dekker/Ogita TwoProduct), the cross terms go to the error
+// word, then a three-part Cody-Waite reduction; the last addition's remainder is kept.
+__device__ __forceinline__ float reduced_phase(float ah, float al, float bh, float bl, float& lo) {
     const float p = ah * bh;
     float e = fmaf(ah, bh, -p);
     e = fmaf(ah, bl, e);
@@ -310,7 +311,49 @@ __device__ __forceinline__ float reduced_phase(float ah, float al, float bh, flo
     float r = fmaf(-n, kTwoPiA, p);
     r = fmaf(-n, kTwoPiB, r);
     r = fmaf(-n, kTwoPiC, r);
-    return r + e;
+    const float s = r + e;
+    lo = (r - s) + e;  // Fast2Sum remainder (|r| >= |e| or r = 0)
+    return s;
+}
+
+// sin and cos of |x| <= pi/2 from their Taylor series about 0, terms to x^15 and x^16
+// (truncation below 1e-9 on the interval), Horner form with FMA.
+__device__ __forceinline__ void taylor_sincos(float x, float& s, float& c) {
+    const float x2 = x * x;
+    float ps = -7.647163732e-13f;       // -1/15!
+    ps = fmaf(ps, x2, 1.605904384e-10f);  // 1/13!
+    ps = fmaf(ps, x2, -2.505210839e-08f); // -1/11!
+    ps = fmaf(ps, x2, 2.755731922e-06f);  // 1/9!
+    ps = fmaf(ps, x2, -1.984126984e-04f); // -1/7!
+    ps = fmaf(ps, x2, 8.333333333e-03f);  // 1/5!
+    ps = fmaf(ps, x2, -1.666666667e-01f); // -1/3!
+    s = fmaf(ps * x2, x, x);
+    float pc = 4.779477332e-14f;          // 1/16!
+    pc = fmaf(pc, x2, -1.147074560e-11f); // -1/14!
+    pc = fmaf(pc, x2, 2.087675699e-09f);  // 1/12!
+    pc = fmaf(pc, x2, -2.755731922e-07f); // -1/10!
+    pc = fmaf(pc, x2, 2.480158730e-05f);  // 1/8!
+    pc = fmaf(pc, x2, -1.388888889e-03f); // -1/6!
+    pc = fmaf(pc, x2, 4.166666667e-02f);  // 1/4!
+    pc = fmaf(pc, x2, -5.000000000e-01f); // -1/2!
+    c = fmaf(pc, x2, 1.0f);
+}
+
+// z = e^{-i (r + lo)} - 1 for |r| <= pi.  |r| > pi/2 is reflected through pi (pi_f - |r| is
+// exact by Sterbenz, then the low part of pi), (sin, cos) are renormalised to unit modulus
+// so that every layer matrix built from z stays unitary to rounding, and the remainder lo
+// enters to first order: e^{-i lo} = 1 - i lo.
+__device__ __forceinline__ void unit_phase_minus_one(float r, float lo, float& zre, float& zim) {
+    const float a = fabsf(r);
+    const bool refl = a > 1.57079637f;
+    const float x = refl ? (3.14159274f - a) + -8.74227766e-8f : a;
+    float sx, cx;
+    taylor_sincos(x, sx, cx);
+    const float inv = rsqrtf(fmaf(sx, sx, cx * cx));
+    const float sn = copysignf(sx * inv, r);
+    const float cs = (refl ? -cx : cx) * inv;
+    zre = fmaf(-lo, sn, cs - 1.0f);
+    zim = fmaf(-lo, cs, -sn);
 }
 
 __device__ __forceinline__ cf cmulf(cf a, cf b) {

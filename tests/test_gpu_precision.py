@@ -1,0 +1,31 @@
+"""The precision study at full size: 59 equal shells, 2000 cos x 2000 log-E (0.1-100 GeV),
+neutrino and antineutrino.  FP64 kernel against the oracle on a slice of cosine rows
+(<= 1e-12), then the mixed kernel against the FP64 kernel on every one of the 4e6 bins and
+every channel (<= 1e-5, the mixed-precision bar)."""
+import os
+
+import numpy as np
+import pytest
+
+from cudaprob3_gb300 import earth
+from tests.gpu_helpers import run_atmos
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("anti", [False, True])
+def test_precision_study_59_shells_full_grid(oracle, anti):
+    from oracle.oracle import Mixing as OMix
+    m = earth.NOMINAL
+    mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+    knu = -1 if anti else 1
+    r, rho, ye = earth.synthetic_shells(59)
+    cz, en = earth.cosine_grid(2000), earth.log_energy_grid(2000)
+    f64 = run_atmos("fp64", mix6, knu, anti, cz, en, r, rho, ye, 22.0)
+    mixed = run_atmos("mixed", mix6, knu, anti, cz, en, r, rho, ye, 22.0)
+    rows = np.concatenate([np.arange(0, 40), np.arange(40, 2000, 97)])  # all deep rows + a spread
+    ref = oracle.atmos(OMix(*mix6[:4], mix6[4], mix6[5], knu), anti, cz[rows], en, r, rho, ye,
+                       22.0, nthreads=os.cpu_count() or 1)
+    assert np.abs(f64[rows] - ref).max() <= 1e-12
+    err = np.abs(mixed - f64).max(axis=(0, 1))  # per channel
+    assert err.max() <= 1e-5, err

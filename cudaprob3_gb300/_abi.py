@@ -19,7 +19,7 @@ EXPORTS = (
     "cp3_set_production_height_averaging", "cp3_calculate", "cp3_calculate_async",
     "cp3_synchronize", "cp3_get_probability", "cp3_get_probability_beam",
     "cp3_get_probability_arr", "cp3_device_result", "cp3_copy_result_async",
-    "cp3_trajectory_table", "cp3_set_profiling", "cp3_kernel_times",
+    "cp3_trajectory_table", "cp3_set_profiling", "cp3_kernel_times", "cp3_atmos_mixed_noalloc",
 )
 
 CP3_OK = 0
@@ -59,6 +59,10 @@ _SIGS = {
     "cp3_trajectory_table": ([_dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, C.c_int, C.c_double,
                               _ip, _ip, _ip, _dp, _dp, _ip, _dp], C.c_int),
     "cp3_set_profiling": ([_h, C.c_int], C.c_int),
+    "cp3_atmos_mixed_noalloc": ([C.c_int, C.c_void_p, C.c_int, _ip, _dp, _ip, C.c_int, _dp, C.c_int]
+                                + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double, C.c_int,
+                                                      C.c_void_p, C.c_void_p, C.c_char_p,
+                                                      C.c_size_t], C.c_int),
     "cp3_kernel_times": ([_h, _dp, _dp], C.c_int),
 }
 

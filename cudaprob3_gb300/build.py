@@ -28,6 +28,7 @@ UNITS = [
     ("cp3_abi.cu", []),
     ("cp3_tables.cu", ["-fmad=false"]),
     ("cp3_atmos.cu", []),
+    ("cp3_noalloc.cu", []),
 ]
 
 

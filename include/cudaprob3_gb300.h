@@ -199,6 +199,49 @@ int cp3_set_profiling(cp3_propagator* h, int enable);
  * per-bin kernel, milliseconds.  eigen_ms is 0 where no table kernel runs (beam). */
 int cp3_kernel_times(cp3_propagator* h, double* eigen_ms, double* bins_ms);
 
+/* ---- atmospheric propagation without allocation ------------------------------------------ */
+
+/* Size of the device scratch behind cp3_atmos_mixed_noalloc (reserved on every GPU that
+ * loads the library, for the life of the process). */
+#define CP3_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
+
+/* No counterpart in the reference: an addition for callers that cannot allocate device
+ * memory when they propagate -- a fitter whose memory pool owns the whole GPU, code that
+ * must not call cudaMalloc (it can synchronise the device, or is forbidden where the call
+ * happens), or a host loop that must not touch any allocator.
+ *
+ * Computes what a CP3_MIXED atmospheric handle computes, for one oscillation-parameter set
+ * and one neutrino type, without allocating anything: no cudaMalloc/cudaFree, no host heap.
+ * Its working memory (the staged trajectory table and the per-(class, energy) eigen table)
+ * is one fixed device array of CP3_NOALLOC_SCRATCH_BYTES; a grid that does not fit is
+ * rejected with CP3_ERR_BAD_SIZE before anything runs.  The headline 59-shell 2000 x 2000
+ * grid fits.
+ *
+ * Inputs and outputs stay the caller's:
+ *   d_energies   device, n_energies doubles (GeV)
+ *   seg_offset, seg_len_km, seg_class, class_rho_e   host arrays, exactly as filled by
+ *                cp3_trajectory_table for the caller's cosines, model and production height
+ *                (validated here, then copied in; pageable arrays may be reused as soon as
+ *                the call returns, page-locked ones once the stream has passed this call)
+ *   d_out        device, 9 * n_cosines * n_energies floats, layout [9][n_cosines][n_energies]
+ *   stream       cudaStream_t (NULL = the legacy default stream); the call is asynchronous
+ *                with respect to the device
+ *   err          optional buffer for a message on failure (err_len bytes, NUL-terminated)
+ *
+ * Every call on a device shares the one scratch array, which keeps the last call's
+ * contents; nothing in it has to start at zero (each call writes every element it reads).
+ * Calls whose work overlaps on the GPU (other streams, or other host threads) race on that
+ * array: order them on one stream or synchronise between them.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress, with that device
+ * current); make that first call before any stream capture on the device. */
+int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int n_energies,
+                            const int* seg_offset, const double* seg_len_km,
+                            const int* seg_class, int n_cosines, const double* class_rho_e,
+                            int n_classes, double theta12, double theta13, double theta23,
+                            double dcp, int knutype, double dm12sq, double dm23sq,
+                            int neutrino_type, float* d_out, void* stream, char* err,
+                            size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

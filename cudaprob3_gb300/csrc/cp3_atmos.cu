@@ -159,22 +159,17 @@ __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1
     }
 }
 
-__device__ __forceinline__ void segment_matrix_mixed(const float* __restrict__ t, int ne_pad,
-                                                     float2 L, cs6& S) {
-    float z[2][2], P1[6], P2[6];
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        const float wh = __ldg(t + (size_t)(12 + 2 * k) * ne_pad);
-        const float wl = __ldg(t + (size_t)(13 + 2 * k) * ne_pad);
-        float lo;
-        const float r = reduced_phase(wh, wl, L.x, L.y, lo);
-        unit_phase_minus_one(r, lo, z[k][0], z[k][1]);
-    }
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-        P1[q] = __ldg(t + (size_t)q * ne_pad);
-        P2[q] = __ldg(t + (size_t)(6 + q) * ne_pad);
-    }
+// t points at this bin's 64-byte table entry: P1[6], P2[6], omega_1 (hi, lo), omega_2.
+__device__ __forceinline__ void segment_matrix_mixed(const float* __restrict__ t, float2 L, cs6& S) {
+    const float4* t4 = reinterpret_cast<const float4*>(t);
+    const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2), w = __ldg(t4 + 3);
+    const float P1[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+    const float P2[6] = {b.z, b.w, c.x, c.y, c.z, c.w};
+    float z[2][2], lo;
+    float r = reduced_phase(w.x, w.y, L.x, L.y, lo);
+    unit_phase_minus_one(r, lo, z[0][0], z[0][1]);
+    r = reduced_phase(w.z, w.w, L.x, L.y, lo);
+    unit_phase_minus_one(r, lo, z[1][0], z[1][1]);
     layer_matrix(z, P1, P2, S);
 }
 
@@ -306,11 +301,11 @@ __global__ void __launch_bounds__(kBlock)
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
     const size_t cls_stride = (size_t)kMixFields * ne_pad;
-    const float* tab = table + ie;
+    const float* tab = table + (size_t)ie * kMixFields;
     const int M = nseg - 1;
 
     cs6 S0;
-    segment_matrix_mixed(tab + s_cls[0] * cls_stride, ne_pad, s_len[0], S0);
+    segment_matrix_mixed(tab + s_cls[0] * cls_stride, s_len[0], S0);
     cg9 A2;
     if (M == 0) {
         sym_to_gen(S0, A2);
@@ -318,17 +313,17 @@ __global__ void __launch_bounds__(kBlock)
         cs6 S;
         cg9 B;
         if (M == 1) {
-            segment_matrix_mixed(tab + s_cls[1] * cls_stride, ne_pad, s_len[1], S);
+            segment_matrix_mixed(tab + s_cls[1] * cls_stride, s_len[1], S);
             sym_to_gen(S, B);  // B = S_1, Q = S_1
             mul_gs(B, S0, A2);
         } else {
-            segment_matrix_mixed(tab + s_cls[1] * cls_stride, ne_pad, s_len[1], S);
+            segment_matrix_mixed(tab + s_cls[1] * cls_stride, s_len[1], S);
             sym_to_gen(S, B);
             for (int l = 2; l < M; l++) {
-                segment_matrix_mixed(tab + s_cls[l] * cls_stride, ne_pad, s_len[l], S);
+                segment_matrix_mixed(tab + s_cls[l] * cls_stride, s_len[l], S);
                 mul_sg(S, B, B);
             }
-            segment_matrix_mixed(tab + s_cls[M] * cls_stride, ne_pad, s_len[M], S);
+            segment_matrix_mixed(tab + s_cls[M] * cls_stride, s_len[M], S);
             cg9 X;
             mul_sg(S, B, X);  // X = S_M B
             cs6 Q;            // Q = B^T X (symmetric)
@@ -354,32 +349,24 @@ __global__ void __launch_bounds__(kBlock)
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out + (size_t)ic * ne + ie, plane);
 }
 
-// Beam, mixed: per-bin FP64 eigen-decomposition, FP64 phase reduction, FP32 matrix work.
+// Beam, mixed: per-bin eigen-decomposition with double-float refinement
+// (rotated_eigen_mixed), double-float phase, FP32 matrix work.
 __global__ void __launch_bounds__(kBlock)
     beam_mixed_kernel(const __grid_constant__ OscParams p, WParams w,
-                      const double* __restrict__ energies, int ne, double rho_e, double L,
+                      const double* __restrict__ energies, int ne, double rho_e, float2 L,
                       float* __restrict__ out) {
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    double P[2][6], om[2];
-    rotated_eigen_f64(&p, energies[ie], rho_e, P, om);
-    float z[2][2], P1[6], P2[6];
+    float P[2][6], om[2][2], z[2][2];
+    rotated_eigen_mixed(&p, energies[ie], rho_e, P, om);
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-        const double x = om[k] * L;
-        const double n = rint(x * (1.0 / (2.0 * M_PI)));
-        // 2 pi = 6.283185307179586 + 2.4492935982947064e-16 (double-double)
-        const double rd = fma(-n, 2.4492935982947064e-16, fma(-n, 6.283185307179586, x));
-        const float r = (float)rd;
-        unit_phase_minus_one(r, (float)(rd - (double)r), z[k][0], z[k][1]);
-    }
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-        P1[q] = (float)P[0][q];
-        P2[q] = (float)P[1][q];
+        float lo;
+        const float r = reduced_phase(om[k][0], om[k][1], L.x, L.y, lo);
+        unit_phase_minus_one(r, lo, z[k][0], z[k][1]);
     }
     cs6 S;
-    layer_matrix(z, P1, P2, S);
+    layer_matrix(z, P[0], P[1], S);
     cg9 A2;
     sym_to_gen(S, A2);
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out + ie, (size_t)ne);
@@ -424,8 +411,10 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
 cudaError_t launch_beam_mixed(const OscParams& p, const double* energies, int ne, double rho_e,
                               double L_km, float* out, cudaStream_t s) {
     if (ne <= 0) return cudaSuccess;
+    const float Lh = (float)L_km;
+    const float2 L = make_float2(Lh, (float)(L_km - (double)Lh));
     beam_mixed_kernel<<<(ne + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, wparams(p), energies, ne,
-                                                                    rho_e, L_km, out);
+                                                                    rho_e, L, out);
     return cudaGetLastError();
 }
 

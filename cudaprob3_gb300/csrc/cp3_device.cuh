@@ -13,6 +13,20 @@
 
 namespace cp3 {
 
+// Pure arithmetic: callable from the host as well (the CPU checks of the mixed solver).
+#define CP3_HD __host__ __device__ __forceinline__
+
+// Separately rounded float product / sum, never fused by the compiler: the error-free
+// transformations below rely on it (a product contracted into the following addition
+// would make TwoSum / Fast2Sum / TwoProduct inexact).
+#ifdef __CUDA_ARCH__
+#define CP3_FMUL(a, b) __fmul_rn((a), (b))
+#define CP3_FADD(a, b) __fadd_rn((a), (b))
+#else
+#define CP3_FMUL(a, b) ((a) * (b))
+#define CP3_FADD(a, b) ((a) + (b))
+#endif
+
 struct cd {
     double re, im;
 };
@@ -26,7 +40,7 @@ struct cf {
 // physics::getMfast (physics.hpp:267-340): matter eigenvalues of 2E.H (eV^2), ordered by the
 // vacuum root order.  Returns mm[i]; the reference's dmMatVac[i][j] = mm[i] - DM(j,0) and
 // dmMatMat[i][j] = mm[i] - mm[j].
-__device__ __forceinline__ void matter_masses_f64(const OscParams* __restrict__ p, double E,
+CP3_HD void matter_masses_f64(const OscParams* __restrict__ p, double E,
                                                   double rho, double mm[3]) {
     const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
     const double d01 = CP3_DM(p, 0, 1), d02 = CP3_DM(p, 0, 2);
@@ -62,7 +76,7 @@ __device__ __forceinline__ void matter_masses_f64(const OscParams* __restrict__ 
 
 // physics::get_product (physics.hpp:345-430) + getC (:459-514): the flavour-basis projectors
 // C[k][a][b] of the expansion T = sum_k C_k exp(i arg_k).
-__device__ __forceinline__ void flavour_projectors_f64(const OscParams* __restrict__ p, double E,
+CP3_HD void flavour_projectors_f64(const OscParams* __restrict__ p, double E,
                                                        double rho, const double mm[3],
                                                        cd C[3][3][3]) {
     const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
@@ -155,7 +169,7 @@ __device__ __forceinline__ void flavour_projectors_f64(const OscParams* __restri
 
 // physics::get_product + getA (physics.hpp:345-430, 516-598): the beam amplitude
 // A = U (sum_k e^{i arg_k} prod_k) U^dagger through AXFAC.  A[n][m]: row = final flavour.
-__device__ __forceinline__ void beam_amplitude_f64(const OscParams* __restrict__ p, double E,
+CP3_HD void beam_amplitude_f64(const OscParams* __restrict__ p, double E,
                                                    double rho, double L, cd A[3][3]) {
     double mm[3];
     matter_masses_f64(p, E, rho, mm);
@@ -248,7 +262,7 @@ __host__ __device__ constexpr int sidx(int i, int j) {
 //   P_k = (H - m_a)(H - m_b) / ((m_k - m_a)(m_k - m_b)),  {a, b} = the other two,
 // (P_0 = 1 - P_1 - P_2), and the phase rates relative to eigenvalue 0 are
 //   omega_k = 2.534 (m_k - m_0) / E   [rad / km].
-__device__ __forceinline__ void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
+CP3_HD void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
                                                   double rho, double P[2][6], double om[2]) {
     double mm[3];
     matter_masses_f64(p, E, rho, mm);
@@ -302,8 +316,8 @@ constexpr float kInvTwoPi = 0.15915494309189535f;
 // |lo| <= ulp(r)/2 (error of the pair ~1e-9 rad for |x| < 1e4).  The exact product of the
 // leading parts comes from an FMA (Dekker/Ogita TwoProduct), the cross terms go to the error
 // word, then a three-part Cody-Waite reduction; the last addition's remainder is kept.
-__device__ __forceinline__ float reduced_phase(float ah, float al, float bh, float bl, float& lo) {
-    const float p = ah * bh;
+CP3_HD float reduced_phase(float ah, float al, float bh, float bl, float& lo) {
+    const float p = CP3_FMUL(ah, bh);
     float e = fmaf(ah, bh, -p);
     e = fmaf(ah, bl, e);
     e = fmaf(al, bh, e);
@@ -311,14 +325,14 @@ __device__ __forceinline__ float reduced_phase(float ah, float al, float bh, flo
     float r = fmaf(-n, kTwoPiA, p);
     r = fmaf(-n, kTwoPiB, r);
     r = fmaf(-n, kTwoPiC, r);
-    const float s = r + e;
-    lo = (r - s) + e;  // Fast2Sum remainder (|r| >= |e| or r = 0)
+    const float s = CP3_FADD(r, e);
+    lo = CP3_FADD(CP3_FADD(r, -s), e);  // Fast2Sum remainder (|r| >= |e| or r = 0)
     return s;
 }
 
 // sin and cos of |x| <= pi/2 from their Taylor series about 0, terms to x^15 and x^16
 // (truncation below 1e-9 on the interval), Horner form with FMA.
-__device__ __forceinline__ void taylor_sincos(float x, float& s, float& c) {
+CP3_HD void taylor_sincos(float x, float& s, float& c) {
     const float x2 = x * x;
     float ps = -7.647163732e-13f;       // -1/15!
     ps = fmaf(ps, x2, 1.605904384e-10f);  // 1/13!
@@ -343,7 +357,7 @@ __device__ __forceinline__ void taylor_sincos(float x, float& s, float& c) {
 // exact by Sterbenz, then the low part of pi), (sin, cos) are renormalised to unit modulus
 // so that every layer matrix built from z stays unitary to rounding, and the remainder lo
 // enters to first order: e^{-i lo} = 1 - i lo.
-__device__ __forceinline__ void unit_phase_minus_one(float r, float lo, float& zre, float& zim) {
+CP3_HD void unit_phase_minus_one(float r, float lo, float& zre, float& zim) {
     const float a = fabsf(r);
     const bool refl = a > 1.57079637f;
     const float x = refl ? (3.14159274f - a) + -8.74227766e-8f : a;
@@ -356,7 +370,142 @@ __device__ __forceinline__ void unit_phase_minus_one(float r, float lo, float& z
     zim = fmaf(-lo, cs, -sn);
 }
 
-__device__ __forceinline__ cf cmulf(cf a, cf b) {
+// ---------------------------------------------------------------------------------------
+// Double-float ("df64") arithmetic on the FP32 pipe: a value is hi + lo with |lo| <=
+// ulp(hi)/2, ~48 significant bits.  Error-free transformations: TwoSum (Knuth),
+// Fast2Sum (Dekker), TwoProduct through FMA; the sums are the "sloppy" variant (one
+// renormalisation), which is accurate to a few df64 ulps of the larger operand.
+
+struct df {
+    float hi, lo;
+};
+
+CP3_HD df df_from(double x) {
+    const float h = (float)x;
+    return df{h, (float)(x - (double)h)};
+}
+CP3_HD df df_fast2sum(float a, float b) {  // |a| >= |b|
+    const float s = CP3_FADD(a, b);
+    return df{s, CP3_FADD(b, -CP3_FADD(s, -a))};
+}
+CP3_HD df df_add(df x, df y) {
+    const float s = CP3_FADD(x.hi, y.hi);
+    const float bb = CP3_FADD(s, -x.hi);
+    float e = CP3_FADD(CP3_FADD(x.hi, -CP3_FADD(s, -bb)), CP3_FADD(y.hi, -bb));
+    e = CP3_FADD(e, CP3_FADD(x.lo, y.lo));
+    return df_fast2sum(s, e);
+}
+CP3_HD df df_neg(df x) { return df{-x.hi, -x.lo}; }
+CP3_HD df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+CP3_HD df df_mul(df x, df y) {
+    const float p = CP3_FMUL(x.hi, y.hi);
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+    return df_fast2sum(p, e);
+}
+CP3_HD df df_mulf(df x, float y) {
+    const float p = CP3_FMUL(x.hi, y);
+    const float e = fmaf(x.hi, y, -p);
+    return df_fast2sum(p, fmaf(x.lo, y, e));
+}
+// 1 / x to df64 accuracy: float reciprocal, then one Newton step in df64.
+CP3_HD df df_recip(df x) {
+    const float r = 1.0f / x.hi;
+    const df one_minus = df_sub(df{1.0f, 0.0f}, df_mulf(x, r));  // 1 - x r, small
+    return df_add(df{r, 0.0f}, df_mulf(one_minus, r));
+}
+
+// The mixed kernels' eigen-decomposition without FP64 on the common path:
+//   1. V = -fac (matter potential in 2E.H units, eV^2) and the cubic's coefficients in df64;
+//   2. the three roots from the trigonometric solution in FP32;
+//   3. two Newton steps per root on the df64 polynomial (the third root from the trace);
+//   4. P1, P2 = (H - m_a)(H - m_b)/((m_k - m_a)(m_k - m_b)) in df64, rounded to float;
+//      omega_k = 2.534 (m_k - m_0) / E in df64 (hi, lo).
+// Where two refined roots lie closer than 1e-4 of the spread (exactly degenerate vacuum
+// masses, the reference's 5e-9 eV^2 degeneracy break) the FP64 reference cubic takes over.
+CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
+                                                    double rho, float P[2][6], float om[2][2]) {
+    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
+    const df V = df_from(-fac);
+    // det(l - H) = l^3 - c2 l^2 + c1 l - c0 with H = H0 + V e0 e0^T (OscParams::cpoly)
+    const df c2 = df_add(df_from(p->cpoly[0]), V);
+    const df c1 = df_add(df_from(p->cpoly[1]), df_mul(V, df_from(p->cpoly[3])));
+    const df c0 = df_add(df_from(p->cpoly[2]), df_mul(V, df_from(p->cpoly[4])));
+    // FP32 trigonometric roots of l^3 - c2 l^2 + c1 l - c0
+    const float a2 = c2.hi, a1 = c1.hi, a0 = c0.hi;
+    const float s = a2 * (1.0f / 3.0f);
+    const float pp = fmaf(-a2, s, a1);                        // c1 - c2^2/3  (< 0)
+    const float qq = fmaf(s, fmaf(-2.0f * s, s, a1), -a0);    // -(2 s^3 - s c1 + c0)
+    const float mp3 = fmaxf(-pp * (1.0f / 3.0f), 1e-30f);
+    const float rt = sqrtf(mp3);
+    // t = 2 sqrt(m) cos(a) solves t^3 + P t + Q = 0 when cos(3a) = -Q / (2 m^{3/2})
+    const float carg = fminf(1.0f, fmaxf(-1.0f, (-0.5f * qq) / (mp3 * rt)));
+    const float th = acosf(carg) * (1.0f / 3.0f);
+    float l0 = fmaf(2.0f * rt, cosf(th), s);
+    float l1 = fmaf(2.0f * rt, cosf(th - 2.0943951f), s);
+    df r[3] = {df{l0, 0.0f}, df{l1, 0.0f}, df{0.0f, 0.0f}};
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+            const df x = r[k];
+            const df f = df_sub(df_mul(df_add(df_mul(df_sub(x, c2), x), c1), x), c0);
+            const df d = df_add(df_mul(df_sub(df_mulf(x, 3.0f), df_mulf(c2, 2.0f)), x), c1);
+            r[k] = df_sub(x, df{f.hi / d.hi, 0.0f});
+        }
+    r[2] = df_sub(df_sub(c2, r[0]), r[1]);
+    const float spread = fmaxf(fabsf(r[0].hi - r[1].hi), fmaxf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
+    const float gap = fminf(fabsf(r[0].hi - r[1].hi), fminf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
+    if (!(gap > 1e-4f * spread)) {
+        double Pd[2][6], omd[2];
+        rotated_eigen_f64(p, E, rho, Pd, omd);
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+#pragma unroll
+            for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
+            om[k][0] = (float)omd[k];
+            om[k][1] = (float)(omd[k] - (double)om[k][0]);
+        }
+        return;
+    }
+    df h[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) h[q] = df_from(p->h0[q]);
+    h[0] = df_add(h[0], V);
+    const df loe = df_from(kLoEFac / E);
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++) {
+        const int k = kk + 1, a = 0, b = k == 1 ? 2 : 1;
+        df A[6], B[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            A[q] = h[q];
+            B[q] = h[q];
+        }
+        A[0] = df_sub(A[0], r[a]);
+        A[3] = df_sub(A[3], r[a]);
+        A[5] = df_sub(A[5], r[a]);
+        B[0] = df_sub(B[0], r[b]);
+        B[3] = df_sub(B[3], r[b]);
+        B[5] = df_sub(B[5], r[b]);
+        const df inv = df_recip(df_mul(df_sub(r[k], r[a]), df_sub(r[k], r[b])));
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = i; j < 3; j++) {
+                df acc = df_mul(A[sidx(i, 0)], B[sidx(0, j)]);
+                acc = df_add(acc, df_mul(A[sidx(i, 1)], B[sidx(1, j)]));
+                acc = df_add(acc, df_mul(A[sidx(i, 2)], B[sidx(2, j)]));
+                const df pv = df_mul(acc, inv);
+                P[kk][sidx(i, j)] = pv.hi + pv.lo;
+            }
+        const df w = df_mul(df_sub(r[k], r[0]), loe);
+        om[kk][0] = w.hi;
+        om[kk][1] = w.lo;
+    }
+}
+
+CP3_HD cf cmulf(cf a, cf b) {
     return cf{fmaf(a.re, b.re, -a.im * b.im), fmaf(a.re, b.im, a.im * b.re)};
 }
 

@@ -104,6 +104,13 @@ void build_osc_params(const MixingInput& m, int antineutrino, OscParams* o) {
         const int i = ij[q][0], j = ij[q][1];
         o->h0[q] = O[i][0] * O[j][0] * dk[0] + O[i][1] * O[j][1] * dk[1] + O[i][2] * O[j][2] * dk[2];
     }
+    const double* h = o->h0;
+    o->cpoly[0] = h[0] + h[3] + h[5];
+    o->cpoly[1] = h[0] * h[3] - h[1] * h[1] + h[0] * h[5] - h[2] * h[2] + h[3] * h[5] - h[4] * h[4];
+    o->cpoly[2] = h[0] * (h[3] * h[5] - h[4] * h[4]) - h[1] * (h[1] * h[5] - h[4] * h[2]) +
+                  h[2] * (h[1] * h[4] - h[3] * h[2]);
+    o->cpoly[3] = h[3] + h[5];
+    o->cpoly[4] = h[3] * h[5] - h[4] * h[4];
     o->w[0] = c23;
     o->w[1] = s23;
     o->w[2] = cd;

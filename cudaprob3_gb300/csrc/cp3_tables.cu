@@ -44,8 +44,10 @@ __global__ void __launch_bounds__(kTableBlock)
 }
 
 // Mixed table: real projectors P1, P2 of H0 + V e0 e0^T and the phase rates
-// omega_k = 2.534 (m_k - m_0) / E split into float pairs.  Field layout as above with
-// kMixFields: 0-5 P1, 6-11 P2 (00,01,02,11,12,22), 12/13 omega_1 hi/lo, 14/15 omega_2.
+// omega_k = 2.534 (m_k - m_0) / E as float pairs (rotated_eigen_mixed: FP32 roots refined in
+// double-float; FP64 only where two roots nearly coincide).  One 64-byte entry per
+// (class c, energy e) at table[(c * ne_pad + e) * 16]: P1 (00,01,02,11,12,22), P2, then
+// omega_1 hi/lo, omega_2 hi/lo -- four 16-byte words a thread reads with vector loads.
 __global__ void __launch_bounds__(kTableBlock)
     table_mixed_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
                        int ne, int ne_pad, const double* __restrict__ cls_rho,
@@ -53,17 +55,13 @@ __global__ void __launch_bounds__(kTableBlock)
     const int ie = blockIdx.x * kTableBlock + threadIdx.x;
     const int c = blockIdx.y;
     if (ie >= ne) return;
-    double P[2][6], om[2];
-    rotated_eigen_f64(&p, energies[ie], cls_rho[c], P, om);
-    float* t = table + (size_t)c * kMixFields * ne_pad + ie;
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-#pragma unroll
-        for (int q = 0; q < 6; q++) t[(size_t)(k * 6 + q) * ne_pad] = (float)P[k][q];
-        const float hi = (float)om[k];
-        t[(size_t)(12 + 2 * k) * ne_pad] = hi;
-        t[(size_t)(13 + 2 * k) * ne_pad] = (float)(om[k] - (double)hi);
-    }
+    float P[2][6], om[2][2];
+    rotated_eigen_mixed(&p, energies[ie], cls_rho[c], P, om);
+    float4* t = reinterpret_cast<float4*>(table + ((size_t)c * ne_pad + ie) * kMixFields);
+    t[0] = make_float4(P[0][0], P[0][1], P[0][2], P[0][3]);
+    t[1] = make_float4(P[0][4], P[0][5], P[1][0], P[1][1]);
+    t[2] = make_float4(P[1][2], P[1][3], P[1][4], P[1][5]);
+    t[3] = make_float4(om[0][0], om[0][1], om[1][0], om[1][1]);
 }
 
 // physics::calculate_beam (physics.hpp:1153-1260), one thread per energy; result [9][ne].

@@ -27,6 +27,10 @@ struct alignas(16) OscParams {
     // W = R23 . diag(1,1,e^{i d}) and O = R13 . R12 real, so 2E.H = W (H0 + V e0 e0^T) W^+.
     double h0[6];        // H0 = O . diag(DM(k,0)) . O^T : 00,01,02,11,12,22 (eV^2)
     double w[4];         // c23, s23, cos d, sin d (d = the dcp actually used in U)
+    // det(l - H0 - V e0 e0^T) = l^3 - (t + V) l^2 + (c + V m) l - (D + V n):
+    // cpoly = {t = tr H0, c = sum of principal 2x2 minors, D = det H0,
+    //          m = h11 + h22, n = h11 h22 - h12^2}
+    double cpoly[5];
     int order[3];        // root order from the vacuum cubic (prepare_getMfast)
     int anti;            // 1: antineutrino sign of the matter potential
     int pad[4];

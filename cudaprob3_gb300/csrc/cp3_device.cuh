@@ -425,12 +425,15 @@ CP3_HD df df_recip(df x) {
 // masses, the reference's 5e-9 eV^2 degeneracy break) the FP64 reference cubic takes over.
 CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
                                                     double rho, float P[2][6], float om[2][2]) {
-    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
-    const df V = df_from(-fac);
+    // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos
+    const df Ed = df_from(E);
+    const df tw = df{1.52588e-4f, -7.040322e-12f};  // kTwoRtTwoGf = hi + lo
+    df V = df_mul(df_mul(tw, Ed), df_from(rho));
+    if (p->anti) V = df_neg(V);
     // det(l - H) = l^3 - c2 l^2 + c1 l - c0 with H = H0 + V e0 e0^T (OscParams::cpoly)
-    const df c2 = df_add(df_from(p->cpoly[0]), V);
-    const df c1 = df_add(df_from(p->cpoly[1]), df_mul(V, df_from(p->cpoly[3])));
-    const df c0 = df_add(df_from(p->cpoly[2]), df_mul(V, df_from(p->cpoly[4])));
+    const df c2 = df_add(df{p->cpolyf[0][0], p->cpolyf[0][1]}, V);
+    const df c1 = df_add(df{p->cpolyf[1][0], p->cpolyf[1][1]}, df_mul(V, df{p->cpolyf[3][0], p->cpolyf[3][1]}));
+    const df c0 = df_add(df{p->cpolyf[2][0], p->cpolyf[2][1]}, df_mul(V, df{p->cpolyf[4][0], p->cpolyf[4][1]}));
     // FP32 trigonometric roots of l^3 - c2 l^2 + c1 l - c0
     const float a2 = c2.hi, a1 = c1.hi, a0 = c0.hi;
     const float s = a2 * (1.0f / 3.0f);
@@ -470,9 +473,9 @@ CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
     }
     df h[6];
 #pragma unroll
-    for (int q = 0; q < 6; q++) h[q] = df_from(p->h0[q]);
+    for (int q = 0; q < 6; q++) h[q] = df{p->h0f[q][0], p->h0f[q][1]};
     h[0] = df_add(h[0], V);
-    const df loe = df_from(kLoEFac / E);
+    const df loe = df_mul(df{2.534f, 8.010864e-08f}, df_recip(Ed));  // kLoEFac (= hi + lo) / E
 #pragma unroll
     for (int kk = 0; kk < 2; kk++) {
         const int k = kk + 1, a = 0, b = k == 1 ? 2 : 1;

@@ -111,6 +111,12 @@ void build_osc_params(const MixingInput& m, int antineutrino, OscParams* o) {
                   h[2] * (h[1] * h[4] - h[3] * h[2]);
     o->cpoly[3] = h[3] + h[5];
     o->cpoly[4] = h[3] * h[5] - h[4] * h[4];
+    auto split = [](double x, float out[2]) {
+        out[0] = (float)x;
+        out[1] = (float)(x - (double)out[0]);
+    };
+    for (int q = 0; q < 6; q++) split(o->h0[q], o->h0f[q]);
+    for (int q = 0; q < 5; q++) split(o->cpoly[q], o->cpolyf[q]);
     o->w[0] = c23;
     o->w[1] = s23;
     o->w[2] = cd;

@@ -31,6 +31,10 @@ struct alignas(16) OscParams {
     // cpoly = {t = tr H0, c = sum of principal 2x2 minors, D = det H0,
     //          m = h11 + h22, n = h11 h22 - h12^2}
     double cpoly[5];
+    // The same numbers as float pairs (hi, lo), split on the host for the double-float
+    // eigen-solver of the mixed kernels.
+    float h0f[6][2];
+    float cpolyf[5][2];
     int order[3];        // root order from the vacuum cubic (prepare_getMfast)
     int anti;            // 1: antineutrino sign of the matter potential
     int pad[4];

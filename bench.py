@@ -59,7 +59,139 @@ def workload(name):
     if name == "beam":
         return dict(kind="beam", en=earth.lin_energy_grid(100000), rho=2.6, L=1300.0,
                     desc="beam, rho=2.6 g/cm^3, L=1300 km, 1e5 E (0.1-10 GeV), nu+nubar")
+    if name == "batch_atmos":
+        sets = earth.gaussian_sets(256, seed=2024)
+        grids = earth.uneven_grids(256, seed=2025)
+        return dict(kind="batch", model=earth.PREM_12LAYER, h=22.0, sets=sets, grids=grids,
+                    beam=None,
+                    desc="batched atmospheric: 256 Gaussian parameter sets (half inverted "
+                         "ordering), own grids n_cos U[100,1000] x n_E U[100,2000], PREM "
+                         "12-layer, h=22 km, nu+nubar (512 problems), one persistent launch")
+    if name == "batch_beam":
+        sets = earth.gaussian_sets(4096, seed=2026)
+        return dict(kind="batch", model=None, h=None, sets=sets, grids=None,
+                    beam=dict(en=earth.lin_energy_grid(100000), rho=2.6, L=[295.0, 1300.0]),
+                    desc="batched beam: 4096 Gaussian parameter sets (half inverted ordering), "
+                         "1e5 E (0.1-10 GeV), rho=2.6, L=295 and 1300 km, nu+nubar "
+                         "(8192 problems), one persistent launch")
     raise SystemExit(f"unknown workload {name}")
+
+
+def build_batch(w):
+    from cudaprob3_gb300 import earth
+    from cudaprob3_gb300.batch import Batch
+    b = Batch(0)
+    flops = 0.0
+    nbins = 0
+    if w["model"] is not None:
+        b.set_earth(*w["model"], w["h"])
+        r = np.asarray(w["model"][0], dtype=np.float64)
+        rd = np.sort(r)[::-1]
+        lim = -np.sqrt(1 - rd ** 2 / 6371.0 ** 2)
+        lim[0] = 0.0
+        for m, (nc, ne) in zip(w["sets"], w["grids"]):
+            cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
+            M = (cz[:, None] < lim[None, :]).sum(axis=1)
+            for anti in (False, True):
+                pid = b.add_atmos(cz, en)
+                b.set_params(pid, m, anti)
+                flops += float(f_bin(M).sum()) * ne
+                nbins += nc * ne
+    else:
+        bw = w["beam"]
+        for m in w["sets"]:
+            for anti in (False, True):
+                pid = b.add_beam(bw["en"], bw["rho"], bw["L"])
+                b.set_params(pid, m, anti)
+                flops += float(f_bin(0)) * len(bw["en"]) * len(bw["L"])
+                nbins += len(bw["en"]) * len(bw["L"])
+    b.commit()
+    return b, flops, nbins
+
+
+def run_batch(args, w, rank, world):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    b, flops, nbins = build_batch(w)
+    t0 = time.perf_counter()
+    b.tune(use_cache=True)
+    tune_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b.run()
+    b.synchronize()
+    ms = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            b.run()
+            ms.append(b.synchronize())
+    t_ms = float(np.mean(ms))
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    probs = 9 * nbins
+    peaks = fma_peaks(dev)
+    achieved = flops / (t_ms * 1e-3) / 1e12
+    info = b.info()
+    line = {
+        "metric": "oscillation probabilities/s (mixed precision, max err <= 1e-5 vs FP64 oracle)",
+        "value": world * probs / (t_ms * 1e-3), "unit": "probabilities/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded parameter sets and grids)",
+        "config": {"workload": args.workload, "description": w["desc"], "precision": "mixed",
+                   "probabilities_per_step": probs, "problems": info["problems"],
+                   "tiles": info["tiles"], "result_bytes": info["result_bytes"],
+                   "tile_shape": b.shape(), "autotune_s": round(tune_s, 2),
+                   "l2": f"per-run output {info['result_bytes'] / 1e9:.1f} GB exceeds L2"},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
+                     "peak": round(peaks["fp32"], 3), "unit": "TFLOP/s",
+                     "frac": round(achieved / peaks["fp32"], 4), "traffic": None,
+                     "kernel": "batch_kernel (one persistent launch per step)",
+                     "flops_per_launch": flops,
+                     "hbm_gbs_output": round(info["result_bytes"] / (t_ms * 1e-3) / 1e9, 1)},
+        "peaks_tflops": peaks,
+    }
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        line["roofline"]["hbm_frac_of_measured"] = round(line["roofline"]["hbm_gbs_output"] / mp["hbm_gbs"], 4)
+    except (OSError, KeyError, ValueError):
+        pass
+    if rank == 0:
+        line["max_abs_err_vs_oracle"] = check_batch_against_oracle(w, b)
+    line["clocks"] = clk.summary()
+    return line
+
+
+def check_batch_against_oracle(w, b, n_check=4):
+    """A few problems of the timed batch against the CPU oracle."""
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix, Oracle
+    orc = Oracle()
+    errs = []
+    for i in range(n_check):
+        k = (i * 37) % len(w["sets"])
+        m = w["sets"][k]
+        for anti in (False, True):
+            pid = 2 * k + int(anti)
+            om = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, -1 if anti else 1)
+            got = b.result(pid)
+            if w["model"] is not None:
+                nc, ne = w["grids"][k]
+                cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
+                rows = np.arange(0, nc, max(1, nc // 40))
+                ref = orc.atmos(om, anti, cz[rows], en, *w["model"], w["h"], nthreads=os.cpu_count() or 1)
+                errs.append(float(np.abs(np.transpose(got, (1, 2, 0))[rows] - ref).max()))
+            else:
+                bw = w["beam"]
+                for j, L in enumerate(bw["L"]):
+                    ref = orc.beam(om, anti, bw["en"], bw["rho"], L, nthreads=os.cpu_count() or 1)
+                    errs.append(float(np.abs(got[j].T - ref).max()))
+    return max(errs)
 
 
 def shells_crossed(w):
@@ -162,6 +294,8 @@ def run_ours(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     w = workload(args.workload)
+    if w["kind"] == "batch":
+        return run_batch(args, w, rank, world)
     prec = args.precision
     # weak scaling: each rank propagates its own parameter set over the full grid
     m = earth.NOMINAL if rank == 0 else earth.gaussian_sets(world, seed=77)[rank]
@@ -425,7 +559,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="atmos59", choices=["atmos59", "prem4", "beam"])
+    ap.add_argument("--workload", default="atmos59",
+                    choices=["atmos59", "prem4", "beam", "batch_atmos", "batch_beam"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=2.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -20,6 +20,10 @@ EXPORTS = (
     "cp3_synchronize", "cp3_get_probability", "cp3_get_probability_beam",
     "cp3_get_probability_arr", "cp3_device_result", "cp3_copy_result_async",
     "cp3_trajectory_table", "cp3_set_profiling", "cp3_kernel_times", "cp3_atmos_mixed_noalloc",
+    "cp3_batch_create", "cp3_batch_destroy", "cp3_batch_last_error", "cp3_batch_set_earth",
+    "cp3_batch_add_atmos", "cp3_batch_add_beam", "cp3_batch_set_params", "cp3_batch_commit",
+    "cp3_batch_set_shape", "cp3_batch_get_shape", "cp3_batch_tune", "cp3_batch_run",
+    "cp3_batch_synchronize", "cp3_batch_result", "cp3_batch_copy_result", "cp3_batch_info",
 )
 
 CP3_OK = 0
@@ -59,6 +63,24 @@ _SIGS = {
     "cp3_trajectory_table": ([_dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, C.c_int, C.c_double,
                               _ip, _ip, _ip, _dp, _dp, _ip, _dp], C.c_int),
     "cp3_set_profiling": ([_h, C.c_int], C.c_int),
+    "cp3_batch_create": ([C.c_int, C.POINTER(_h)], C.c_int),
+    "cp3_batch_destroy": ([_h], C.c_int),
+    "cp3_batch_last_error": ([_h], C.c_char_p),
+    "cp3_batch_set_earth": ([_h, _dp, _dp, _dp, C.c_int, C.c_double], C.c_int),
+    "cp3_batch_add_atmos": ([_h, _dp, C.c_int, _dp, C.c_int, _ip], C.c_int),
+    "cp3_batch_add_beam": ([_h, _dp, C.c_int, C.c_double, _dp, C.c_int, _ip], C.c_int),
+    "cp3_batch_set_params": ([_h, C.c_int] + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double,
+                                                                    C.c_int], C.c_int),
+    "cp3_batch_commit": ([_h], C.c_int),
+    "cp3_batch_set_shape": ([_h, C.c_int, C.c_int, C.c_int], C.c_int),
+    "cp3_batch_get_shape": ([_h, _ip, _ip, _ip], C.c_int),
+    "cp3_batch_tune": ([_h, C.c_int], C.c_int),
+    "cp3_batch_run": ([_h, C.c_void_p], C.c_int),
+    "cp3_batch_synchronize": ([_h, _dp], C.c_int),
+    "cp3_batch_result": ([_h, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], C.c_int),
+    "cp3_batch_copy_result": ([_h, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
+    "cp3_batch_info": ([_h, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_size_t),
+                        C.POINTER(C.c_longlong)], C.c_int),
     "cp3_atmos_mixed_noalloc": ([C.c_int, C.c_void_p, C.c_int, _ip, _dp, _ip, C.c_int, _dp, C.c_int]
                                 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double, C.c_int,
                                                       C.c_void_p, C.c_void_p, C.c_char_p,

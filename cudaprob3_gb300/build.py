@@ -29,6 +29,7 @@ UNITS = [
     ("cp3_tables.cu", ["-fmad=false"]),
     ("cp3_atmos.cu", []),
     ("cp3_noalloc.cu", []),
+    ("cp3_batch.cu", []),
 ]
 
 

@@ -9,6 +9,7 @@
 // 32 consecutive elements (128 B in FP32, 256 B in FP64).
 #include "cp3_device.cuh"
 #include "cp3_kernels.hpp"
+#include "cp3_mixed.cuh"
 
 namespace cp3 {
 
@@ -134,156 +135,8 @@ __global__ void __launch_bounds__(kBlock)
         }
 }
 
-// ------------------------------------------------------------------------------------
-// Mixed: the same physics, rearranged for FP32.
-//   T_l = W S_l W^+,  S_l = 1 + z1 P1 + z2 P2,  z_k = e^{-i omega_k L_l} - 1   (symmetric)
-//   A   = W (S_1..S_{M-1}) S_M (S_{M-1}..S_1) S_0 W^+ = W (B^T S_M B) S_0 W^+,
-// with B = S_{M-1}..S_1, because S_l^T = S_l.  That is M+1 complex 3x3 products per bin
-// instead of the reference's 2M-1, on symmetric factors.
-
-struct cs6 {  // complex symmetric 3x3
-    cf a[6];
-};
-struct cg9 {  // complex general 3x3
-    cf a[3][3];
-};
-
-// S = 1 + z1 P1 + z2 P2 from the two phase factors and the real projectors.
-__device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1[6],
-                                             const float P2[6], cs6& S) {
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-        const float one = (q == 0 || q == 3 || q == 5) ? 1.0f : 0.0f;
-        S.a[q].re = fmaf(z[1][0], P2[q], fmaf(z[0][0], P1[q], one));
-        S.a[q].im = fmaf(z[1][1], P2[q], z[0][1] * P1[q]);
-    }
-}
-
-// t points at this bin's 64-byte table entry: P1[6], P2[6], omega_1 (hi, lo), omega_2.
-__device__ __forceinline__ void segment_matrix_mixed(const float* __restrict__ t, float2 L, cs6& S) {
-    const float4* t4 = reinterpret_cast<const float4*>(t);
-    const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2), w = __ldg(t4 + 3);
-    const float P1[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
-    const float P2[6] = {b.z, b.w, c.x, c.y, c.z, c.w};
-    float z[2][2], lo;
-    float r = reduced_phase(w.x, w.y, L.x, L.y, lo);
-    unit_phase_minus_one(r, lo, z[0][0], z[0][1]);
-    r = reduced_phase(w.z, w.w, L.x, L.y, lo);
-    unit_phase_minus_one(r, lo, z[1][0], z[1][1]);
-    layer_matrix(z, P1, P2, S);
-}
-
-// One Newton-Schulz step toward the nearest unitary matrix, A <- A (3 - A^+ A) / 2.  The
-// rounding of FP32 layer matrices leaves each slightly non-unitary and that part of the
-// error accumulates over the ~2M products of a deep trajectory; one step at the end removes
-// it to second order (measured: max error on the 59-shell, 2000 x 2000 grid drops by ~2x).
-__device__ __forceinline__ void newton_schulz(cg9& A) {
-    cg9 G;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            float re = 0.f, im = 0.f;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const cf a = A.a[k][i], b = A.a[k][j];  // conj(a) b
-                re = fmaf(a.re, b.re, fmaf(a.im, b.im, re));
-                im = fmaf(a.re, b.im, fmaf(-a.im, b.re, im));
-            }
-            G.a[i][j] = cf{(i == j ? 1.5f : 0.f) - 0.5f * re, -0.5f * im};
-        }
-    cg9 R;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cf acc = cmulf(A.a[i][0], G.a[0][j]);
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                const cf a = A.a[i][k], g = G.a[k][j];
-                acc.re = fmaf(a.re, g.re, fmaf(-a.im, g.im, acc.re));
-                acc.im = fmaf(a.re, g.im, fmaf(a.im, g.re, acc.im));
-            }
-            R.a[i][j] = acc;
-        }
-    A = R;
-}
-
-// R = S . G (S symmetric)
-__device__ __forceinline__ void mul_sg(const cs6& S, const cg9& G, cg9& R) {
-    cg9 t;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cf acc = cmulf(S.a[sidx(i, 0)], G.a[0][j]);
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                const cf s = S.a[sidx(i, k)], g = G.a[k][j];
-                acc.re = fmaf(s.re, g.re, fmaf(-s.im, g.im, acc.re));
-                acc.im = fmaf(s.re, g.im, fmaf(s.im, g.re, acc.im));
-            }
-            t.a[i][j] = acc;
-        }
-    R = t;
-}
-
-// R = G . S (S symmetric)
-__device__ __forceinline__ void mul_gs(const cg9& G, const cs6& S, cg9& R) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cf acc = cmulf(G.a[i][0], S.a[sidx(0, j)]);
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                const cf g = G.a[i][k], s = S.a[sidx(k, j)];
-                acc.re = fmaf(g.re, s.re, fmaf(-g.im, s.im, acc.re));
-                acc.im = fmaf(g.re, s.im, fmaf(g.im, s.re, acc.im));
-            }
-            R.a[i][j] = acc;
-        }
-}
-
-__device__ __forceinline__ void sym_to_gen(const cs6& S, cg9& G) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) G.a[i][j] = S.a[sidx(i, j)];
-}
-
-// Probabilities of A = W A2 W^+, W = [[1,0,0],[0,c,s e],[0,-s,c e]], e = e^{i d}; stores
-// channel a*3+b = |A[b][a]|^2 at out[ch * plane].
-__device__ __forceinline__ void store_probabilities(const cg9& A2, float c, float s, float ed_re,
-                                                    float ed_im, float* __restrict__ out,
-                                                    size_t plane) {
-    cg9 Y;  // Y = A2 W^+ : columns 1, 2 mix through (c, -s) and e* (s, c)
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const cf a1 = A2.a[i][1], a2 = A2.a[i][2];
-        const cf f{a2.re * ed_re + a2.im * ed_im, a2.im * ed_re - a2.re * ed_im};  // e* a2
-        Y.a[i][0] = A2.a[i][0];
-        Y.a[i][1] = cf{fmaf(c, a1.re, s * f.re), fmaf(c, a1.im, s * f.im)};
-        Y.a[i][2] = cf{fmaf(-s, a1.re, c * f.re), fmaf(-s, a1.im, c * f.im)};
-    }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        const cf y1 = Y.a[1][j], y2 = Y.a[2][j];
-        const cf g{y2.re * ed_re - y2.im * ed_im, y2.re * ed_im + y2.im * ed_re};  // e y2
-        const cf r0 = Y.a[0][j];
-        const cf r1{fmaf(c, y1.re, s * g.re), fmaf(c, y1.im, s * g.im)};
-        const cf r2{fmaf(-s, y1.re, c * g.re), fmaf(-s, y1.im, c * g.im)};
-        // column j = initial flavour j; rows 0..2 = final flavours
-        out[(size_t)(j * 3 + 0) * plane] = fmaf(r0.re, r0.re, r0.im * r0.im);
-        out[(size_t)(j * 3 + 1) * plane] = fmaf(r1.re, r1.re, r1.im * r1.im);
-        out[(size_t)(j * 3 + 2) * plane] = fmaf(r2.re, r2.re, r2.im * r2.im);
-    }
-}
-
-struct WParams {
-    float c, s, er, ei;
-};
-
+// Mixed atmospheric bins (the physics of calculate_atmos rearranged for FP32: see
+// cp3_mixed.cuh).
 __global__ void __launch_bounds__(kBlock)
     atmos_mixed_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
                        const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
@@ -300,53 +153,8 @@ __global__ void __launch_bounds__(kBlock)
     __syncthreads();
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    const size_t cls_stride = (size_t)kMixFields * ne_pad;
-    const float* tab = table + (size_t)ie * kMixFields;
-    const int M = nseg - 1;
-
-    cs6 S0;
-    segment_matrix_mixed(tab + s_cls[0] * cls_stride, s_len[0], S0);
-    cg9 A2;
-    if (M == 0) {
-        sym_to_gen(S0, A2);
-    } else {
-        cs6 S;
-        cg9 B;
-        if (M == 1) {
-            segment_matrix_mixed(tab + s_cls[1] * cls_stride, s_len[1], S);
-            sym_to_gen(S, B);  // B = S_1, Q = S_1
-            mul_gs(B, S0, A2);
-        } else {
-            segment_matrix_mixed(tab + s_cls[1] * cls_stride, s_len[1], S);
-            sym_to_gen(S, B);
-            for (int l = 2; l < M; l++) {
-                segment_matrix_mixed(tab + s_cls[l] * cls_stride, s_len[l], S);
-                mul_sg(S, B, B);
-            }
-            segment_matrix_mixed(tab + s_cls[M] * cls_stride, s_len[M], S);
-            cg9 X;
-            mul_sg(S, B, X);  // X = S_M B
-            cs6 Q;            // Q = B^T X (symmetric)
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = i; j < 3; j++) {
-                    cf acc = cmulf(B.a[0][i], X.a[0][j]);
-#pragma unroll
-                    for (int k = 1; k < 3; k++) {
-                        const cf b = B.a[k][i], x = X.a[k][j];
-                        acc.re = fmaf(b.re, x.re, fmaf(-b.im, x.im, acc.re));
-                        acc.im = fmaf(b.re, x.im, fmaf(b.im, x.re, acc.im));
-                    }
-                    Q.a[sidx(i, j)] = acc;
-                }
-            sym_to_gen(Q, B);
-            mul_gs(B, S0, A2);
-        }
-    }
-    newton_schulz(A2);
-    const size_t plane = (size_t)nc * ne;
-    store_probabilities(A2, w.c, w.s, w.er, w.ei, out + (size_t)ic * ne + ie, plane);
+    atmos_bin_mixed(table + (size_t)ie * kMixFields, (size_t)kMixFields * ne_pad, s_len, s_cls,
+                    nseg - 1, w, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
 
 // Beam, mixed: per-bin eigen-decomposition with double-float refinement
@@ -357,23 +165,7 @@ __global__ void __launch_bounds__(kBlock)
                       float* __restrict__ out) {
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    float P[2][6], om[2][2], z[2][2];
-    rotated_eigen_mixed(&p, energies[ie], rho_e, P, om);
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        float lo;
-        const float r = reduced_phase(om[k][0], om[k][1], L.x, L.y, lo);
-        unit_phase_minus_one(r, lo, z[k][0], z[k][1]);
-    }
-    cs6 S;
-    layer_matrix(z, P[0], P[1], S);
-    cg9 A2;
-    sym_to_gen(S, A2);
-    store_probabilities(A2, w.c, w.s, w.er, w.ei, out + ie, (size_t)ne);
-}
-
-WParams wparams(const OscParams& p) {
-    return WParams{(float)p.w[0], (float)p.w[1], (float)p.w[2], (float)p.w[3]};
+    beam_bin_mixed(&p, w, energies[ie], rho_e, &L, 1, out + ie, (size_t)ne, 0);
 }
 
 }  // namespace

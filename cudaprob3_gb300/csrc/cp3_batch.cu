@@ -1,0 +1,724 @@
+// cp3_batch.cu -- many independent propagation problems in one persistent launch.
+//
+// A batch holds atmospheric problems (one Earth model and production height for the batch,
+// each problem with its own cosine and energy grid) and beam problems (own energies, density
+// and one or more baselines), each with its own oscillation parameters and neutrino type.
+// One run is one launch of a persistent kernel, captured once in a CUDA graph:
+//
+//   * the grid is (SMs x resident blocks); every block pulls tiles from one atomic counter;
+//   * tiles [0, A) build the per-(class, energy) eigen tables of the atmospheric problems,
+//     tiles [A, A+B) compute bins: atmospheric tiles are R cosine rows x 128 energies, beam
+//     tiles are 128 R x beam_chunk energies with every baseline of the problem;
+//   * an atmospheric bin tile first waits until its own problem's table tiles are done.
+//     Those tiles were handed out before it by the same counter, so the blocks holding them
+//     are running and the wait ends; it is bounded all the same (status flag on time-out);
+//   * everything a run needs -- descriptors, tile prefix sums, parameters -- is in device
+//     memory, so the captured graph replays unchanged while parameters change between runs.
+//
+// The tile shape (R, blocks per SM, beam_chunk) does not change any bin's arithmetic:
+// results are bit-identical across shapes, which lets an autotuner pick it by timing alone.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "../../include/cudaprob3_gb300.h"
+#include "cp3_host.hpp"
+#include "cp3_kernels.hpp"
+#include "cp3_mixed.cuh"
+
+namespace cp3 {
+namespace {
+
+constexpr int kTileE = 128;             // energies per atmospheric tile row
+constexpr long long kSpinLimit = 20000000;  // ~seconds with the nanosleep back-off
+
+struct Problem {
+    int kind;          // 0 atmospheric, 1 beam
+    int ne, ne_pad;
+    int nrows;         // atmospheric: cosines; beam: baselines
+    int ncls;          // atmospheric: density classes
+    int param;         // index into the parameter arena
+    long long e_off;   // energies arena (doubles)
+    long long row_off; // atmospheric: first of nrows + 1 row offsets; beam: first baseline
+    long long cls_off; // atmospheric: first class density
+    long long tab_off; // atmospheric: float offset of the table [ncls][ne_pad][16]
+    long long out_off; // float offset of the result
+    double rho_e;      // beam: electron density (rho * 0.5)
+};
+
+struct Header {
+    int nprob;
+    int beam_chunk;
+    long long total_a, total_b;
+};
+
+struct Args {
+    const Header* hdr;
+    const Problem* probs;
+    const long long* a_start;  // nprob + 1 (table tiles)
+    const long long* b_start;  // nprob + 1 (bin tiles)
+    const OscParams* params;
+    const double* energies;
+    const int* row_off;
+    const float2* seg_len;
+    const int* seg_cls;
+    const double* cls_rho;
+    const float2* baselines;
+    float* tables;
+    float* out;
+    int* done_a;
+    unsigned long long* counter;
+    int* status;
+};
+
+// Largest p with prefix[p] <= t (prefix[n] = total > t); skips empty ranges.
+__device__ __forceinline__ int find_problem(const long long* __restrict__ prefix, int n, long long t) {
+    int lo = 0, hi = n;  // invariant: prefix[lo] <= t < prefix[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(prefix + mid) <= t)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+template <int R>
+// 64 registers per thread (the budget of the standalone per-bin kernel): 8 blocks of 128
+// or 4 of 256 threads per SM.
+__global__ void __launch_bounds__(128 * R, 8 / R) batch_kernel(const Args a) {
+    constexpr int T = 128 * R;
+    __shared__ long long s_tile;
+    __shared__ float2 s_len[R][kMaxSegments];
+    __shared__ int s_cls[R][kMaxSegments];
+    const int r = threadIdx.x >> 7;
+    const int lane = threadIdx.x & 127;
+    const Header hdr = *a.hdr;
+    const long long total = hdr.total_a + hdr.total_b;
+    for (;;) {
+        __syncthreads();  // previous tile finished with the shared staging
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(a.counter, 1ULL);
+        __syncthreads();
+        const long long t = s_tile;
+        if (t >= total) return;
+        if (t < hdr.total_a) {
+            // ---- eigen-table tile: R classes x 128 energies of one atmospheric problem ----
+            const int p = find_problem(a.a_start, hdr.nprob, t);
+            const Problem P = a.probs[p];
+            const long long local = t - a.a_start[p];
+            const int nchunk = (P.ne + kTileE - 1) / kTileE;
+            const int c = (int)(local / nchunk) * R + r;
+            const int e = (int)(local % nchunk) * kTileE + lane;
+            if (c < P.ncls && e < P.ne) {
+                float Pp[2][6], om[2][2];
+                rotated_eigen_mixed(a.params + P.param, a.energies[P.e_off + e],
+                                    a.cls_rho[P.cls_off + c], Pp, om);
+                float4* d = reinterpret_cast<float4*>(a.tables + P.tab_off +
+                                                      ((size_t)c * P.ne_pad + e) * kMixFields);
+                d[0] = make_float4(Pp[0][0], Pp[0][1], Pp[0][2], Pp[0][3]);
+                d[1] = make_float4(Pp[0][4], Pp[0][5], Pp[1][0], Pp[1][1]);
+                d[2] = make_float4(Pp[1][2], Pp[1][3], Pp[1][4], Pp[1][5]);
+                d[3] = make_float4(om[0][0], om[0][1], om[1][0], om[1][1]);
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) atomicAdd(a.done_a + p, 1);
+            continue;
+        }
+        // ---- bin tile --------------------------------------------------------------------
+        const long long tb = t - hdr.total_a;
+        const int p = find_problem(a.b_start, hdr.nprob, tb);
+        const Problem P = a.probs[p];
+        const long long local = tb - a.b_start[p];
+        const OscParams* prm = a.params + P.param;
+        const WParams w{(float)prm->w[0], (float)prm->w[1], (float)prm->w[2], (float)prm->w[3]};
+        if (P.kind == 0) {
+            if (threadIdx.x == 0) {
+                const int need = (int)(a.a_start[p + 1] - a.a_start[p]);
+                const volatile int* done = a.done_a + p;
+                long long it = 0;
+                while (*done < need) {
+                    __nanosleep(256);
+                    if (++it > kSpinLimit) {
+                        atomicExch(a.status, 1);  // tables never completed: report, do not hang
+                        break;
+                    }
+                }
+                __threadfence();
+            }
+            const int nchunk = (P.ne + kTileE - 1) / kTileE;
+            const int ic = (int)(local / nchunk) * R + r;
+            const int e = (int)(local % nchunk) * kTileE + lane;
+            int nseg = 0;
+            if (ic < P.nrows) {
+                const int s0 = a.row_off[P.row_off + ic];
+                nseg = a.row_off[P.row_off + ic + 1] - s0;
+                for (int i = lane; i < nseg; i += 128) {
+                    s_len[r][i] = a.seg_len[s0 + i];
+                    s_cls[r][i] = a.seg_cls[s0 + i];
+                }
+            }
+            __syncthreads();
+            if (ic < P.nrows && e < P.ne)
+                atmos_bin_mixed<true>(a.tables + P.tab_off + (size_t)e * kMixFields,
+                                      (size_t)kMixFields * P.ne_pad, s_len[r], s_cls[r], nseg - 1,
+                                      w, a.out + P.out_off + (size_t)ic * P.ne + e,
+                                      (size_t)P.nrows * P.ne);
+        } else {
+            const long long e0 = local * (long long)T * hdr.beam_chunk;
+            for (int k = 0; k < hdr.beam_chunk; k++) {
+                const long long e = e0 + (long long)k * T + threadIdx.x;
+                if (e < P.ne)
+                    beam_bin_mixed(prm, w, a.energies[P.e_off + e], P.rho_e, a.baselines + P.row_off,
+                                   P.nrows, a.out + P.out_off + e, (size_t)P.ne, (size_t)9 * P.ne);
+            }
+        }
+    }
+}
+
+template <class T>
+struct Buf {
+    T* ptr = nullptr;
+    size_t n = 0;
+    ~Buf() {
+        if (ptr) cudaFree(ptr);
+    }
+    cudaError_t alloc(size_t count) {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        n = 0;
+        const cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
+        if (v.empty()) return cudaSuccess;
+        return cudaMemcpyAsync(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+}  // namespace cp3
+
+using namespace cp3;
+
+struct cp3_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int sms = 0;
+
+    EarthModel model;
+    bool model_set = false;
+    double height_cm = 0.0;
+
+    struct HostProblem {
+        int kind = 0;
+        std::vector<double> cz, en, L;
+        double rho = 0.0;
+        MixingInput mix;
+        int type = 0;
+        bool params_set = false;
+    };
+    std::vector<HostProblem> hp;
+    bool committed = false;
+
+    std::vector<Problem> probs;
+    std::vector<long long> out_off;
+    size_t out_floats = 0;
+    long long total_bins = 0;
+
+    Buf<Problem> d_probs;
+    Buf<long long> d_astart, d_bstart;
+    Buf<Header> d_hdr;
+    Buf<OscParams> d_params;
+    Buf<double> d_energies, d_cls_rho;
+    Buf<int> d_row_off, d_seg_cls, d_done, d_status;
+    Buf<float2> d_seg_len, d_baselines;
+    Buf<float> d_tables, d_out;
+    Buf<unsigned long long> d_counter;
+    OscParams* h_params = nullptr;  // pinned staging
+    bool params_dirty = true;
+
+    int R = 1, blocks_per_sm = 0, beam_chunk = 4;
+    long long total_a = 0, total_b = 0;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev_params = nullptr, ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+
+    ~cp3_batch() {
+        cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (cudaEvent_t e : {ev_params, ev0, ev1})
+            if (e) cudaEventDestroy(e);
+        if (h_params) cudaFreeHost(h_params);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+thread_local std::string g_batch_create_error;
+
+int bfail(cp3_batch* b, int code, const std::string& msg) {
+    if (b)
+        b->err = msg;
+    else
+        g_batch_create_error = msg;
+    return code;
+}
+
+int bcuda(cp3_batch* b, cudaError_t e, const char* where) {
+    cudaGetLastError();
+    return bfail(b, e == cudaErrorMemoryAllocation ? CP3_ERR_OOM : CP3_ERR_CUDA,
+                 std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define B_CUDA(b, call, where)                                  \
+    do {                                                        \
+        const cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return bcuda(b, e_, where);      \
+    } while (0)
+
+int occupancy(int R, int* blocks) {
+    cudaError_t e = R == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batch_kernel<1>, 128, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batch_kernel<2>, 256, 0);
+    return e == cudaSuccess ? 0 : 1;
+}
+
+// Tile counts for the current shape, the device header and the graph.
+int configure(cp3_batch* b) {
+    const int n = (int)b->probs.size();
+    std::vector<long long> a(n + 1, 0), bb(n + 1, 0);
+    for (int p = 0; p < n; p++) {
+        const Problem& P = b->probs[p];
+        const long long nchunk = (P.ne + kTileE - 1) / kTileE;
+        if (P.kind == 0) {
+            a[p + 1] = a[p] + nchunk * ((P.ncls + b->R - 1) / b->R);
+            bb[p + 1] = bb[p] + nchunk * ((P.nrows + b->R - 1) / b->R);
+        } else {
+            a[p + 1] = a[p];
+            const long long per = 128LL * b->R * b->beam_chunk;
+            bb[p + 1] = bb[p] + (P.ne + per - 1) / per;
+        }
+    }
+    b->total_a = a[n];
+    b->total_b = bb[n];
+    Header h{n, b->beam_chunk, a[n], bb[n]};
+    B_CUDA(b, cudaMemcpyAsync(b->d_astart.ptr, a.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
+    B_CUDA(b, cudaMemcpyAsync(b->d_bstart.ptr, bb.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
+    B_CUDA(b, cudaMemcpyAsync(b->d_hdr.ptr, &h, sizeof(Header), cudaMemcpyHostToDevice, b->stream), "upload header");
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "configure");
+
+    int occ = 0;
+    if (occupancy(b->R, &occ) || occ < 1) return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
+    const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, occ) : occ;
+    const int grid = std::max(1, b->sms * bps);
+    Args args{b->d_hdr.ptr, b->d_probs.ptr, b->d_astart.ptr, b->d_bstart.ptr, b->d_params.ptr,
+              b->d_energies.ptr, b->d_row_off.ptr, b->d_seg_len.ptr, b->d_seg_cls.ptr,
+              b->d_cls_rho.ptr, b->d_baselines.ptr, b->d_tables.ptr, b->d_out.ptr,
+              b->d_done.ptr, b->d_counter.ptr, b->d_status.ptr};
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaStream_t cs;
+    B_CUDA(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter.ptr, 0, sizeof(unsigned long long), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_done.ptr, 0, sizeof(int) * std::max(n, 1), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_status.ptr, 0, sizeof(int), cs);
+    if (e == cudaSuccess) {
+        if (b->R == 1)
+            batch_kernel<1><<<grid, 128, 0, cs>>>(args);
+        else
+            batch_kernel<2><<<grid, 256, 0, cs>>>(args);
+        e = cudaGetLastError();
+    }
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (e2 == cudaSuccess) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return bcuda(b, e, "graph capture");
+    return CP3_OK;
+}
+
+int commit(cp3_batch* b) {
+    const int n = (int)b->hp.size();
+    if (n == 0) return bfail(b, CP3_ERR_NOT_SET, "the batch has no problems");
+    std::vector<double> energies, cls_rho;
+    std::vector<int> row_off, seg_cls;
+    std::vector<float2> seg_len, baselines;
+    b->probs.assign(n, Problem{});
+    b->out_off.assign(n, 0);
+    size_t tab = 0, out = 0;
+    b->total_bins = 0;
+    auto split = [](double x) {
+        const float h = (float)x;
+        return make_float2(h, (float)(x - (double)h));
+    };
+    for (int p = 0; p < n; p++) {
+        const cp3_batch::HostProblem& H = b->hp[p];
+        if (!H.params_set) return bfail(b, CP3_ERR_NOT_SET, "problem " + std::to_string(p) + " has no parameters");
+        Problem& P = b->probs[p];
+        P.kind = H.kind;
+        P.ne = (int)H.en.size();
+        P.ne_pad = pad_energies(P.ne);
+        P.param = p;
+        P.e_off = (long long)energies.size();
+        energies.insert(energies.end(), H.en.begin(), H.en.end());
+        if (H.kind == 0) {
+            if (!b->model_set) return bfail(b, CP3_ERR_NOT_SET, "atmospheric problems need cp3_batch_set_earth first");
+            TrajectoryTable t;
+            std::string msg;
+            int rc = build_trajectories(b->model, H.cz.data(), (int)H.cz.size(), b->height_cm, &t, &msg);
+            if (rc) return bfail(b, rc, msg);
+            P.nrows = (int)H.cz.size();
+            P.ncls = 1 + *std::max_element(t.maxlayers.begin(), t.maxlayers.end());
+            P.row_off = (long long)row_off.size();
+            const int base = (int)seg_len.size();
+            for (int v : t.offset) row_off.push_back(base + v);
+            for (size_t i = 0; i < t.len_km.size(); i++) {
+                seg_len.push_back(split(t.len_km[i]));
+                seg_cls.push_back(t.cls[i]);
+            }
+            P.cls_off = (long long)cls_rho.size();
+            cls_rho.push_back(0.0);
+            for (int c = 1; c < P.ncls; c++) cls_rho.push_back(b->model.rho[c - 1] * b->model.ye[c - 1]);
+            P.tab_off = (long long)tab;
+            tab += align_up((size_t)P.ncls * P.ne_pad * kMixFields, 64);
+            P.out_off = (long long)out;
+            out += align_up((size_t)9 * P.nrows * P.ne, 32);
+            b->total_bins += (long long)P.nrows * P.ne;
+        } else {
+            P.nrows = (int)H.L.size();
+            P.row_off = (long long)baselines.size();
+            for (double L : H.L) baselines.push_back(split(L));
+            P.rho_e = H.rho * kDensityConvert;
+            P.out_off = (long long)out;
+            out += align_up((size_t)9 * P.nrows * P.ne, 32);
+            b->total_bins += (long long)P.nrows * P.ne;
+        }
+        b->out_off[p] = P.out_off;
+    }
+    b->out_floats = out;
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    B_CUDA(b, b->d_probs.alloc(n), "allocate");
+    B_CUDA(b, b->d_astart.alloc(n + 1), "allocate");
+    B_CUDA(b, b->d_bstart.alloc(n + 1), "allocate");
+    B_CUDA(b, b->d_hdr.alloc(1), "allocate");
+    B_CUDA(b, b->d_params.alloc(n), "allocate");
+    B_CUDA(b, b->d_energies.alloc(energies.size()), "allocate");
+    B_CUDA(b, b->d_cls_rho.alloc(cls_rho.size()), "allocate");
+    B_CUDA(b, b->d_row_off.alloc(row_off.size()), "allocate");
+    B_CUDA(b, b->d_seg_cls.alloc(seg_cls.size()), "allocate");
+    B_CUDA(b, b->d_seg_len.alloc(seg_len.size()), "allocate");
+    B_CUDA(b, b->d_baselines.alloc(baselines.size()), "allocate");
+    B_CUDA(b, b->d_tables.alloc(tab), "allocate eigen tables");
+    B_CUDA(b, b->d_out.alloc(out), "allocate results");
+    B_CUDA(b, b->d_done.alloc(n), "allocate");
+    B_CUDA(b, b->d_status.alloc(1), "allocate");
+    B_CUDA(b, b->d_counter.alloc(1), "allocate");
+    B_CUDA(b, b->d_probs.upload(b->probs, b->stream), "upload");
+    B_CUDA(b, b->d_energies.upload(energies, b->stream), "upload");
+    B_CUDA(b, b->d_cls_rho.upload(cls_rho, b->stream), "upload");
+    B_CUDA(b, b->d_row_off.upload(row_off, b->stream), "upload");
+    B_CUDA(b, b->d_seg_cls.upload(seg_cls, b->stream), "upload");
+    B_CUDA(b, b->d_seg_len.upload(seg_len, b->stream), "upload");
+    B_CUDA(b, b->d_baselines.upload(baselines, b->stream), "upload");
+    if (b->h_params) cudaFreeHost(b->h_params);
+    b->h_params = nullptr;
+    B_CUDA(b, cudaMallocHost(&b->h_params, sizeof(OscParams) * n), "pinned parameters");
+    for (int p = 0; p < n; p++) build_osc_params(b->hp[p].mix, b->hp[p].type, b->h_params + p);
+    b->params_dirty = true;
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "commit");
+    b->committed = true;
+    return configure(b);
+}
+
+int launch(cp3_batch* b, cudaStream_t s) {
+    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    if (b->params_dirty) {
+        B_CUDA(b, cudaMemcpyAsync(b->d_params.ptr, b->h_params, sizeof(OscParams) * b->probs.size(),
+                                  cudaMemcpyHostToDevice, s), "upload parameters");
+        B_CUDA(b, cudaEventRecord(b->ev_params, s), "event");
+        b->params_dirty = false;
+    }
+    B_CUDA(b, cudaEventRecord(b->ev0, s), "event");
+    B_CUDA(b, cudaGraphLaunch(b->graph, s), "graph launch");
+    B_CUDA(b, cudaEventRecord(b->ev1, s), "event");
+    b->timed = true;
+    return CP3_OK;
+}
+
+std::string tune_cache_path() {
+    if (const char* p = std::getenv("CP3_TUNE_CACHE")) return p;
+    const char* home = std::getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/cp3gb300_tune.txt";
+}
+
+std::string tune_key(cp3_batch* b) {
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, b->device);
+    long long na = 0, nb = 0;
+    for (const Problem& P : b->probs) (P.kind == 0 ? na : nb)++;
+    // problem mix and size, bucketed by powers of two
+    const int lg = (int)std::log2((double)std::max<long long>(1, b->total_bins));
+    std::string name(prop.name);
+    std::replace(name.begin(), name.end(), ' ', '_');
+    return name + ":a" + std::to_string(na > 0) + "b" + std::to_string(nb > 0) + ":bins2^" + std::to_string(lg);
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp3_batch_create(int device, cp3_batch** out) {
+    if (!out) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return bfail(nullptr, CP3_ERR_CUDA, "No GPU found");
+    }
+    if (device < 0 || device >= ndev)
+        return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "The requested GPU Id " + std::to_string(device) + " is not available.");
+    cp3_batch* b = new cp3_batch();
+    b->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    for (cudaEvent_t* ev : {&b->ev_params, &b->ev0, &b->ev1})
+        if (e == cudaSuccess) e = cudaEventCreate(ev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        const std::string msg = std::string("batch creation failed: ") + cudaGetErrorString(e);
+        delete b;
+        return bfail(nullptr, CP3_ERR_CUDA, msg);
+    }
+    *out = b;
+    return CP3_OK;
+}
+
+int cp3_batch_destroy(cp3_batch* b) {
+    delete b;
+    return CP3_OK;
+}
+
+const char* cp3_batch_last_error(const cp3_batch* b) {
+    return b ? b->err.c_str() : g_batch_create_error.c_str();
+}
+
+int cp3_batch_set_earth(cp3_batch* b, const double* radii, const double* rho, const double* ye,
+                        int n, double production_height_km) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (b->committed) return bfail(b, CP3_ERR_UNSUPPORTED, "the batch is committed");
+    std::string msg;
+    int rc = make_earth_model(radii, rho, nullptr, nullptr, ye, n, false, &b->model, &msg);
+    if (rc) return bfail(b, rc, msg);
+    b->height_cm = production_height_km * 100000.0;
+    b->model_set = true;
+    return CP3_OK;
+}
+
+int cp3_batch_add_atmos(cp3_batch* b, const double* cosines, int nc, const double* energies,
+                        int ne, int* id) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (b->committed) return bfail(b, CP3_ERR_UNSUPPORTED, "the batch is committed");
+    if (nc < 1 || ne < 1 || !cosines || !energies) return bfail(b, CP3_ERR_BAD_SIZE, "empty grid");
+    if (!b->model_set) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_set_earth before atmospheric problems");
+    for (int i = 0; i < nc; i++)
+        if (count_shells(b->model, cosines[i]) > kMaxShells)
+            return bfail(b, CP3_ERR_LAYER_LIMIT, "setMaxlayers : invalid number of maxLayer");
+    cp3_batch::HostProblem H;
+    H.kind = 0;
+    H.cz.assign(cosines, cosines + nc);
+    H.en.assign(energies, energies + ne);
+    b->hp.push_back(std::move(H));
+    if (id) *id = (int)b->hp.size() - 1;
+    return CP3_OK;
+}
+
+int cp3_batch_add_beam(cp3_batch* b, const double* energies, int ne, double rho,
+                       const double* path_km, int n_baselines, int* id) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (b->committed) return bfail(b, CP3_ERR_UNSUPPORTED, "the batch is committed");
+    if (ne < 1 || !energies || n_baselines < 1 || !path_km) return bfail(b, CP3_ERR_BAD_SIZE, "empty grid");
+    cp3_batch::HostProblem H;
+    H.kind = 1;
+    H.en.assign(energies, energies + ne);
+    H.L.assign(path_km, path_km + n_baselines);
+    H.rho = rho;
+    b->hp.push_back(std::move(H));
+    if (id) *id = (int)b->hp.size() - 1;
+    return CP3_OK;
+}
+
+int cp3_batch_set_params(cp3_batch* b, int id, double t12, double t13, double t23, double dcp,
+                         int knutype, double dm12sq, double dm23sq, int neutrino_type) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (id < 0 || id >= (int)b->hp.size()) return bfail(b, CP3_ERR_INDEX, "no such problem");
+    if (neutrino_type != CP3_NEUTRINO && neutrino_type != CP3_ANTINEUTRINO)
+        return bfail(b, CP3_ERR_BAD_ARGUMENT, "neutrino type must be Neutrino or Antineutrino");
+    cp3_batch::HostProblem& H = b->hp[id];
+    H.mix.theta12 = t12;
+    H.mix.theta13 = t13;
+    H.mix.theta23 = t23;
+    H.mix.dcp = dcp;
+    H.mix.knutype = knutype;
+    H.mix.dm12sq = dm12sq;
+    H.mix.dm23sq = dm23sq;
+    H.type = neutrino_type;
+    H.params_set = true;
+    if (b->committed) {
+        // the previous upload from the staging area must have left before it is rewritten
+        B_CUDA(b, cudaEventSynchronize(b->ev_params), "event");
+        build_osc_params(H.mix, H.type, b->h_params + id);
+        b->params_dirty = true;
+    }
+    return CP3_OK;
+}
+
+int cp3_batch_commit(cp3_batch* b) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (b->committed) return CP3_OK;
+    return commit(b);
+}
+
+int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int beam_chunk) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if ((rows_per_tile != 1 && rows_per_tile != 2) || blocks_per_sm < 0 || beam_chunk < 1 || beam_chunk > 64)
+        return bfail(b, CP3_ERR_BAD_ARGUMENT, "shape: rows_per_tile 1|2, blocks_per_sm >= 0, beam_chunk 1..64");
+    b->R = rows_per_tile;
+    b->blocks_per_sm = blocks_per_sm;
+    b->beam_chunk = beam_chunk;
+    if (!b->committed) return CP3_OK;
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+    return configure(b);
+}
+
+int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_sm, int* beam_chunk) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (rows_per_tile) *rows_per_tile = b->R;
+    if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
+    if (beam_chunk) *beam_chunk = b->beam_chunk;
+    return CP3_OK;
+}
+
+int cp3_batch_run(cp3_batch* b, void* stream) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    return launch(b, stream ? (cudaStream_t)stream : b->stream);
+}
+
+int cp3_batch_synchronize(cp3_batch* b, double* ms) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (!b->timed) return CP3_OK;
+    B_CUDA(b, cudaEventSynchronize(b->ev1), "synchronize");
+    if (ms) {
+        float f = 0.f;
+        B_CUDA(b, cudaEventElapsedTime(&f, b->ev0, b->ev1), "elapsed");
+        *ms = f;
+    }
+    int st = 0;
+    B_CUDA(b, cudaMemcpy(&st, b->d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost), "status");
+    if (st) return bfail(b, CP3_ERR_CUDA, "batch kernel: eigen tables did not complete (wait limit)");
+    return CP3_OK;
+}
+
+int cp3_batch_tune(cp3_batch* b, int use_cache) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    const std::string key = tune_key(b), path = tune_cache_path();
+    if (use_cache) {
+        std::ifstream f(path);
+        std::string k;
+        int R, bps, bc;
+        while (f >> k >> R >> bps >> bc)
+            if (k == key) return cp3_batch_set_shape(b, R, bps, bc);
+    }
+    int occ1 = 0, occ2 = 0;
+    occupancy(1, &occ1);
+    occupancy(2, &occ2);
+    struct Shape {
+        int R, bps, bc;
+    };
+    std::vector<Shape> cand;
+    for (int bc : {1, 4, 16}) {
+        cand.push_back({1, 0, bc});
+        cand.push_back({2, 0, bc});
+        if (occ1 > 1) cand.push_back({1, std::max(1, occ1 / 2), bc});
+    }
+    double best = 1e30;
+    Shape pick = cand[0];
+    for (const Shape& s : cand) {
+        int rc = cp3_batch_set_shape(b, s.R, s.bps, s.bc);
+        if (rc) return rc;
+        double total = 0;
+        for (int it = 0; it < 4; it++) {
+            rc = cp3_batch_run(b, nullptr);
+            double ms = 0;
+            if (!rc) rc = cp3_batch_synchronize(b, &ms);
+            if (rc) return rc;
+            if (it > 0) total += ms;
+        }
+        if (total < best) {
+            best = total;
+            pick = s;
+        }
+    }
+    int rc = cp3_batch_set_shape(b, pick.R, pick.bps, pick.bc);
+    if (rc) return rc;
+    if (use_cache) {
+        std::ofstream f(path, std::ios::app);
+        if (f) f << key << " " << pick.R << " " << pick.bps << " " << pick.bc << "\n";
+    }
+    return CP3_OK;
+}
+
+int cp3_batch_result(cp3_batch* b, int id, const float** ptr, size_t* count) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    if (id < 0 || id >= (int)b->probs.size()) return bfail(b, CP3_ERR_INDEX, "no such problem");
+    const Problem& P = b->probs[id];
+    if (ptr) *ptr = b->d_out.ptr + P.out_off;
+    if (count) *count = (size_t)9 * P.nrows * P.ne;
+    return CP3_OK;
+}
+
+int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    const float* src = nullptr;
+    size_t n = 0;
+    if (int rc = cp3_batch_result(b, id, &src, &n)) return rc;
+    if (!dst) return bfail(b, CP3_ERR_BAD_ARGUMENT, "null destination");
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    B_CUDA(b, cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToHost,
+                              stream ? (cudaStream_t)stream : b->stream), "copy result");
+    return CP3_OK;
+}
+
+int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins, size_t* result_bytes,
+                   long long* tiles) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (n_problems) *n_problems = (int)b->hp.size();
+    if (total_bins) *total_bins = b->total_bins;
+    if (result_bytes) *result_bytes = b->out_floats * sizeof(float);
+    if (tiles) *tiles = b->total_a + b->total_b;
+    return CP3_OK;
+}
+
+}  // extern "C"

@@ -199,6 +199,57 @@ int cp3_set_profiling(cp3_propagator* h, int enable);
  * per-bin kernel, milliseconds.  eigen_ms is 0 where no table kernel runs (beam). */
 int cp3_kernel_times(cp3_propagator* h, double* eigen_ms, double* bins_ms);
 
+/* ---- batches: many problems, one persistent launch --------------------------------------- */
+
+/* No reference counterpart (the reference propagates one grid per call; SURVEY C2-C4 ask
+ * for many parameter sets with uneven grids in one launch).  A batch holds atmospheric
+ * problems (one Earth model and production height per batch, own cosine/energy grid each)
+ * and beam problems (own energies, density and baselines), each with its own oscillation
+ * parameters and neutrino type, computed in MIXED precision by one persistent kernel
+ * replayed from a CUDA graph.  Results stay on the device:
+ *   atmospheric problem  [9][n_cosines][n_energies] floats
+ *   beam problem         [n_baselines][9][n_energies] floats */
+typedef struct cp3_batch cp3_batch;
+
+int cp3_batch_create(int device, cp3_batch** out);
+int cp3_batch_destroy(cp3_batch* b);
+const char* cp3_batch_last_error(const cp3_batch* b);
+
+/* Earth model (as cp3_set_layers) and production height shared by the atmospheric problems. */
+int cp3_batch_set_earth(cp3_batch* b, const double* radii, const double* rho, const double* ye,
+                        int n, double production_height_km);
+int cp3_batch_add_atmos(cp3_batch* b, const double* cosines, int n_cosines,
+                        const double* energies, int n_energies, int* id);
+/* rho in g/cm^3 (Ye = 0.5); all baselines of one problem share its eigen-decompositions. */
+int cp3_batch_add_beam(cp3_batch* b, const double* energies, int n_energies, double rho,
+                       const double* path_km, int n_baselines, int* id);
+/* setMNSMatrix + setNeutrinoMasses + the neutrino type of one problem; may change between
+ * runs after the commit (the next run uploads them). */
+int cp3_batch_set_params(cp3_batch* b, int id, double theta12, double theta13, double theta23,
+                         double dcp, int knutype, double dm12sq, double dm23sq,
+                         int neutrino_type);
+/* Freezes the problem list: trajectories, device arenas, the CUDA graph. */
+int cp3_batch_commit(cp3_batch* b);
+/* Tile shape of the persistent kernel (results do not depend on it): cosine rows per tile
+ * (1 or 2), resident blocks per SM (0 = as many as fit), beam energy chunks per tile. */
+int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int beam_chunk);
+int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_sm,
+                        int* beam_chunk);
+/* Autotuner: times every candidate shape on this batch and keeps the fastest; use_cache != 0
+ * reads and appends the choice to $CP3_TUNE_CACHE (default ~/.cache/cp3gb300_tune.txt),
+ * keyed by GPU and batch size. */
+int cp3_batch_tune(cp3_batch* b, int use_cache);
+/* One run over every problem on `stream` (NULL = the batch's own stream). */
+int cp3_batch_run(cp3_batch* b, void* stream);
+/* Waits for the last run; *ms = its device time. */
+int cp3_batch_synchronize(cp3_batch* b, double* ms);
+/* Device pointer and float count of one problem's result. */
+int cp3_batch_result(cp3_batch* b, int id, const float** ptr, size_t* count);
+/* Asynchronous copy of one problem's result to dst (count floats) on `stream`. */
+int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream);
+int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins,
+                   size_t* result_bytes, long long* tiles);
+
 /* ---- atmospheric propagation without allocation ------------------------------------------ */
 
 /* Size of the device scratch behind cp3_atmos_mixed_noalloc (reserved on every GPU that

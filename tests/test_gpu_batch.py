@@ -1,0 +1,142 @@
+"""Batches (one persistent launch over many problems) against single propagators, the
+oracle, and themselves under every tile shape."""
+import numpy as np
+import pytest
+
+from cudaprob3_gb300 import AtmosCudaPropagatorSingle, BeamCudaPropagatorSingle, earth
+from cudaprob3_gb300.batch import Batch
+from tests.gpu_helpers import run_atmos
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 1e-5
+
+
+def single_atmos(m, anti, cz, en, model, h):
+    p = AtmosCudaPropagatorSingle(0, len(cz), len(en), precision="mixed")
+    p.setEnergyList(en)
+    p.setCosineList(cz)
+    p.setMNSMatrix(m.theta12, m.theta13, m.theta23, m.dcp, -1 if anti else 1)
+    p.setNeutrinoMasses(m.dm12sq, m.dm23sq)
+    p.setDensity(*model)
+    p.setProductionHeight(h)
+    p.calculateProbabilities(1 if anti else 0)
+    return p.result()
+
+
+def single_beam(m, anti, en, rho, L):
+    b = BeamCudaPropagatorSingle(0, len(en), 1, precision="mixed")
+    b.setEnergyList(en)
+    b.setMNSMatrix(m.theta12, m.theta13, m.theta23, m.dcp, -1 if anti else 1)
+    b.setNeutrinoMasses(m.dm12sq, m.dm23sq)
+    b.setDensity(rho)
+    b.setPathLength(L)
+    b.calculateProbabilities(1 if anti else 0)
+    return b.result()
+
+
+def build_batch(sets, rng):
+    b = Batch(0)
+    model = earth.PREM_12LAYER
+    b.set_earth(*model, 22.0)
+    probs = []
+    for i, m in enumerate(sets):
+        nc, ne = int(rng.integers(20, 150)), int(rng.integers(30, 300))
+        cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
+        for anti in (False, True):
+            pid = b.add_atmos(cz, en)
+            b.set_params(pid, m, anti)
+            probs.append(("atmos", pid, m, anti, cz, en))
+    for i, m in enumerate(sets[:3]):
+        en = earth.lin_energy_grid(int(rng.integers(1000, 5000)))
+        for anti in (False, True):
+            pid = b.add_beam(en, 2.6, [295.0, 1300.0])
+            b.set_params(pid, m, anti)
+            probs.append(("beam", pid, m, anti, en, None))
+    b.commit()
+    return b, probs
+
+
+def test_batch_matches_single_propagators_and_oracle(oracle):
+    from oracle.oracle import Mixing as OMix
+    rng = np.random.default_rng(3)
+    sets = earth.gaussian_sets(5, seed=12)
+    b, probs = build_batch(sets, rng)
+    b.run()
+    b.synchronize()
+    for kind, pid, m, anti, x, en in probs:
+        got = b.result(pid)
+        om = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, -1 if anti else 1)
+        if kind == "atmos":
+            cz = x
+            want = single_atmos(m, anti, cz, en, earth.PREM_12LAYER, 22.0)
+            assert np.abs(got - want).max() <= MIXED_TOL
+            ref = oracle.atmos(om, anti, cz, en, *earth.PREM_12LAYER, 22.0)
+            assert np.abs(np.transpose(got, (1, 2, 0)) - ref).max() <= MIXED_TOL
+        else:
+            for j, L in enumerate((295.0, 1300.0)):
+                want = single_beam(m, anti, x, 2.6, L)
+                assert np.abs(got[j] - want).max() <= MIXED_TOL
+                ref = oracle.beam(om, anti, x, 2.6, L)
+                assert np.abs(got[j].T - ref).max() <= MIXED_TOL
+
+
+def test_batch_results_do_not_depend_on_tile_shape():
+    rng = np.random.default_rng(4)
+    b, probs = build_batch(earth.gaussian_sets(3, seed=13), rng)
+    ref = None
+    for shape in [(1, 0, 4), (2, 0, 1), (1, 2, 16), (2, 1, 4)]:
+        b.set_shape(*shape)
+        b.run()
+        b.synchronize()
+        res = [b.result(pid) for _, pid, *_ in probs]
+        if ref is None:
+            ref = res
+        else:
+            for a, c in zip(ref, res):
+                assert np.array_equal(a, c), shape
+
+
+def test_batch_parameter_update_between_runs():
+    rng = np.random.default_rng(5)
+    sets = earth.gaussian_sets(2, seed=14)
+    b, probs = build_batch(sets, rng)
+    b.run()
+    b.synchronize()
+    new = earth.gaussian_sets(3, seed=99)[2]
+    kind, pid, m, anti, cz, en = probs[0]
+    b.set_params(pid, new, anti)
+    b.run()
+    b.synchronize()
+    want = single_atmos(new, anti, cz, en, earth.PREM_12LAYER, 22.0)
+    assert np.abs(b.result(pid) - want).max() <= MIXED_TOL
+
+
+def test_batch_tuner_keeps_results():
+    rng = np.random.default_rng(6)
+    b, probs = build_batch(earth.gaussian_sets(2, seed=15), rng)
+    b.run()
+    b.synchronize()
+    before = [b.result(pid) for _, pid, *_ in probs]
+    b.tune(use_cache=False)
+    b.run()
+    b.synchronize()
+    for (_, pid, *_), a in zip(probs, before):
+        assert np.array_equal(b.result(pid), a)
+
+
+def test_batch_errors():
+    from cudaprob3_gb300._abi import CP3Error
+    b = Batch(0)
+    with pytest.raises(CP3Error, match="set_earth"):
+        b.add_atmos([-1.0, 0.5], [1.0, 2.0])
+    with pytest.raises(CP3Error, match="commit"):
+        b.run()
+    pid = b.add_beam([1.0, 2.0], 2.6, [810.0])
+    with pytest.raises(CP3Error, match="no parameters"):
+        b.commit()
+    b.set_params(pid, earth.NOMINAL, False)
+    b.commit()
+    with pytest.raises(CP3Error, match="committed"):
+        b.add_beam([1.0], 2.6, [810.0])
+    with pytest.raises(CP3Error, match="no such problem"):
+        b.result_ptr(7)

@@ -287,12 +287,96 @@ def set_params(p, m, knu):
     p.setNeutrinoMasses(m.dm12sq, m.dm23sq)
 
 
+def run_serve(args, rank, world):
+    """64 closed-loop chains (each waits for its result, then thinks for an
+    exponential time and submits again) over request sizes {atm 200^2, 500^2, 2000^2; beam
+    1e4, 1e5}; the think time is swept down to zero (saturation)."""
+    import threading
+    from cudaprob3_gb300 import earth
+    from cudaprob3_gb300.serve import Server
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    srv = Server(dev, pool_bytes=16 << 30, max_batch=256, max_bins_per_launch=8_000_000)
+    srv.set_earth(*earth.PREM_4LAYER, 22.0)
+    kinds = []
+    for n in (200, 500, 2000):
+        kinds.append((f"atm{n}x{n}", srv.add_atmos_grid(earth.cosine_grid(n), earth.log_energy_grid(n)), n * n))
+    for n in (10000, 100000):
+        kinds.append((f"beam{n}", srv.add_beam_grid(earth.lin_energy_grid(n), 2.6, [1300.0]), n))
+    srv.start()
+    sets = earth.gaussian_sets(512, seed=31)
+    n_chains = 64
+    # warm-up: every kind once
+    for _, g, _ in kinds:
+        rid = srv.submit(g, sets[0], False)
+        srv.wait(rid)
+        srv.release(rid)
+    levels = []
+    for think_ms in (args.serve_think or [20.0, 5.0, 1.0, 0.0]):
+        records, lock = [], threading.Lock()
+        t_end = time.perf_counter() + args.serve_seconds
+
+        def chain(cid):
+            rng = np.random.default_rng(1000 * cid + int(think_ms * 10))
+            local = []
+            while time.perf_counter() < t_end:
+                if think_ms > 0:
+                    time.sleep(rng.exponential(think_ms * 1e-3))
+                k = int(rng.integers(len(kinds)))
+                rid = srv.submit(kinds[k][1], sets[int(rng.integers(len(sets)))], bool(rng.integers(2)))
+                srv.wait(rid, 60.0)
+                local.append((k, srv.latency_ms(rid)))
+                srv.release(rid)
+            with lock:
+                records.extend(local)
+
+        st0 = srv.stats()
+        t0 = time.perf_counter()
+        th = [threading.Thread(target=chain, args=(c,)) for c in range(n_chains)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        wall = time.perf_counter() - t0
+        st1 = srv.stats()
+        lat = np.array([x[1] for x in records])
+        kk = np.array([x[0] for x in records])
+        probs = 9.0 * sum(kinds[k][2] for k in kk)
+        lv = {"think_ms": think_ms, "requests": len(records),
+              "requests_per_s": round(len(records) / wall, 1),
+              "probabilities_per_s": probs / wall,
+              "launches": st1["launches"] - st0["launches"],
+              "p50_ms": round(float(np.percentile(lat, 50)), 3),
+              "p99_ms": round(float(np.percentile(lat, 99)), 3)}
+        for k, (name, _, _) in enumerate(kinds):
+            sel = lat[kk == k]
+            if len(sel):
+                lv[name] = {"n": int(len(sel)), "p50_ms": round(float(np.percentile(sel, 50)), 3),
+                            "p99_ms": round(float(np.percentile(sel, 99)), 3)}
+        levels.append(lv)
+    sat = levels[-1]
+    srv.close()
+    return {
+        "metric": "serving: probabilities/s at saturation (64 closed-loop chains), p50/p99 latency vs load",
+        "value": sat["probabilities_per_s"], "unit": "probabilities/s", "n_gpus": world,
+        "steps": len(levels), "warmup": 1, "ms_per_step": args.serve_seconds * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded parameter sets; PREM 4-layer, h=22 km; beam rho=2.6, L=1300 km)",
+        "config": {"workload": "serve", "chains": n_chains,
+                   "request_sizes": [k[0] for k in kinds], "pool_bytes": 16 << 30,
+                   "max_bins_per_launch": 8_000_000, "scheduling": "smallest-first, 4 ms aging"},
+        "latency_p99_atm500_at_saturation_ms": sat.get("atm500x500", {}).get("p99_ms"),
+        "levels": levels,
+    }
+
+
 def run_ours(args, rank, world):
     import torch
     from cudaprob3_gb300 import earth
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
+    if args.workload == "serve":
+        return run_serve(args, rank, world)
     w = workload(args.workload)
     if w["kind"] == "batch":
         return run_batch(args, w, rank, world)
@@ -560,7 +644,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="atmos59",
-                    choices=["atmos59", "prem4", "beam", "batch_atmos", "batch_beam"])
+                    choices=["atmos59", "prem4", "beam", "batch_atmos", "batch_beam", "serve"])
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-think", type=float, nargs="*", default=None,
+                    help="mean think times (ms) of the chains, one load level each")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=2.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -24,6 +24,11 @@ EXPORTS = (
     "cp3_batch_add_atmos", "cp3_batch_add_beam", "cp3_batch_set_params", "cp3_batch_commit",
     "cp3_batch_set_shape", "cp3_batch_get_shape", "cp3_batch_tune", "cp3_batch_run",
     "cp3_batch_synchronize", "cp3_batch_result", "cp3_batch_copy_result", "cp3_batch_info",
+    "cp3_server_create", "cp3_server_destroy", "cp3_server_last_error", "cp3_server_set_earth",
+    "cp3_server_add_atmos_grid", "cp3_server_add_beam_grid", "cp3_server_start",
+    "cp3_server_submit", "cp3_server_wait", "cp3_server_result", "cp3_server_copy_result",
+    "cp3_server_release",
+    "cp3_server_stats",
 )
 
 CP3_OK = 0
@@ -81,6 +86,23 @@ _SIGS = {
     "cp3_batch_copy_result": ([_h, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
     "cp3_batch_info": ([_h, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_size_t),
                         C.POINTER(C.c_longlong)], C.c_int),
+    "cp3_server_create": ([C.c_int, C.c_size_t, C.c_int, C.c_longlong, C.POINTER(_h)], C.c_int),
+    "cp3_server_destroy": ([_h], C.c_int),
+    "cp3_server_last_error": ([_h], C.c_char_p),
+    "cp3_server_set_earth": ([_h, _dp, _dp, _dp, C.c_int, C.c_double], C.c_int),
+    "cp3_server_add_atmos_grid": ([_h, _dp, C.c_int, _dp, C.c_int, _ip], C.c_int),
+    "cp3_server_add_beam_grid": ([_h, _dp, C.c_int, C.c_double, _dp, C.c_int, _ip], C.c_int),
+    "cp3_server_start": ([_h], C.c_int),
+    "cp3_server_submit": ([_h, C.c_int] + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double,
+                                                                C.c_int, C.POINTER(C.c_ulonglong)],
+                          C.c_int),
+    "cp3_server_wait": ([_h, C.c_ulonglong, C.c_double, _ip], C.c_int),
+    "cp3_server_result": ([_h, C.c_ulonglong, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), _dp],
+                          C.c_int),
+    "cp3_server_copy_result": ([_h, C.c_ulonglong, C.c_void_p], C.c_int),
+    "cp3_server_release": ([_h, C.c_ulonglong], C.c_int),
+    "cp3_server_stats": ([_h, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                          C.POINTER(C.c_longlong)], C.c_int),
     "cp3_atmos_mixed_noalloc": ([C.c_int, C.c_void_p, C.c_int, _ip, _dp, _ip, C.c_int, _dp, C.c_int]
                                 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double, C.c_int,
                                                       C.c_void_p, C.c_void_p, C.c_char_p,

@@ -30,6 +30,7 @@ UNITS = [
     ("cp3_atmos.cu", []),
     ("cp3_noalloc.cu", []),
     ("cp3_batch.cu", []),
+    ("cp3_serve.cu", []),
 ]
 
 

@@ -1,0 +1,622 @@
+// cp3_serve.cu -- continuous-batching request loop over the persistent many-problem kernel.
+//
+// Requests (a registered grid + one parameter set + a neutrino type) are submitted from any
+// thread and return at once.  A scheduler thread admits queued requests in arrival order
+// whenever device memory and a launch slot are free, packs them into one launch of the
+// persistent kernel, and keeps going: a request that arrives while others run joins the next
+// launch, which starts on the second slot (stream) while the first is still finishing, so
+// work from consecutive launches overlaps on the device.  Grids (trajectory tables, energies,
+// class densities) are registered once and stay resident; each request's eigen table and
+// result live in a device pool until the client releases the request.  A host callback on the
+// stream stamps the completion time of every request of a launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cudaprob3_gb300.h"
+#include "cp3_batch_kernel.cuh"
+#include "cp3_host.hpp"
+
+using namespace cp3;
+using namespace cp3::batchk;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+int64_t now_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now().time_since_epoch()).count();
+}
+
+constexpr size_t kUnit = 64;  // pool granularity in floats (256 bytes)
+
+template <class T>
+struct DBuf {
+    T* ptr = nullptr;
+    ~DBuf() {
+        if (ptr) cudaFree(ptr);
+    }
+    cudaError_t alloc(size_t n) { return cudaMalloc(&ptr, std::max<size_t>(n, 1) * sizeof(T)); }
+};
+template <class T>
+struct HBuf {  // pinned
+    T* ptr = nullptr;
+    ~HBuf() {
+        if (ptr) cudaFreeHost(ptr);
+    }
+    cudaError_t alloc(size_t n) { return cudaMallocHost(&ptr, std::max<size_t>(n, 1) * sizeof(T)); }
+};
+
+struct Template {
+    int kind = 0, ne = 0, ne_pad = 0, nrows = 0, ncls = 0;
+    long long e_off = 0, row_off = 0, cls_off = 0;
+    double rho_e = 0.0;
+    size_t tab_floats = 0, out_floats = 0;
+    long long bins = 0;
+};
+
+// First-fit allocator over one device arena, in kUnit-float units.
+class Pool {
+    std::map<size_t, size_t> free_;  // offset -> length
+public:
+    void init(size_t units) {
+        free_.clear();
+        if (units) free_[0] = units;
+    }
+    bool alloc(size_t units, size_t* off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < units) continue;
+            *off = it->first;
+            const size_t rest = it->second - units, o = it->first + units;
+            free_.erase(it);
+            if (rest) free_[o] = rest;
+            return true;
+        }
+        return false;
+    }
+    void release(size_t off, size_t units) {
+        auto next = free_.lower_bound(off);
+        if (next != free_.end() && off + units == next->first) {
+            units += next->second;
+            next = free_.erase(next);
+        }
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {
+                prev->second += units;
+                return;
+            }
+        }
+        free_[off] = units;
+    }
+};
+
+enum { kQueued = 0, kRunning = 1, kDone = 2 };
+
+struct Request {
+    uint64_t id = 0;
+    int tmpl = 0;
+    OscParams params;
+    int64_t t_submit = 0, t_start = 0, t_done = 0;
+    size_t pool_off = 0, pool_units = 0;
+    std::atomic<int> state{kQueued};
+};
+
+struct Slot {
+    struct cp3_server* owner = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    DBuf<Problem> d_probs;
+    DBuf<long long> d_a, d_b;
+    DBuf<Header> d_hdr;
+    DBuf<OscParams> d_params;
+    DBuf<int> d_done, d_status;
+    DBuf<unsigned long long> d_counter;
+    HBuf<Problem> h_probs;
+    HBuf<long long> h_a, h_b;
+    HBuf<Header> h_hdr;
+    HBuf<OscParams> h_params;
+    std::vector<std::shared_ptr<Request>> reqs;
+    bool busy = false;
+    std::atomic<int> finished{0};
+};
+
+}  // namespace
+
+struct cp3_server {
+    int device = 0, sms = 0;
+    std::string err;
+    std::mutex mu;  // requests map, incoming queue, pool, stats
+    std::condition_variable cv;
+    EarthModel model;
+    bool model_set = false;
+    double height_cm = 0.0;
+    int max_batch = 256;
+    long long max_bins = 8000000;
+    int64_t aging_ns = 4000000;  // 4 ms
+    size_t pool_bytes = 0;
+
+    // registration (host), then resident device arenas
+    std::vector<Template> tmpls;
+    std::vector<double> h_energies, h_cls_rho;
+    std::vector<int> h_row_off, h_seg_cls;
+    std::vector<float2> h_seg_len, h_baselines;
+    DBuf<double> d_energies, d_cls_rho;
+    DBuf<int> d_row_off, d_seg_cls;
+    DBuf<float2> d_seg_len, d_baselines;
+    DBuf<float> d_pool;
+    Pool pool;
+    Slot slots[2];
+
+    std::unordered_map<uint64_t, std::shared_ptr<Request>> requests;
+    std::deque<std::shared_ptr<Request>> incoming;
+    uint64_t next_id = 1;
+    std::thread loop;
+    std::atomic<bool> stop{false};
+    bool started = false;
+    std::atomic<long long> launches{0}, completed{0};
+    std::atomic<int> kernel_status{0};
+
+    ~cp3_server();
+};
+
+namespace {
+
+thread_local std::string g_server_create_error;
+
+int sfail(cp3_server* s, int code, const std::string& msg) {
+    if (s)
+        s->err = msg;
+    else
+        g_server_create_error = msg;
+    return code;
+}
+
+int scuda(cp3_server* s, cudaError_t e, const char* where) {
+    cudaGetLastError();
+    return sfail(s, e == cudaErrorMemoryAllocation ? CP3_ERR_OOM : CP3_ERR_CUDA,
+                 std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define S_CUDA(s, call, where)                              \
+    do {                                                    \
+        const cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return scuda(s, e_, where);  \
+    } while (0)
+
+// Host callback after a slot's launch: every request of the launch is done.
+void CUDART_CB on_launch_done(void* user) {
+    Slot* slot = static_cast<Slot*>(user);
+    const int64_t t = now_ns();
+    for (auto& r : slot->reqs) {
+        r->t_done = t;
+        r->state.store(kDone);
+    }
+    slot->owner->completed += (long long)slot->reqs.size();
+    slot->finished.store(1);
+    slot->owner->cv.notify_all();
+}
+
+// Packs queued requests into one launch on `slot`; caller holds s->mu.  Order: requests
+// older than the aging limit first (arrival order), then the rest smallest-first, so small
+// requests are not stuck behind large ones and large ones cannot starve.  A request is
+// admitted only if its table and result fit in the pool (admission by device memory).
+void launch_slot(cp3_server* s, Slot& slot) {
+    slot.reqs.clear();
+    const int64_t now = now_ns();
+    std::vector<std::shared_ptr<Request>> q(s->incoming.begin(), s->incoming.end());
+    std::stable_sort(q.begin(), q.end(), [&](const std::shared_ptr<Request>& a, const std::shared_ptr<Request>& b) {
+        const bool oa = now - a->t_submit > s->aging_ns, ob = now - b->t_submit > s->aging_ns;
+        if (oa != ob) return oa;
+        if (oa) return a->t_submit < b->t_submit;
+        return s->tmpls[a->tmpl].bins < s->tmpls[b->tmpl].bins;
+    });
+    long long bins = 0;
+    std::vector<char> taken(q.size(), 0);
+    for (size_t i = 0; i < q.size() && (int)slot.reqs.size() < s->max_batch; i++) {
+        Request& r = *q[i];
+        const Template& T = s->tmpls[r.tmpl];
+        if (!slot.reqs.empty() && bins + T.bins > s->max_bins) continue;
+        const size_t units = (T.tab_floats + T.out_floats) / kUnit;
+        size_t off = 0;
+        if (!s->pool.alloc(units, &off)) continue;  // waits for releases
+        r.pool_off = off;
+        r.pool_units = units;
+        bins += T.bins;
+        slot.reqs.push_back(q[i]);
+        taken[i] = 1;
+    }
+    if (slot.reqs.empty()) return;
+    std::deque<std::shared_ptr<Request>> rest;
+    for (size_t i = 0; i < q.size(); i++)
+        if (!taken[i]) rest.push_back(q[i]);
+    std::stable_sort(rest.begin(), rest.end(), [](const std::shared_ptr<Request>& a, const std::shared_ptr<Request>& b) {
+        return a->t_submit < b->t_submit;
+    });
+    s->incoming.swap(rest);
+    const int n = (int)slot.reqs.size();
+    long long a = 0, b = 0;
+    slot.h_a.ptr[0] = slot.h_b.ptr[0] = 0;
+    const int64_t t0 = now_ns();
+    for (int i = 0; i < n; i++) {
+        Request& r = *slot.reqs[i];
+        const Template& T = s->tmpls[r.tmpl];
+        Problem P{};
+        P.kind = T.kind;
+        P.ne = T.ne;
+        P.ne_pad = T.ne_pad;
+        P.nrows = T.nrows;
+        P.ncls = T.ncls;
+        P.param = i;
+        P.e_off = T.e_off;
+        P.row_off = T.row_off;
+        P.cls_off = T.cls_off;
+        P.tab_off = (long long)(r.pool_off * kUnit);
+        P.out_off = P.tab_off + (long long)T.tab_floats;
+        P.rho_e = T.rho_e;
+        slot.h_probs.ptr[i] = P;
+        slot.h_params.ptr[i] = r.params;
+        const long long nchunk = (T.ne + kTileE - 1) / kTileE;
+        if (T.kind == 0) {
+            a += nchunk * T.ncls;
+            b += nchunk * T.nrows;
+        } else {
+            b += (T.ne + 127) / 128;  // beam_chunk 1, R 1
+        }
+        slot.h_a.ptr[i + 1] = a;
+        slot.h_b.ptr[i + 1] = b;
+        r.t_start = t0;
+        r.state.store(kRunning);
+    }
+    *slot.h_hdr.ptr = Header{n, 1, a, b};
+    cudaStream_t st = slot.stream;
+    cudaMemcpyAsync(slot.d_probs.ptr, slot.h_probs.ptr, sizeof(Problem) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(slot.d_params.ptr, slot.h_params.ptr, sizeof(OscParams) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(slot.d_a.ptr, slot.h_a.ptr, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(slot.d_b.ptr, slot.h_b.ptr, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(slot.d_hdr.ptr, slot.h_hdr.ptr, sizeof(Header), cudaMemcpyHostToDevice, st);
+    cudaGraphLaunch(slot.graph, st);
+    slot.finished.store(0);
+    slot.busy = true;
+    cudaLaunchHostFunc(st, on_launch_done, &slot);
+    s->launches++;
+}
+
+void scheduler(cp3_server* s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (!s->stop.load()) {
+        for (Slot& sl : s->slots) {
+            if (sl.busy && sl.finished.load()) {
+                int st = 0;
+                cudaMemcpy(&st, sl.d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost);
+                if (st) s->kernel_status.store(st);
+                sl.busy = false;
+                sl.reqs.clear();
+            }
+        }
+        bool launched = false;
+        for (Slot& sl : s->slots)
+            if (!sl.busy && !s->incoming.empty()) {
+                launch_slot(s, sl);
+                launched = launched || sl.busy;
+            }
+        // The completion callback notifies without the mutex (it must not block a CUDA thread),
+        // so the wait is short and the state is re-read on every pass.
+        if (!launched)
+            s->cv.wait_for(lk, std::chrono::microseconds(20), [s] {
+                if (s->stop.load()) return true;
+                for (Slot& sl : s->slots)
+                    if (sl.busy && sl.finished.load()) return true;
+                bool free_slot = !s->slots[0].busy || !s->slots[1].busy;
+                return free_slot && !s->incoming.empty();
+            });
+    }
+}
+
+int capture_slot(cp3_server* s, Slot& sl) {
+    const int cap = s->max_batch;
+    S_CUDA(s, cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking), "stream");
+    S_CUDA(s, sl.d_probs.alloc(cap), "allocate");
+    S_CUDA(s, sl.d_a.alloc(cap + 1), "allocate");
+    S_CUDA(s, sl.d_b.alloc(cap + 1), "allocate");
+    S_CUDA(s, sl.d_hdr.alloc(1), "allocate");
+    S_CUDA(s, sl.d_params.alloc(cap), "allocate");
+    S_CUDA(s, sl.d_done.alloc(cap), "allocate");
+    S_CUDA(s, sl.d_status.alloc(1), "allocate");
+    S_CUDA(s, sl.d_counter.alloc(1), "allocate");
+    S_CUDA(s, sl.h_probs.alloc(cap), "pinned");
+    S_CUDA(s, sl.h_a.alloc(cap + 1), "pinned");
+    S_CUDA(s, sl.h_b.alloc(cap + 1), "pinned");
+    S_CUDA(s, sl.h_hdr.alloc(1), "pinned");
+    S_CUDA(s, sl.h_params.alloc(cap), "pinned");
+    S_CUDA(s, cudaMemset(sl.d_status.ptr, 0, sizeof(int)), "memset");
+    int occ = 0;
+    S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<1>, 128, 0), "occupancy");
+    const int grid = std::max(1, s->sms * std::max(occ, 1));
+    Args args{sl.d_hdr.ptr, sl.d_probs.ptr, sl.d_a.ptr, sl.d_b.ptr, sl.d_params.ptr,
+              s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr, s->d_seg_cls.ptr,
+              s->d_cls_rho.ptr, s->d_baselines.ptr, s->d_pool.ptr, s->d_pool.ptr,
+              sl.d_done.ptr, sl.d_counter.ptr, sl.d_status.ptr};
+    cudaStream_t cs;
+    S_CUDA(s, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, sizeof(unsigned long long), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_done.ptr, 0, sizeof(int) * cap, cs);
+    if (e == cudaSuccess) {
+        batch_kernel<1><<<grid, 128, 0, cs>>>(args);
+        e = cudaGetLastError();
+    }
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.graph, g, 0);
+    if (e2 == cudaSuccess) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return scuda(s, e, "graph capture");
+    return CP3_OK;
+}
+
+template <class T>
+cudaError_t upload(DBuf<T>& d, const std::vector<T>& v) {
+    cudaError_t e = d.alloc(v.size());
+    if (e == cudaSuccess && !v.empty())
+        e = cudaMemcpy(d.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+    return e;
+}
+
+}  // namespace
+
+cp3_server::~cp3_server() {
+    stop.store(true);
+    cv.notify_all();
+    if (loop.joinable()) loop.join();
+    cudaSetDevice(device);
+    for (Slot& sl : slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.graph) cudaGraphExecDestroy(sl.graph);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+}
+
+extern "C" {
+
+int cp3_server_create(int device, size_t pool_bytes, int max_batch, long long max_bins_per_launch,
+                      cp3_server** out) {
+    if (!out) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (max_batch < 1 || max_batch > 65536 || max_bins_per_launch < 1 || pool_bytes < (1u << 20))
+        return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "max_batch 1..65536, max_bins >= 1, pool >= 1 MiB");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return sfail(nullptr, CP3_ERR_CUDA, "No GPU found");
+    }
+    if (device < 0 || device >= ndev)
+        return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "The requested GPU Id " + std::to_string(device) + " is not available.");
+    cp3_server* s = new cp3_server();
+    s->device = device;
+    s->max_batch = max_batch;
+    s->max_bins = max_bins_per_launch;
+    s->pool_bytes = pool_bytes;
+    cudaSetDevice(device);
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device);
+    for (Slot& sl : s->slots) sl.owner = s;
+    *out = s;
+    return CP3_OK;
+}
+
+int cp3_server_destroy(cp3_server* s) {
+    delete s;
+    return CP3_OK;
+}
+
+const char* cp3_server_last_error(const cp3_server* s) {
+    return s ? s->err.c_str() : g_server_create_error.c_str();
+}
+
+int cp3_server_set_earth(cp3_server* s, const double* radii, const double* rho, const double* ye,
+                         int n, double production_height_km) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (s->started) return sfail(s, CP3_ERR_UNSUPPORTED, "the server is running");
+    std::string msg;
+    int rc = make_earth_model(radii, rho, nullptr, nullptr, ye, n, false, &s->model, &msg);
+    if (rc) return sfail(s, rc, msg);
+    s->height_cm = production_height_km * 100000.0;
+    s->model_set = true;
+    return CP3_OK;
+}
+
+int cp3_server_add_atmos_grid(cp3_server* s, const double* cosines, int nc, const double* energies,
+                              int ne, int* grid) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (s->started) return sfail(s, CP3_ERR_UNSUPPORTED, "the server is running");
+    if (!s->model_set) return sfail(s, CP3_ERR_NOT_SET, "cp3_server_set_earth before atmospheric grids");
+    if (nc < 1 || ne < 1 || !cosines || !energies) return sfail(s, CP3_ERR_BAD_SIZE, "empty grid");
+    TrajectoryTable t;
+    std::string msg;
+    int rc = build_trajectories(s->model, cosines, nc, s->height_cm, &t, &msg);
+    if (rc) return sfail(s, rc, msg);
+    Template T;
+    T.kind = 0;
+    T.ne = ne;
+    T.ne_pad = pad_energies(ne);
+    T.nrows = nc;
+    T.ncls = 1 + *std::max_element(t.maxlayers.begin(), t.maxlayers.end());
+    T.e_off = (long long)s->h_energies.size();
+    s->h_energies.insert(s->h_energies.end(), energies, energies + ne);
+    T.row_off = (long long)s->h_row_off.size();
+    const int base = (int)s->h_seg_len.size();
+    for (int v : t.offset) s->h_row_off.push_back(base + v);
+    for (size_t i = 0; i < t.len_km.size(); i++) {
+        const float h = (float)t.len_km[i];
+        s->h_seg_len.push_back(make_float2(h, (float)(t.len_km[i] - (double)h)));
+        s->h_seg_cls.push_back(t.cls[i]);
+    }
+    T.cls_off = (long long)s->h_cls_rho.size();
+    s->h_cls_rho.push_back(0.0);
+    for (int c = 1; c < T.ncls; c++) s->h_cls_rho.push_back(s->model.rho[c - 1] * s->model.ye[c - 1]);
+    T.tab_floats = (size_t)T.ncls * T.ne_pad * kMixFields;  // multiple of kUnit (ne_pad % 32 == 0)
+    T.out_floats = ((size_t)9 * nc * ne + kUnit - 1) / kUnit * kUnit;
+    T.bins = (long long)nc * ne;
+    s->tmpls.push_back(T);
+    if (grid) *grid = (int)s->tmpls.size() - 1;
+    return CP3_OK;
+}
+
+int cp3_server_add_beam_grid(cp3_server* s, const double* energies, int ne, double rho,
+                             const double* path_km, int n_baselines, int* grid) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (s->started) return sfail(s, CP3_ERR_UNSUPPORTED, "the server is running");
+    if (ne < 1 || !energies || n_baselines < 1 || !path_km) return sfail(s, CP3_ERR_BAD_SIZE, "empty grid");
+    Template T;
+    T.kind = 1;
+    T.ne = ne;
+    T.ne_pad = pad_energies(ne);
+    T.nrows = n_baselines;
+    T.e_off = (long long)s->h_energies.size();
+    s->h_energies.insert(s->h_energies.end(), energies, energies + ne);
+    T.row_off = (long long)s->h_baselines.size();
+    for (int j = 0; j < n_baselines; j++) {
+        const float h = (float)path_km[j];
+        s->h_baselines.push_back(make_float2(h, (float)(path_km[j] - (double)h)));
+    }
+    T.rho_e = rho * kDensityConvert;
+    T.tab_floats = 0;
+    T.out_floats = ((size_t)9 * n_baselines * ne + kUnit - 1) / kUnit * kUnit;
+    T.bins = (long long)n_baselines * ne;
+    s->tmpls.push_back(T);
+    if (grid) *grid = (int)s->tmpls.size() - 1;
+    return CP3_OK;
+}
+
+int cp3_server_start(cp3_server* s) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (s->started) return CP3_OK;
+    if (s->tmpls.empty()) return sfail(s, CP3_ERR_NOT_SET, "no grids registered");
+    S_CUDA(s, cudaSetDevice(s->device), "cudaSetDevice");
+    S_CUDA(s, upload(s->d_energies, s->h_energies), "upload grids");
+    S_CUDA(s, upload(s->d_cls_rho, s->h_cls_rho), "upload grids");
+    S_CUDA(s, upload(s->d_row_off, s->h_row_off), "upload grids");
+    S_CUDA(s, upload(s->d_seg_cls, s->h_seg_cls), "upload grids");
+    S_CUDA(s, upload(s->d_seg_len, s->h_seg_len), "upload grids");
+    S_CUDA(s, upload(s->d_baselines, s->h_baselines), "upload grids");
+    const size_t units = s->pool_bytes / (kUnit * sizeof(float));
+    S_CUDA(s, s->d_pool.alloc(units * kUnit), "allocate pool");
+    s->pool.init(units);
+    for (const Template& T : s->tmpls)
+        if ((T.tab_floats + T.out_floats) / kUnit > units)
+            return sfail(s, CP3_ERR_BAD_SIZE, "a registered grid does not fit in the pool");
+    for (Slot& sl : s->slots)
+        if (int rc = capture_slot(s, sl)) return rc;
+    s->started = true;
+    s->loop = std::thread(scheduler, s);
+    return CP3_OK;
+}
+
+int cp3_server_submit(cp3_server* s, int grid, double t12, double t13, double t23, double dcp,
+                      int knutype, double dm12sq, double dm23sq, int neutrino_type,
+                      unsigned long long* id) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (!s->started) return sfail(s, CP3_ERR_NOT_SET, "cp3_server_start first");
+    if (grid < 0 || grid >= (int)s->tmpls.size()) return sfail(s, CP3_ERR_INDEX, "no such grid");
+    if (neutrino_type != CP3_NEUTRINO && neutrino_type != CP3_ANTINEUTRINO)
+        return sfail(s, CP3_ERR_BAD_ARGUMENT, "neutrino type must be Neutrino or Antineutrino");
+    auto r = std::make_shared<Request>();
+    r->tmpl = grid;
+    MixingInput m;
+    m.theta12 = t12;
+    m.theta13 = t13;
+    m.theta23 = t23;
+    m.dcp = dcp;
+    m.knutype = knutype;
+    m.dm12sq = dm12sq;
+    m.dm23sq = dm23sq;
+    build_osc_params(m, neutrino_type, &r->params);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->id = s->next_id++;
+        r->t_submit = now_ns();
+        s->requests[r->id] = r;
+        s->incoming.push_back(r);
+    }
+    s->cv.notify_all();
+    if (id) *id = r->id;
+    return CP3_OK;
+}
+
+int cp3_server_wait(cp3_server* s, unsigned long long id, double timeout_s, int* done) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(id);
+    if (it == s->requests.end()) return sfail(s, CP3_ERR_INDEX, "no such request");
+    std::shared_ptr<Request> r = it->second;
+    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                             std::chrono::duration<double>(timeout_s));
+    // short timed waits: the completion callback notifies without taking the mutex
+    while (r->state.load() != kDone && Clock::now() < deadline)
+        s->cv.wait_for(lk, std::chrono::microseconds(100));
+    if (done) *done = r->state.load() == kDone ? 1 : 0;
+    if (s->kernel_status.load()) return sfail(s, CP3_ERR_CUDA, "batch kernel reported a wait time-out");
+    return CP3_OK;
+}
+
+int cp3_server_result(cp3_server* s, unsigned long long id, const float** ptr, size_t* count,
+                      double* latency_ms) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->requests.find(id);
+    if (it == s->requests.end()) return sfail(s, CP3_ERR_INDEX, "no such request");
+    const Request& r = *it->second;
+    if (r.state.load() != kDone) return sfail(s, CP3_ERR_NOT_SET, "request not done");
+    const Template& T = s->tmpls[r.tmpl];
+    if (ptr) *ptr = s->d_pool.ptr + r.pool_off * kUnit + T.tab_floats;
+    if (count) *count = (size_t)9 * T.nrows * T.ne;
+    if (latency_ms) *latency_ms = (r.t_done - r.t_submit) * 1e-6;
+    return CP3_OK;
+}
+
+int cp3_server_copy_result(cp3_server* s, unsigned long long id, void* dst) {
+    const float* src = nullptr;
+    size_t n = 0;
+    if (int rc = cp3_server_result(s, id, &src, &n, nullptr)) return rc;
+    if (!dst) return sfail(s, CP3_ERR_BAD_ARGUMENT, "null destination");
+    S_CUDA(s, cudaSetDevice(s->device), "cudaSetDevice");
+    S_CUDA(s, cudaMemcpy(dst, src, n * sizeof(float), cudaMemcpyDeviceToHost), "copy result");
+    return CP3_OK;
+}
+
+int cp3_server_release(cp3_server* s, unsigned long long id) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->requests.find(id);
+        if (it == s->requests.end()) return sfail(s, CP3_ERR_INDEX, "no such request");
+        if (it->second->state.load() != kDone) return sfail(s, CP3_ERR_NOT_SET, "request not done");
+        s->pool.release(it->second->pool_off, it->second->pool_units);
+        s->requests.erase(it);
+    }
+    s->cv.notify_all();
+    return CP3_OK;
+}
+
+int cp3_server_stats(cp3_server* s, long long* launches, long long* completed, long long* queued) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (launches) *launches = s->launches.load();
+    if (completed) *completed = s->completed.load();
+    if (queued) *queued = (long long)s->incoming.size();
+    return CP3_OK;
+}
+
+}  // extern "C"

@@ -250,6 +250,43 @@ int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream);
 int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins,
                    size_t* result_bytes, long long* tiles);
 
+/* ---- serving: continuous batching ------------------------------------------------------- */
+
+/* No reference counterpart.  A request is one registered grid + one parameter set
+ * + a neutrino type; submit returns at once.  A scheduler thread admits queued requests in
+ * arrival order as device memory (a pool of pool_bytes for their tables and results) and one
+ * of two launch slots free up, packs up to max_batch requests / max_bins_per_launch bins
+ * into one persistent launch, and overlaps consecutive launches on two streams.  Grids stay
+ * resident; a request's result stays on the device until cp3_server_release. */
+typedef struct cp3_server cp3_server;
+
+int cp3_server_create(int device, size_t pool_bytes, int max_batch,
+                      long long max_bins_per_launch, cp3_server** out);
+int cp3_server_destroy(cp3_server* s);
+const char* cp3_server_last_error(const cp3_server* s);
+int cp3_server_set_earth(cp3_server* s, const double* radii, const double* rho,
+                         const double* ye, int n, double production_height_km);
+int cp3_server_add_atmos_grid(cp3_server* s, const double* cosines, int n_cosines,
+                              const double* energies, int n_energies, int* grid);
+int cp3_server_add_beam_grid(cp3_server* s, const double* energies, int n_energies, double rho,
+                             const double* path_km, int n_baselines, int* grid);
+/* Uploads the grids, allocates the pool, captures the launch graphs, starts the loop. */
+int cp3_server_start(cp3_server* s);
+int cp3_server_submit(cp3_server* s, int grid, double theta12, double theta13, double theta23,
+                      double dcp, int knutype, double dm12sq, double dm23sq, int neutrino_type,
+                      unsigned long long* id);
+/* Blocks up to timeout_s; *done = 1 when the request's result is ready. */
+int cp3_server_wait(cp3_server* s, unsigned long long id, double timeout_s, int* done);
+/* Device pointer / float count of a finished request's result (layout as for batches) and its
+ * latency (submit to completion of its launch, ms). */
+int cp3_server_result(cp3_server* s, unsigned long long id, const float** ptr, size_t* count,
+                      double* latency_ms);
+/* Synchronous copy of a finished request's result to host memory (count floats). */
+int cp3_server_copy_result(cp3_server* s, unsigned long long id, void* dst);
+int cp3_server_release(cp3_server* s, unsigned long long id);
+int cp3_server_stats(cp3_server* s, long long* launches, long long* completed,
+                     long long* queued);
+
 /* ---- atmospheric propagation without allocation ------------------------------------------ */
 
 /* Size of the device scratch behind cp3_atmos_mixed_noalloc (reserved on every GPU that

@@ -311,16 +311,11 @@ void scheduler(cp3_server* s) {
                 launch_slot(s, sl);
                 launched = launched || sl.busy;
             }
-        // The completion callback notifies without the mutex (it must not block a CUDA thread),
-        // so the wait is short and the state is re-read on every pass.
-        if (!launched)
-            s->cv.wait_for(lk, std::chrono::microseconds(20), [s] {
-                if (s->stop.load()) return true;
-                for (Slot& sl : s->slots)
-                    if (sl.busy && sl.finished.load()) return true;
-                bool free_slot = !s->slots[0].busy || !s->slots[1].busy;
-                return free_slot && !s->incoming.empty();
-            });
+        // Nothing launchable (slots busy, queue empty, or the pool full until a release):
+        // sleep with the mutex released.  No predicate here -- a predicate that is already true
+        // would return without releasing it, and release() needs the mutex to free memory.
+        // The completion callback notifies without the mutex, so the wait is short.
+        if (!launched) s->cv.wait_for(lk, std::chrono::microseconds(20));
     }
 }
 

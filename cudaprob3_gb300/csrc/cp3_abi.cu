@@ -75,7 +75,7 @@ struct cp3_propagator {
 
     DevBuf<double> d_energies;
     DevBuf<int> d_seg_off, d_seg_cls;
-    DevBuf<double> d_seg_len, d_cls_rho;
+    DevBuf<double> d_seg_len, d_cls_rho, d_seg_rho;
     DevBuf<float2> d_seg_len_df;
     DevBuf<double> d_table64;
     DevBuf<float> d_table32;
@@ -193,6 +193,13 @@ int prepare_atmos(cp3_propagator* h) {
         CP3_CUDA(h, cudaMemcpy(h->d_seg_len_df.ptr, df.data(), sizeof(float2) * nseg,
                                cudaMemcpyHostToDevice), "upload trajectories");
     }
+    if (h->model.poly) {  // per-segment densities, no classes or eigen table
+        CP3_CUDA(h, h->d_seg_rho.reserve(nseg), "allocate trajectories");
+        CP3_CUDA(h, cudaMemcpy(h->d_seg_rho.ptr, t.rho_e.data(), sizeof(double) * nseg,
+                               cudaMemcpyHostToDevice), "upload trajectories");
+        h->traj_dirty = false;
+        return CP3_OK;
+    }
     // density classes: 0 = air, 1 + i = shell i (getDensityOfLayer: rhos[i] * yps[i])
     h->ncls_used = 1 + *std::max_element(t.maxlayers.begin(), t.maxlayers.end());
     std::vector<double> cls_rho(h->ncls_used, 0.0);
@@ -232,12 +239,16 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
         if (h->avg_bins > 0)
             return fail(h, CP3_ERR_UNSUPPORTED,
                         "production-height averaging is computed by the oracle only in this build");
-        if (h->model.poly)
-            return fail(h, CP3_ERR_UNSUPPORTED, "polynomial density model not yet on the GPU path");
         int rc = prepare_atmos(h);
         if (rc) return rc;
         mark(0);
-        if (h->precision == CP3_FP64) {
+        if (h->model.poly) {
+            mark(1);
+            const bool mixed = h->precision == CP3_MIXED;
+            e = launch_atmos_inline(p, mixed, h->d_energies.ptr, h->ne, h->d_seg_off.ptr,
+                                    mixed ? (const void*)h->d_seg_len_df.ptr : (const void*)h->d_seg_len.ptr,
+                                    h->d_seg_rho.ptr, h->nc, h->d_result.ptr, s);
+        } else if (h->precision == CP3_FP64) {
             e = launch_table_f64(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
                                  h->d_table64.ptr, s);
             mark(1);

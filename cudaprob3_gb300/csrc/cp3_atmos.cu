@@ -66,6 +66,95 @@ __device__ __forceinline__ void segment_matrix_f64(const double* __restrict__ t,
     }
 }
 
+// T = sum_k e^{i arg_k} C_k for a segment of its own density (quadratic model): the
+// reference's per-segment getMfast + get_product + getC, then the same phase sum.
+__device__ __forceinline__ void segment_matrix_inline_f64(const OscParams* __restrict__ p, double E,
+                                                          double rho, double L, cm3& T) {
+    double mm[3];
+    matter_masses_f64(p, E, rho, mm);
+    cd C[3][3][3];
+    flavour_projectors_f64(p, E, rho, mm, C);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) T.a[i][j] = cd{0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double s, c;
+        sincos(-kLoEFac * (mm[k] - p->dm[0]) * L / E, &s, &c);
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const cd v = C[k][q / 3][q % 3];
+            T.a[q / 3][q % 3].re += c * v.re - s * v.im;
+            T.a[q / 3][q % 3].im += c * v.im + s * v.re;
+        }
+    }
+}
+
+// FP64 atmospheric bins, quadratic density: every segment carries its own density.
+__global__ void __launch_bounds__(kBlock)
+    atmos_f64_inline_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
+                            int ne, const int* __restrict__ seg_off,
+                            const double* __restrict__ seg_len, const double* __restrict__ seg_rho,
+                            int ic0, int nc, double* __restrict__ out) {
+    __shared__ double s_len[kMaxSegments];
+    __shared__ double s_rho[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) {
+        s_len[i] = seg_len[s0 + i];
+        s_rho[i] = seg_rho[s0 + i];
+    }
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const double E = energies[ie];
+    const int M = nseg - 1;
+    cm3 fin, mantle, T;
+    segment_matrix_inline_f64(&p, E, s_rho[0], s_len[0], fin);
+    for (int l = 1; l <= M; l++) {
+        segment_matrix_inline_f64(&p, E, s_rho[l], s_len[l], T);
+        mul3(T, fin, fin);
+        if (l < M) {
+            if (l == 1)
+                mantle = T;
+            else
+                mul3(mantle, T, mantle);
+        }
+    }
+    if (M >= 2) mul3(mantle, fin, fin);
+    double mm[3];
+    matter_masses_f64(&p, E, s_rho[0], mm);
+    cd Catm[3][3][3];
+    flavour_projectors_f64(&p, E, s_rho[0], mm, Catm);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            cd P[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                double re = 0.0, im = 0.0;
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    re += fin.a[i][q].re * Catm[k][q][j].re - fin.a[i][q].im * Catm[k][q][j].im;
+                    im += fin.a[i][q].im * Catm[k][q][j].re + fin.a[i][q].re * Catm[k][q][j].im;
+                }
+                P[k] = cd{re, im};
+            }
+            double prob = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                prob += P[k].re * P[k].re + P[k].im * P[k].im;
+#pragma unroll
+                for (int q = 0; q < k; q++)
+                    prob += 2. * P[q].re * P[k].re + 2. * P[q].im * P[k].im;
+            }
+            out[((size_t)(j * 3 + i) * nc + ic) * ne + ie] = prob;
+        }
+}
+
 __global__ void __launch_bounds__(kBlock)
     atmos_f64_kernel(const double* __restrict__ energies, int ne, int ne_pad,
                      const double* __restrict__ table, const int* __restrict__ seg_off,
@@ -157,6 +246,30 @@ __global__ void __launch_bounds__(kBlock)
                     nseg - 1, w, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
 
+// Mixed atmospheric bins, quadratic density: every segment solves its own eigen-system.
+__global__ void __launch_bounds__(kBlock)
+    atmos_mixed_inline_kernel(const __grid_constant__ OscParams p, WParams w,
+                              const double* __restrict__ energies, int ne,
+                              const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
+                              const double* __restrict__ seg_rho, int ic0, int nc,
+                              float* __restrict__ out) {
+    __shared__ float2 s_len[kMaxSegments];
+    __shared__ double s_rho[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) {
+        s_len[i] = seg_len[s0 + i];
+        s_rho[i] = seg_rho[s0 + i];
+    }
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const double E = energies[ie];
+    atmos_bin_mixed_with([&](int l, cs6& S) { segment_matrix_inline(&p, E, s_rho[l], s_len[l], S); },
+                         nseg - 1, w, out + (size_t)ic * ne + ie, (size_t)nc * ne);
+}
+
 // Beam, mixed: per-bin eigen-decomposition with double-float refinement
 // (rotated_eigen_mixed), double-float phase, FP32 matrix work.
 __global__ void __launch_bounds__(kBlock)
@@ -196,6 +309,25 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_mixed_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
                                                    seg_cls, ic0, n_cosines, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
+                                const int* seg_off, const void* seg_len, const double* seg_rho,
+                                int n_cosines, void* out, cudaStream_t s) {
+    if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
+    for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
+        const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
+        dim3 grid((ne + kBlock - 1) / kBlock, rows);
+        if (mixed)
+            atmos_mixed_inline_kernel<<<grid, kBlock, 0, s>>>(p, wparams(p), energies, ne, seg_off,
+                                                              (const float2*)seg_len, seg_rho, ic0,
+                                                              n_cosines, (float*)out);
+        else
+            atmos_f64_inline_kernel<<<grid, kBlock, 0, s>>>(p, energies, ne, seg_off,
+                                                            (const double*)seg_len, seg_rho, ic0,
+                                                            n_cosines, (double*)out);
     }
     return cudaGetLastError();
 }

@@ -30,6 +30,12 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
                                const int* seg_off, const float2* seg_len, const int* seg_cls,
                                int n_cosines, float* out, cudaStream_t s);
 
+// Atmospheric bins whose segments each carry their own electron density (quadratic model):
+// per-segment eigen-solve.  seg_len: double[] (FP64) or float2[] hi/lo (mixed).
+cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
+                                const int* seg_off, const void* seg_len, const double* seg_rho,
+                                int n_cosines, void* out, cudaStream_t s);
+
 // Beam bins: rho_e = rho * 0.5 (electron density), L in km.
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,
                             double L_km, double* out, cudaStream_t s);

@@ -174,16 +174,13 @@ inline WParams wparams(const OscParams& p) {
     return WParams{(float)p.w[0], (float)p.w[1], (float)p.w[2], (float)p.w[3]};
 }
 
-// One atmospheric bin: the trajectory's segment lengths and classes are in shared memory
-// (s_len[0..M], s_cls[0..M]); tab points at this bin's energy column of the table (entry of
-// class c at tab + c * cls_stride); the nine probabilities go to out[ch * plane].
-template <bool kL2Only = false>
-__device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, size_t cls_stride,
-                                                const float2* s_len, const int* s_cls, int M,
-                                                const WParams& w, float* __restrict__ out,
-                                                size_t plane) {
+// One atmospheric bin over M+1 segments, generic in where each segment's layer matrix comes
+// from: seg(l, S) fills S for segment l (0 = air, then shells inwards).
+template <class SegFn>
+__device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WParams& w,
+                                                     float* __restrict__ out, size_t plane) {
     cs6 S0;
-    segment_matrix_mixed<kL2Only>(tab + s_cls[0] * cls_stride, s_len[0], S0);
+    seg(0, S0);
     cg9 A2;
     if (M == 0) {
         sym_to_gen(S0, A2);
@@ -191,17 +188,17 @@ __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, s
         cs6 S;
         cg9 B;
         if (M == 1) {
-            segment_matrix_mixed<kL2Only>(tab + s_cls[1] * cls_stride, s_len[1], S);
+            seg(1, S);
             sym_to_gen(S, B);  // B = S_1, Q = S_1
             mul_gs(B, S0, A2);
         } else {
-            segment_matrix_mixed<kL2Only>(tab + s_cls[1] * cls_stride, s_len[1], S);
+            seg(1, S);
             sym_to_gen(S, B);
             for (int l = 2; l < M; l++) {
-                segment_matrix_mixed<kL2Only>(tab + s_cls[l] * cls_stride, s_len[l], S);
+                seg(l, S);
                 mul_sg(S, B, B);
             }
-            segment_matrix_mixed<kL2Only>(tab + s_cls[M] * cls_stride, s_len[M], S);
+            seg(M, S);
             cg9 X;
             mul_sg(S, B, X);  // X = S_M B
             cs6 Q;            // Q = B^T X (symmetric)
@@ -224,6 +221,34 @@ __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, s
     }
     newton_schulz(A2);
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
+}
+
+// One atmospheric bin from the eigen table: the trajectory's segment lengths and classes are
+// in shared memory (s_len[0..M], s_cls[0..M]); tab points at this bin's energy column of the
+// table (entry of class c at tab + c * cls_stride); probabilities go to out[ch * plane].
+template <bool kL2Only = false>
+__device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, size_t cls_stride,
+                                                const float2* s_len, const int* s_cls, int M,
+                                                const WParams& w, float* __restrict__ out,
+                                                size_t plane) {
+    atmos_bin_mixed_with(
+        [&](int l, cs6& S) { segment_matrix_mixed<kL2Only>(tab + s_cls[l] * cls_stride, s_len[l], S); },
+        M, w, out, plane);
+}
+
+// Layer matrix of a segment whose density is its own (quadratic density model): the
+// eigen-decomposition is solved for this segment (double-float refined).
+__device__ __forceinline__ void segment_matrix_inline(const OscParams* __restrict__ p, double E,
+                                                      double rho_e, float2 L, cs6& S) {
+    float P[2][6], om[2][2], z[2][2];
+    rotated_eigen_mixed(p, E, rho_e, P, om);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        float lo;
+        const float r = reduced_phase(om[k][0], om[k][1], L.x, L.y, lo);
+        unit_phase_minus_one(r, lo, z[k][0], z[k][1]);
+    }
+    layer_matrix(z, P[0], P[1], S);
 }
 
 // One beam energy: eigen-decomposition (double-float refined), then for each baseline

@@ -17,8 +17,7 @@ from tests.gpu_helpers import run_atmos, run_beam, run_fixture
 
 pytestmark = pytest.mark.gpu
 
-GPU_FIXTURES = [f for f in golden_files()
-                if not any(k in os.path.basename(f) for k in ("poly", "avg"))]
+GPU_FIXTURES = [f for f in golden_files() if "avg" not in os.path.basename(f)]
 FP64_TOL = 1e-12
 MIXED_TOL = 1e-5
 DEGENERATE_TOL = 1e-9
@@ -88,4 +87,20 @@ def test_beam_against_oracle(oracle, prec, tol, L):
                                    knu), anti, en, 2.6, L)
             got = run_beam(prec, [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq],
                            knu, anti, en, 2.6, L)
+            assert np.abs(got - ref).max() <= tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_quadratic_density_against_oracle(oracle, prec, tol):
+    """getDensityOfLayerPoly model (physics.hpp:651-739): every segment its own density."""
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix
+    r, a, b, c, ye = earth.PREM_4LAYER_QUAD_V2
+    cz, en = np.linspace(-1, 1, 61), earth.log_energy_grid(47)
+    for m in earth.gaussian_sets(3, seed=21):
+        for anti, knu in ((False, 1), (True, -1)):
+            ref = oracle.atmos(OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq,
+                                    knu), anti, cz, en, r, None, ye, 18.0, poly_abc=(a, b, c))
+            got = run_atmos(prec, [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq],
+                            knu, anti, cz, en, r, None, ye, 18.0, poly_abc=(a, b, c))
             assert np.abs(got - ref).max() <= tol

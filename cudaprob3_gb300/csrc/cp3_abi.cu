@@ -76,6 +76,8 @@ struct cp3_propagator {
     DevBuf<double> d_energies;
     DevBuf<int> d_seg_off, d_seg_cls;
     DevBuf<double> d_seg_len, d_cls_rho, d_seg_rho;
+    DevBuf<double> d_ph_prob, d_ph_shift, d_air_cm;  // production-height averaging
+    bool avg_dirty = true;
     DevBuf<float2> d_seg_len_df;
     DevBuf<double> d_table64;
     DevBuf<float> d_table32;
@@ -216,6 +218,32 @@ int prepare_atmos(cp3_propagator* h) {
     return CP3_OK;
 }
 
+// Averaging inputs: the client's probabilities and, per cosine, the path-length shifts at the
+// bin edges and the air segment in cm (the reference's `dist` of layer 0).
+int prepare_averaging(cp3_propagator* h, AvgArrays* av) {
+    if (h->avg_bins == 0) return CP3_OK;
+    if (h->avg_dirty) {
+        std::vector<double> shifts;
+        production_height_shifts(h->cosines.data(), h->nc, h->height_cm, h->avg_edges.data(),
+                                 h->avg_bins, &shifts);
+        CP3_CUDA(h, h->d_ph_prob.reserve(h->avg_prob.size()), "allocate averaging");
+        CP3_CUDA(h, h->d_ph_shift.reserve(shifts.size()), "allocate averaging");
+        CP3_CUDA(h, h->d_air_cm.reserve(h->nc), "allocate averaging");
+        CP3_CUDA(h, cudaMemcpy(h->d_ph_prob.ptr, h->avg_prob.data(), sizeof(double) * h->avg_prob.size(),
+                               cudaMemcpyHostToDevice), "upload averaging");
+        CP3_CUDA(h, cudaMemcpy(h->d_ph_shift.ptr, shifts.data(), sizeof(double) * shifts.size(),
+                               cudaMemcpyHostToDevice), "upload averaging");
+        CP3_CUDA(h, cudaMemcpy(h->d_air_cm.ptr, h->traj.air_cm.data(), sizeof(double) * h->nc,
+                               cudaMemcpyHostToDevice), "upload averaging");
+        h->avg_dirty = false;
+    }
+    av->prob = h->d_ph_prob.ptr;
+    av->shift = h->d_ph_shift.ptr;
+    av->air_cm = h->d_air_cm.ptr;
+    av->n_bins = h->avg_bins;
+    return CP3_OK;
+}
+
 int launch(cp3_propagator* h, int type, cudaStream_t s) {
     if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
         return fail(h, CP3_ERR_BAD_ARGUMENT, "neutrino type must be Neutrino or Antineutrino");
@@ -236,10 +264,15 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
         if (!h->height_set)
             return fail(h, CP3_ERR_NOT_SET,
                         "CudaPropagatorSingle::calculateProbabilities. production height was not set");
-        if (h->avg_bins > 0)
+        if (h->avg_bins > 0 && h->precision != CP3_FP64)
             return fail(h, CP3_ERR_UNSUPPORTED,
-                        "production-height averaging is computed by the oracle only in this build");
+                        "production-height averaging runs on the FP64 kernels (create the handle with CP3_FP64)");
+        const bool traj_was_dirty = h->traj_dirty;
         int rc = prepare_atmos(h);
+        if (rc) return rc;
+        if (traj_was_dirty) h->avg_dirty = true;
+        AvgArrays av;
+        rc = prepare_averaging(h, &av);
         if (rc) return rc;
         mark(0);
         if (h->model.poly) {
@@ -247,7 +280,7 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
             const bool mixed = h->precision == CP3_MIXED;
             e = launch_atmos_inline(p, mixed, h->d_energies.ptr, h->ne, h->d_seg_off.ptr,
                                     mixed ? (const void*)h->d_seg_len_df.ptr : (const void*)h->d_seg_len.ptr,
-                                    h->d_seg_rho.ptr, h->nc, h->d_result.ptr, s);
+                                    h->d_seg_rho.ptr, h->nc, av, h->d_result.ptr, s);
         } else if (h->precision == CP3_FP64) {
             e = launch_table_f64(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
                                  h->d_table64.ptr, s);
@@ -255,7 +288,7 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
             if (e == cudaSuccess)
                 e = launch_atmos_f64(p, h->d_energies.ptr, h->ne, h->d_table64.ptr,
                                      h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
-                                     (double*)h->d_result.ptr, s);
+                                     av, (double*)h->d_result.ptr, s);
         } else {
             e = launch_table_mixed(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
                                    h->d_table32.ptr, s);
@@ -500,6 +533,7 @@ int cp3_set_production_height_averaging(cp3_propagator* h, int n_bins, const dou
         h->avg_bins = 0;
         return CP3_OK;
     }
+    h->avg_dirty = true;
     if (!prob || !edges_km) return fail(h, CP3_ERR_BAD_ARGUMENT, "null production-height arrays");
     const size_t np = (size_t)n_bins * 2 * 3 * h->ne * h->nc;
     h->avg_prob.assign(prob, prob + np);

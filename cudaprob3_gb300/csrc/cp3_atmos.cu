@@ -66,6 +66,97 @@ __device__ __forceinline__ void segment_matrix_f64(const double* __restrict__ t,
     }
 }
 
+// Production-height averaging (physics.hpp:997-1067), the reference's shift factors for the
+// pairs (k, q) = (1,0), (2,0), (2,1) and each initial flavour f: sf[pair][f] = sum over bins
+// of prob * sinc(d hw / 2) e^{i d hm}, d = darg0[k] - darg0[q]; the diagonal is 1.
+struct AvgInput {
+    const double* prob;    // [2][3][ne][nc][nb]
+    const double* shift;   // [nc][nb + 1] path-length shifts at the bin edges, cm
+    const double* air_cm;  // [nc] segment 0 length, cm
+    int nb, type;
+};
+
+// math::defined_sinc (math.hpp:49-55) as the reference evaluates it: its unqualified abs()
+// binds to int abs(int), so the series branch runs for every |x| < 1.
+__device__ __forceinline__ double sinc_reference(double x) {
+    if (fabs(x) >= 1.0) return sin(x) / x;
+    return 1.0 - x * x / 6. + x * x * x * x / 120.;
+}
+
+__device__ __forceinline__ void avg_shift_factors(const AvgInput& av, int ic, int nc, int ie, int ne,
+                                                  const double arg0[3], cd sf[3][3]) {
+    const double dist = av.air_cm[ic];
+    double d0[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) d0[k] = dist == 0. ? 0. : arg0[k] / dist;
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int f = 0; f < 3; f++) sf[q][f] = cd{0.0, 0.0};
+    const int pa[3] = {1, 2, 2}, pb[3] = {0, 0, 1};
+    const double* sh = av.shift + (size_t)ic * (av.nb + 1);
+    for (int p = 0; p < av.nb; p++) {
+        const double h0 = sh[p], h1 = sh[p + 1];
+        const double hm = (h1 + h0) / 2., hw = (h1 - h0);
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const double d = d0[pa[q]] - d0[pb[q]];
+            const double sarg = 0.5 * d * hw;
+            const double fre = sinc_reference(sarg) * cos(d * hm);
+            const double fim = sinc_reference(sarg) * sin(d * hm);
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                const size_t idx = (((size_t)(av.type * 3 + f) * ne + ie) * nc + ic) * av.nb + p;
+                const double w = av.prob[idx];
+                sf[q][f].re += w * fre;
+                sf[q][f].im += w * fim;
+            }
+        }
+    }
+}
+
+// Probabilities from fin and the air layer's projectors (physics.hpp:1102-1130); with
+// averaging the cross terms carry the shift factors, without they carry 1 + 0i.
+template <class CatmFn>
+__device__ __forceinline__ void store_prob_f64(const cm3& fin, CatmFn catm, const cd (*sf)[3],
+                                               double* __restrict__ out, size_t plane) {
+    const int pair[3][3] = {{-1, -1, -1}, {0, -1, -1}, {1, 2, -1}};  // (k, q) -> index, q < k
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            cd P[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                double re = 0.0, im = 0.0;
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    const cd c = catm(k, q, j);
+                    re += fin.a[i][q].re * c.re - fin.a[i][q].im * c.im;
+                    im += fin.a[i][q].im * c.re + fin.a[i][q].re * c.im;
+                }
+                P[k] = cd{re, im};
+            }
+            double prob = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                prob += P[k].re * P[k].re + P[k].im * P[k].im;
+#pragma unroll
+                for (int q = 0; q < k; q++) {
+                    if (sf) {
+                        const cd t = sf[pair[k][q]][j];
+                        prob += 2. * P[q].re * P[k].re * t.re + 2. * P[q].im * P[k].im * t.re +
+                                2. * P[q].im * P[k].re * t.im - 2. * P[q].re * P[k].im * t.im;
+                    } else {
+                        prob += 2. * P[q].re * P[k].re + 2. * P[q].im * P[k].im;  // shift 1 + 0i
+                    }
+                }
+            }
+            // Prob[i][j] (i final, j initial) is P(j -> i): channel j*3+i.
+            out[(size_t)(j * 3 + i) * plane] = prob;
+        }
+}
+
 // T = sum_k e^{i arg_k} C_k for a segment of its own density (quadratic model): the
 // reference's per-segment getMfast + get_product + getC, then the same phase sum.
 __device__ __forceinline__ void segment_matrix_inline_f64(const OscParams* __restrict__ p, double E,
@@ -96,7 +187,7 @@ __global__ void __launch_bounds__(kBlock)
     atmos_f64_inline_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
                             int ne, const int* __restrict__ seg_off,
                             const double* __restrict__ seg_len, const double* __restrict__ seg_rho,
-                            int ic0, int nc, double* __restrict__ out) {
+                            int ic0, int nc, AvgInput av, double* __restrict__ out) {
     __shared__ double s_len[kMaxSegments];
     __shared__ double s_rho[kMaxSegments];
     const int ic = ic0 + blockIdx.y;
@@ -128,38 +219,25 @@ __global__ void __launch_bounds__(kBlock)
     matter_masses_f64(&p, E, s_rho[0], mm);
     cd Catm[3][3][3];
     flavour_projectors_f64(&p, E, s_rho[0], mm, Catm);
+    auto catm = [&](int k, int q, int j) { return Catm[k][q][j]; };
+    double* o = out + (size_t)ic * ne + ie;
+    if (av.nb > 0) {
+        double arg0[3];
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cd P[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                double re = 0.0, im = 0.0;
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    re += fin.a[i][q].re * Catm[k][q][j].re - fin.a[i][q].im * Catm[k][q][j].im;
-                    im += fin.a[i][q].im * Catm[k][q][j].re + fin.a[i][q].re * Catm[k][q][j].im;
-                }
-                P[k] = cd{re, im};
-            }
-            double prob = 0.0;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                prob += P[k].re * P[k].re + P[k].im * P[k].im;
-#pragma unroll
-                for (int q = 0; q < k; q++)
-                    prob += 2. * P[q].re * P[k].re + 2. * P[q].im * P[k].im;
-            }
-            out[((size_t)(j * 3 + i) * nc + ic) * ne + ie] = prob;
-        }
+        for (int k = 0; k < 3; k++) arg0[k] = -kLoEFac * (mm[k] - p.dm[0]) * s_len[0] / E;
+        cd sf[3][3];
+        avg_shift_factors(av, ic, nc, ie, ne, arg0, sf);
+        store_prob_f64(fin, catm, sf, o, (size_t)nc * ne);
+    } else {
+        store_prob_f64(fin, catm, (const cd(*)[3]) nullptr, o, (size_t)nc * ne);
+    }
 }
 
 __global__ void __launch_bounds__(kBlock)
     atmos_f64_kernel(const double* __restrict__ energies, int ne, int ne_pad,
                      const double* __restrict__ table, const int* __restrict__ seg_off,
                      const double* __restrict__ seg_len, const int* __restrict__ seg_cls,
-                     int ic0, int nc, double* __restrict__ out) {
+                     int ic0, int nc, AvgInput av, double* __restrict__ out) {
     __shared__ double s_len[kMaxSegments];
     __shared__ int s_cls[kMaxSegments];
     const int ic = ic0 + blockIdx.y;
@@ -191,37 +269,23 @@ __global__ void __launch_bounds__(kBlock)
     }
     if (M >= 2) mul3(mantle, fin, fin);
 
-    // Probabilities as physics.hpp:1102-1130 with no averaging: Product_k = fin . C_atm[k],
-    // Prob = sum_k |Product_k|^2 + 2 sum_{q<k} Re(Product_q conj Product_k).
+    // Probabilities: Product_k = fin . C_atm[k] with the air layer's projectors from the table.
     const double* ta = tab + s_cls[0] * cls_stride;
+    auto catm = [&](int k, int q, int j) {
+        return cd{__ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2) * ne_pad),
+                  __ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2 + 1) * ne_pad)};
+    };
+    double* o = out + (size_t)ic * ne + ie;
+    if (av.nb > 0) {
+        double arg0[3];
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cd P[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                double re = 0.0, im = 0.0;
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    const double cre = __ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2) * ne_pad);
-                    const double cim = __ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2 + 1) * ne_pad);
-                    re += fin.a[i][q].re * cre - fin.a[i][q].im * cim;
-                    im += fin.a[i][q].im * cre + fin.a[i][q].re * cim;
-                }
-                P[k] = cd{re, im};
-            }
-            double prob = 0.0;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                prob += P[k].re * P[k].re + P[k].im * P[k].im;
-#pragma unroll
-                for (int q = 0; q < k; q++)
-                    prob += 2. * P[q].re * P[k].re + 2. * P[q].im * P[k].im;  // shift = 1 + 0i
-            }
-            // Prob[i][j] (i final, j initial) is P(j -> i): channel j*3+i.
-            out[((size_t)(j * 3 + i) * nc + ic) * ne + ie] = prob;
-        }
+        for (int k = 0; k < 3; k++) arg0[k] = -kLoEFac * __ldg(ta + (size_t)(54 + k) * ne_pad) * s_len[0] / E;
+        cd sf[3][3];
+        avg_shift_factors(av, ic, nc, ie, ne, arg0, sf);
+        store_prob_f64(fin, catm, sf, o, (size_t)nc * ne);
+    } else {
+        store_prob_f64(fin, catm, (const cd(*)[3]) nullptr, o, (size_t)nc * ne);
+    }
 }
 
 // Mixed atmospheric bins (the physics of calculate_atmos rearranged for FP32: see
@@ -285,15 +349,17 @@ __global__ void __launch_bounds__(kBlock)
 
 cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
                              const double* table, const int* seg_off, const double* seg_len,
-                             const int* seg_cls, int n_cosines, double* out, cudaStream_t s) {
+                             const int* seg_cls, int n_cosines, const AvgArrays& avg, double* out,
+                             cudaStream_t s) {
     (void)p;
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
+    const AvgInput av{avg.prob, avg.shift, avg.air_cm, avg.n_bins, p.anti};
     for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
         const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_f64_kernel<<<grid, kBlock, 0, s>>>(energies, ne, ne_pad, table, seg_off, seg_len,
-                                                 seg_cls, ic0, n_cosines, out);
+                                                 seg_cls, ic0, n_cosines, av, out);
     }
     return cudaGetLastError();
 }
@@ -315,8 +381,9 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
 
 cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
                                 const int* seg_off, const void* seg_len, const double* seg_rho,
-                                int n_cosines, void* out, cudaStream_t s) {
+                                int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
+    const AvgInput av{avg.prob, avg.shift, avg.air_cm, avg.n_bins, p.anti};
     for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
         const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
@@ -327,7 +394,7 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
         else
             atmos_f64_inline_kernel<<<grid, kBlock, 0, s>>>(p, energies, ne, seg_off,
                                                             (const double*)seg_len, seg_rho, ic0,
-                                                            n_cosines, (double*)out);
+                                                            n_cosines, av, (double*)out);
     }
     return cudaGetLastError();
 }

@@ -243,6 +243,8 @@ int build_trajectories(const EarthModel& e, const double* cosines, int nc, doubl
         t.max_segments = std::max(t.max_segments, M + 1);
     }
     const int total = t.offset[nc];
+    t.air_cm.resize(nc);
+    t.path_cm.resize(nc);
     t.len_km.resize(total);
     t.rho_e.resize(total);
     t.cls.resize(total);
@@ -255,9 +257,11 @@ int build_trajectories(const EarthModel& e, const double* cosines, int nc, doubl
             std::sqrt((kREarthCm + height_cm) * (kREarthCm + height_cm) -
                       (kREarthCm * kREarthCm) * (1 - cosz * cosz)) -
             kREarthCm * cosz;
+        t.path_cm[ic] = path_cm;
         for (int l = 0; l <= M; l++) {
             const int s = t.offset[ic] + l;
             const double d = segment_cm(e, l, M, path_cm, earth_cm, cosz);
+            if (l == 0) t.air_cm[ic] = d;
             t.len_km[s] = d / kKm2Cm;
             if (e.poly) {
                 t.rho_e[s] = segment_density_poly(e, cosz, l, M, d);
@@ -271,6 +275,21 @@ int build_trajectories(const EarthModel& e, const double* cosines, int nc, doubl
     }
     *out = std::move(t);
     return CP3_OK;
+}
+
+void production_height_shifts(const double* cosines, int nc, double height_cm,
+                              const double* edges_km, int nb, std::vector<double>* out) {
+    out->assign((size_t)nc * (nb + 1), 0.0);
+    const double R = kREarthCm;
+    for (int ic = 0; ic < nc; ic++) {
+        const double c = cosines[ic];
+        const double path = std::sqrt((R + height_cm) * (R + height_cm) - (R * R) * (1 - c * c)) - R * c;
+        for (int p = 0; p <= nb; p++) {
+            const double hcm = kKm2Cm * edges_km[p];
+            const double v = std::sqrt((R + hcm) * (R + hcm) - (R * R) * (1 - c * c)) - R * c;
+            (*out)[(size_t)ic * (nb + 1) + p] = v - path;
+        }
+    }
 }
 
 int parse_model_file(const char* path, int* ncols, std::vector<std::vector<double>>* cols,

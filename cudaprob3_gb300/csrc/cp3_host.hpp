@@ -46,8 +46,15 @@ struct TrajectoryTable {
     std::vector<double> rho_e;     // segments
     std::vector<int> cls;          // segments
     std::vector<int> maxlayers;    // n_cosines
+    std::vector<double> air_cm;    // n_cosines: segment 0 in cm, as calculate_atmos's `dist`
+    std::vector<double> path_cm;   // n_cosines: PathLength (physics.hpp:897-898)
     int max_segments = 0;
 };
+
+// Production-height averaging (physics.hpp:1020-1027): for every cosine the shift of the
+// path length at each bin edge, PathLength(edge) - PathLength, cm; out[ic * (nb+1) + p].
+void production_height_shifts(const double* cosines, int nc, double height_cm,
+                              const double* edges_km, int nb, std::vector<double>* out);
 
 // Geometry of physics::calculate_atmos (physics.hpp:837, 897-898) and
 // getTraversedDistanceOfLayer / getDensityOfLayer / getDensityOfLayerPoly (:634-787).

@@ -22,10 +22,19 @@ cudaError_t launch_table_f64(const OscParams& p, const double* energies, int ne,
 cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int ne,
                                const double* cls_rho, int ncls, float* table, cudaStream_t s);
 
-// Atmospheric bins over a cosine range [ic0, ic0 + nrows) of an n_cosines-row result.
+// Production-height averaging inputs of the FP64 kernels (n_bins == 0: fixed height).
+struct AvgArrays {
+    const double* prob = nullptr;    // [2][3][ne][nc][n_bins]
+    const double* shift = nullptr;   // [nc][n_bins + 1] path-length shifts at the edges, cm
+    const double* air_cm = nullptr;  // [nc] first (air) segment, cm
+    int n_bins = 0;
+};
+
+// Atmospheric bins of an n_cosines-row result.
 cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
                              const double* table, const int* seg_off, const double* seg_len,
-                             const int* seg_cls, int n_cosines, double* out, cudaStream_t s);
+                             const int* seg_cls, int n_cosines, const AvgArrays& avg, double* out,
+                             cudaStream_t s);
 cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
                                const int* seg_off, const float2* seg_len, const int* seg_cls,
                                int n_cosines, float* out, cudaStream_t s);
@@ -34,7 +43,7 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
 // per-segment eigen-solve.  seg_len: double[] (FP64) or float2[] hi/lo (mixed).
 cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
                                 const int* seg_off, const void* seg_len, const double* seg_rho,
-                                int n_cosines, void* out, cudaStream_t s);
+                                int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s);
 
 // Beam bins: rho_e = rho * 0.5 (electron density), L in km.
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,

@@ -1,0 +1,76 @@
+"""Production-height averaging on the FP64 kernels (physics.hpp:997-1067, switched on
+explicitly: the reference's own switch never enables it) against the fixture made by the
+reference's calculate_atmos and against the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from cudaprob3_gb300 import AtmosCudaPropagatorSingle, earth
+from tests.conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def run_avg(prec, mix6, knu, anti, cz, en, radii, rho, ye, h, nb, prob, edges, poly_abc=None):
+    p = AtmosCudaPropagatorSingle(0, len(cz), len(en), precision=prec)
+    p.setEnergyList(en)
+    p.setCosineList(cz)
+    p.setMNSMatrix(*mix6[:4], knu)
+    p.setNeutrinoMasses(mix6[4], mix6[5])
+    if poly_abc is None:
+        p.setDensity(radii, rho, ye)
+    else:
+        p.setDensity(radii, *poly_abc, ye)
+    p.setProductionHeight(h)
+    p.SetNumberOfProductionHeightBinsForAveraging(nb)
+    p.setProductionHeightList(prob, edges)
+    p.calculateProbabilities(1 if anti else 0)
+    return p.probabilities()
+
+
+def test_averaging_matches_reference_fixture():
+    d = np.load(os.path.join(GOLDEN, "atmos_avg.npz"))
+    for t, knu in ((0, 1), (1, -1)):
+        got = run_avg("fp64", d["mix"], knu, t == 1, d["cosines"], d["energies"], d["radii"],
+                      d["rho"], d["ye"], float(d["h_km"]), int(d["avg_bins"]), d["avg_prob"],
+                      d["avg_edges"])
+        assert np.abs(got - d["out"][t]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("poly", [False, True])
+def test_averaging_against_oracle(oracle, poly):
+    from oracle.oracle import Mixing as OMix
+    rng = np.random.default_rng(2)
+    cz, en = np.linspace(-1, 1, 33), earth.log_energy_grid(29)
+    nb = 5
+    w = rng.uniform(0.2, 1.0, (2, 3, len(en), len(cz), nb))
+    w /= w.sum(axis=-1, keepdims=True)
+    edges = np.array([8.0, 12.0, 17.0, 24.0, 33.0, 45.0])
+    m = earth.gaussian_sets(1, seed=40)[0]
+    mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+    if poly:
+        r, a, b, c, ye = earth.PREM_4LAYER_QUAD_V2
+        rho, abc = None, (a, b, c)
+    else:
+        r, rho, ye = earth.PREM_4LAYER
+        abc = None
+    for anti, knu in ((False, 1), (True, -1)):
+        ref = oracle.atmos(OMix(*mix6[:4], mix6[4], mix6[5], knu), anti, cz, en, r, rho, ye, 20.0,
+                           poly_abc=abc, avg=(nb, w.ravel(), edges))
+        got = run_avg("fp64", mix6, knu, anti, cz, en, r, rho, ye, 20.0, nb, w.ravel(), edges, abc)
+        assert np.abs(got - ref).max() <= 1e-12
+
+
+def test_averaging_on_mixed_handle_is_refused():
+    p = AtmosCudaPropagatorSingle(0, 3, 2, precision="mixed")
+    p.setEnergyList([1.0, 2.0])
+    p.setCosineList([-0.5, 0.0, 0.5])
+    p.setMNSMatrix(0.5, 0.1, 0.7, 0.0, 1)
+    p.setNeutrinoMasses(7.5e-5, 2.5e-3)
+    p.setDensity(*earth.PREM_4LAYER)
+    p.setProductionHeight(20.0)
+    p.SetNumberOfProductionHeightBinsForAveraging(1)
+    p.setProductionHeightList(np.ones(2 * 3 * 2 * 3), [15.0, 25.0])
+    with pytest.raises(RuntimeError, match="FP64"):
+        p.calculateProbabilities(0)

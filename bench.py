@@ -455,14 +455,20 @@ def run_ours(args, rank, world):
     cz_pinned = (torch.from_numpy(np.asarray(w["cz"], dtype=np.float64)).pin_memory()
                  if w["kind"] == "atmos" else None)
 
+    # neutrino and antineutrino on their own streams: one type's download overlaps the other's
+    # compute
+    e2e_streams = [torch.cuda.Stream() for _ in props]
+
     def e2e_step():
         for t, p in enumerate(props):
             p.setEnergyList(en_pinned.numpy())
             if cz_pinned is not None:
                 p.setCosineList(cz_pinned.numpy())
-            p.calculate_async(t, sptr)
-            p.copy_result_async(host_out[t].data_ptr(), sptr)
-        stream.synchronize()
+            sp = e2e_streams[t].cuda_stream
+            p.calculate_async(t, sp)
+            p.copy_result_async(host_out[t].data_ptr(), sp)
+        for st in e2e_streams:
+            st.synchronize()
 
     for _ in range(max(1, args.warmup)):
         e2e_step()

@@ -408,9 +408,13 @@ int cp3_set_cosines(cp3_propagator* h, const double* cosines, int n) {
             if (count_shells(h->model, cosines[i]) > kMaxShells)
                 return fail(h, CP3_ERR_LAYER_LIMIT, "setMaxlayers : invalid number of maxLayer");
     }
-    h->cosines.assign(cosines, cosines + n);
+    // An unchanged list keeps the trajectories (the reference re-derives them every time; the
+    // result is the same).
+    if (!h->cosines_set || std::memcmp(h->cosines.data(), cosines, sizeof(double) * n) != 0) {
+        h->cosines.assign(cosines, cosines + n);
+        h->traj_dirty = true;
+    }
     h->cosines_set = true;
-    h->traj_dirty = true;
     return CP3_OK;
 }
 

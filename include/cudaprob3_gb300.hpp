@@ -21,6 +21,20 @@ namespace cudaprob3linear {
 enum ProbType : int { e_e = 0, e_m = 1, e_t = 2, m_e = 3, m_m = 4, m_t = 5, t_e = 6, t_m = 7, t_t = 8 };
 enum NeutrinoType { Neutrino, Antineutrino };
 
+// Constants<FLOAT_T> (constants.hpp:24-50): same values; the crossed-shell limit is the
+// runtime CP3_MAX_SHELLS instead of the reference's compile-time 10.
+template <typename FLOAT_T>
+struct Constants {
+    static constexpr FLOAT_T tworttwoGf() { return 1.52588e-4; }
+    static constexpr FLOAT_T km2cm() { return 1.0e5; }
+    static constexpr FLOAT_T REarth() { return 6371.0; }
+    static constexpr FLOAT_T REarthcm() { return REarth() * km2cm(); }
+    static constexpr FLOAT_T density_convert() { return 0.5; }
+    static constexpr int MaxProdHeightBins() { return 20; }
+    static constexpr int MaxNLayers() { return CP3_MAX_SHELLS; }
+    static constexpr FLOAT_T Epsilon() { return 1e-6; }
+};
+
 namespace detail {
 inline void check(int rc, const cp3_propagator* h) {
     if (rc != CP3_OK) throw std::runtime_error(cp3_last_error(h));

@@ -58,3 +58,23 @@ def test_facade_matches_oracle(tmp_path, oracle):
                 assert abs(v - refb[ie, t]) <= 1e-12
                 n += 1
         assert n > 100
+
+
+def test_cmake_package_and_compat_headers(tmp_path):
+    """find_package(CUDAProb3) gives the reference's target names; its header names resolve."""
+    import shutil
+    if not shutil.which("cmake"):
+        pytest.skip("cmake not installed")
+    from cudaprob3_gb300 import build
+    build.build()
+    src = os.path.join(ROOT, "tests", "cpp", "cmake_consumer")
+    bld = str(tmp_path / "b")
+    r = subprocess.run(["cmake", "-S", src, "-B", bld, f"-DCP3_ROOT={ROOT}"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run(["cmake", "--build", bld], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = subprocess.run([os.path.join(bld, "consumer")], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0
+    assert "REarth 6371" in out.stdout
+    assert ("created" in out.stdout) or ("No GPU found" in out.stdout)

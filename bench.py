@@ -33,6 +33,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_TYPES = 2  # neutrino + antineutrino per step
+BATCH_SETS = 0  # --batch-sets: fewer parameter sets for the batched workloads (profiling)
 
 
 def f_bin(M):
@@ -60,15 +61,16 @@ def workload(name):
         return dict(kind="beam", en=earth.lin_energy_grid(100000), rho=2.6, L=1300.0,
                     desc="beam, rho=2.6 g/cm^3, L=1300 km, 1e5 E (0.1-10 GeV), nu+nubar")
     if name == "batch_atmos":
-        sets = earth.gaussian_sets(256, seed=2024)
-        grids = earth.uneven_grids(256, seed=2025)
+        n = BATCH_SETS or 256
+        sets = earth.gaussian_sets(n, seed=2024)
+        grids = earth.uneven_grids(n, seed=2025)
         return dict(kind="batch", model=earth.PREM_12LAYER, h=22.0, sets=sets, grids=grids,
                     beam=None,
                     desc="batched atmospheric: 256 Gaussian parameter sets (half inverted "
                          "ordering), own grids n_cos U[100,1000] x n_E U[100,2000], PREM "
                          "12-layer, h=22 km, nu+nubar (512 problems), one persistent launch")
     if name == "batch_beam":
-        sets = earth.gaussian_sets(4096, seed=2026)
+        sets = earth.gaussian_sets(BATCH_SETS or 4096, seed=2026)
         return dict(kind="batch", model=None, h=None, sets=sets, grids=None,
                     beam=dict(en=earth.lin_energy_grid(100000), rho=2.6, L=[295.0, 1300.0]),
                     desc="batched beam: 4096 Gaussian parameter sets (half inverted ordering), "
@@ -657,8 +659,12 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=2.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-sets", type=int, default=0,
+                    help="parameter sets of the batched workloads (default: the configuration's)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global BATCH_SETS
+    BATCH_SETS = args.batch_sets
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

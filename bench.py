@@ -23,6 +23,7 @@ import ctypes as C
 import json
 import os
 import statistics
+import tempfile
 import subprocess
 import sys
 import time
@@ -214,7 +215,9 @@ class Clocks:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+        # raw samples: $CP3_CLOCKS_DIR if set (kept), else a temporary directory
+        d = os.environ.get("CP3_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"clocks_gpu{gpu_index}.csv")
 
     def __enter__(self):
         try:
@@ -261,10 +264,13 @@ def fma_peaks(device):
     L.cp3peaks_fma_tflops.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]
     out = {}
-    for name, fp64, iters in (("fp32", 0, 8192), ("fp64", 1, 512)):
+    for name, mode, iters in (("fp32_scalar", 0, 8192), ("fp32_paired", 2, 4096), ("fp64", 1, 512)):
         t, ms = C.c_double(), C.c_double()
-        rc = L.cp3peaks_fma_tflops(fp64, device, iters, C.byref(t), C.byref(ms))
+        rc = L.cp3peaks_fma_tflops(mode, device, iters, C.byref(t), C.byref(ms))
         out[name] = t.value if rc == 0 else None
+    # The FP32 roofline is the faster of scalar and paired (two FMAs per instruction) FMA.
+    fp32 = [v for v in (out["fp32_scalar"], out["fp32_paired"]) if v]
+    out["fp32"] = max(fp32) if fp32 else None
     return out
 
 
@@ -290,7 +296,7 @@ def set_params(p, m, knu):
 
 
 def run_serve(args, rank, world):
-    """64 closed-loop chains (each waits for its result, then thinks for an
+    """Serving workload: 64 closed-loop chains (each waits for its result, then thinks for an
     exponential time and submits again) over request sizes {atm 200^2, 500^2, 2000^2; beam
     1e4, 1e5}; the think time is swept down to zero (saturation)."""
     import threading

@@ -74,6 +74,7 @@ struct cp3_propagator {
     int ncls_used = 0;
 
     DevBuf<double> d_energies;
+    DevBuf<float2> d_energies_df, d_cls_rho_df;  // mixed kernels: (hi, lo) pairs split here
     DevBuf<int> d_seg_off, d_seg_cls;
     DevBuf<double> d_seg_len, d_cls_rho, d_seg_rho;
     DevBuf<double> d_ph_prob, d_ph_shift, d_air_cm;  // production-height averaging
@@ -102,6 +103,16 @@ struct cp3_propagator {
 };
 
 namespace {
+
+// x[i] as float pairs (hi, lo), hi + lo = x[i] to ~48 bits (the device's df_from, done once).
+std::vector<float2> split_pairs(const double* x, size_t n) {
+    std::vector<float2> out(n);
+    for (size_t i = 0; i < n; i++) {
+        const float h = (float)x[i];
+        out[i] = make_float2(h, (float)(x[i] - (double)h));
+    }
+    return out;
+}
 
 int fail(cp3_propagator* h, int code, const std::string& msg) {
     if (h)
@@ -157,6 +168,7 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
     if ((e = cudaSetDevice(device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = h->d_energies.reserve(ne)) != cudaSuccess ||
+        (precision == CP3_MIXED && (e = h->d_energies_df.reserve(ne)) != cudaSuccess) ||
         (e = h->d_result.reserve(h->result_bytes)) != cudaSuccess) {
         cudaGetLastError();
         const std::string msg = std::string("propagator creation failed: ") + cudaGetErrorString(e);
@@ -186,11 +198,7 @@ int prepare_atmos(cp3_propagator* h) {
         CP3_CUDA(h, cudaMemcpy(h->d_seg_len.ptr, t.len_km.data(), sizeof(double) * nseg,
                                cudaMemcpyHostToDevice), "upload trajectories");
     } else {
-        std::vector<float2> df(nseg);
-        for (size_t i = 0; i < nseg; i++) {
-            const float hi = (float)t.len_km[i];
-            df[i] = make_float2(hi, (float)(t.len_km[i] - (double)hi));
-        }
+        const std::vector<float2> df = split_pairs(t.len_km.data(), nseg);
         CP3_CUDA(h, h->d_seg_len_df.reserve(nseg), "allocate trajectories");
         CP3_CUDA(h, cudaMemcpy(h->d_seg_len_df.ptr, df.data(), sizeof(float2) * nseg,
                                cudaMemcpyHostToDevice), "upload trajectories");
@@ -209,6 +217,12 @@ int prepare_atmos(cp3_propagator* h) {
     CP3_CUDA(h, h->d_cls_rho.reserve(cls_rho.size()), "allocate classes");
     CP3_CUDA(h, cudaMemcpy(h->d_cls_rho.ptr, cls_rho.data(), sizeof(double) * cls_rho.size(),
                            cudaMemcpyHostToDevice), "upload classes");
+    if (h->precision == CP3_MIXED) {
+        const std::vector<float2> pairs = split_pairs(cls_rho.data(), cls_rho.size());
+        CP3_CUDA(h, h->d_cls_rho_df.reserve(pairs.size()), "allocate classes");
+        CP3_CUDA(h, cudaMemcpy(h->d_cls_rho_df.ptr, pairs.data(), sizeof(float2) * pairs.size(),
+                               cudaMemcpyHostToDevice), "upload classes");
+    }
     const size_t cells = (size_t)h->ncls_used * pad_energies(h->ne);
     if (h->precision == CP3_FP64)
         CP3_CUDA(h, h->d_table64.reserve(cells * kF64Fields), "allocate eigen table");
@@ -290,8 +304,8 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
                                      h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
                                      av, (double*)h->d_result.ptr, s);
         } else {
-            e = launch_table_mixed(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
-                                   h->d_table32.ptr, s);
+            e = launch_table_mixed(p, h->d_energies_df.ptr, h->ne, h->d_cls_rho_df.ptr,
+                                   h->ncls_used, h->d_table32.ptr, s);
             mark(1);
             if (e == cudaSuccess)
                 e = launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
@@ -310,7 +324,7 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
             e = launch_beam_f64(p, h->d_energies.ptr, h->ne, rho_e, h->beam_L,
                                 (double*)h->d_result.ptr, s);
         else
-            e = launch_beam_mixed(p, h->d_energies.ptr, h->ne, rho_e, h->beam_L,
+            e = launch_beam_mixed(p, h->d_energies_df.ptr, h->ne, rho_e, h->beam_L,
                                   (float*)h->d_result.ptr, s);
         mark(2);
         h->timed_table = false;
@@ -393,6 +407,11 @@ int cp3_set_energies(cp3_propagator* h, const double* energies, int n) {
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     CP3_CUDA(h, cudaMemcpy(h->d_energies.ptr, energies, sizeof(double) * n, cudaMemcpyHostToDevice),
              "upload energies");
+    if (h->precision == CP3_MIXED) {
+        const std::vector<float2> pairs = split_pairs(energies, (size_t)n);
+        CP3_CUDA(h, cudaMemcpy(h->d_energies_df.ptr, pairs.data(), sizeof(float2) * n,
+                               cudaMemcpyHostToDevice), "upload energies");
+    }
     h->energies_set = true;
     return CP3_OK;
 }

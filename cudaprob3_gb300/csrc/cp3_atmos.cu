@@ -338,11 +338,11 @@ __global__ void __launch_bounds__(kBlock)
 // (rotated_eigen_mixed), double-float phase, FP32 matrix work.
 __global__ void __launch_bounds__(kBlock)
     beam_mixed_kernel(const __grid_constant__ OscParams p, WParams w,
-                      const double* __restrict__ energies, int ne, double rho_e, float2 L,
+                      const float2* __restrict__ energies, int ne, float2 rho_e, float2 L,
                       float* __restrict__ out) {
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    beam_bin_mixed(&p, w, energies[ie], rho_e, &L, 1, out + ie, (size_t)ne, 0);
+    beam_bin_mixed(&p, w, to_df(energies[ie]), to_df(rho_e), &L, 1, out + ie, (size_t)ne, 0);
 }
 
 }  // namespace
@@ -399,13 +399,14 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
     return cudaGetLastError();
 }
 
-cudaError_t launch_beam_mixed(const OscParams& p, const double* energies, int ne, double rho_e,
+cudaError_t launch_beam_mixed(const OscParams& p, const float2* energies, int ne, double rho_e,
                               double L_km, float* out, cudaStream_t s) {
     if (ne <= 0) return cudaSuccess;
-    const float Lh = (float)L_km;
+    const float Lh = (float)L_km, rh = (float)rho_e;
     const float2 L = make_float2(Lh, (float)(L_km - (double)Lh));
+    const float2 rho2 = make_float2(rh, (float)(rho_e - (double)rh));
     beam_mixed_kernel<<<(ne + kBlock - 1) / kBlock, kBlock, 0, s>>>(p, wparams(p), energies, ne,
-                                                                    rho_e, L, out);
+                                                                    rho2, L, out);
     return cudaGetLastError();
 }
 

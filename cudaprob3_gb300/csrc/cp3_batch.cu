@@ -5,17 +5,17 @@
 // and one or more baselines), each with its own oscillation parameters and neutrino type.
 // One run is one launch of a persistent kernel, captured once in a CUDA graph:
 //
-//   * the grid is (SMs x resident blocks); every block pulls tiles from one atomic counter;
+//   * the grid is (SMs x resident blocks); every warp pulls tiles from one atomic counter;
 //   * tiles [0, A) build the per-(class, energy) eigen tables of the atmospheric problems,
-//     tiles [A, A+B) compute bins: atmospheric tiles are R cosine rows x 128 energies, beam
-//     tiles are 128 R x beam_chunk energies with every baseline of the problem;
+//     tiles [A, A+B) compute bins: atmospheric tiles are rows_per_tile cosine rows x 32
+//     energies, beam tiles are 32 x beam_chunk energies with every baseline of the problem;
 //   * an atmospheric bin tile first waits until its own problem's table tiles are done.
-//     Those tiles were handed out before it by the same counter, so the blocks holding them
+//     Those tiles were handed out before it by the same counter, so the warps holding them
 //     are running and the wait ends; it is bounded all the same (status flag on time-out);
 //   * everything a run needs -- descriptors, tile prefix sums, parameters -- is in device
 //     memory, so the captured graph replays unchanged while parameters change between runs.
 //
-// The tile shape (R, blocks per SM, beam_chunk) does not change any bin's arithmetic:
+// The tile shape (rows_per_tile, blocks per SM, beam_chunk) does not change any bin's arithmetic:
 // results are bit-identical across shapes, which lets an autotuner pick it by timing alone.
 #include <cuda_runtime.h>
 
@@ -93,18 +93,17 @@ struct cp3_batch {
     long long total_bins = 0;
 
     Buf<Problem> d_probs;
-    Buf<long long> d_astart, d_bstart;
+    Buf<int> d_astart, d_bstart;
     Buf<Header> d_hdr;
     Buf<OscParams> d_params;
-    Buf<double> d_energies, d_cls_rho;
     Buf<int> d_row_off, d_seg_cls, d_done, d_status;
-    Buf<float2> d_seg_len, d_baselines;
+    Buf<float2> d_energies, d_cls_rho, d_seg_len, d_baselines;
     Buf<float> d_tables, d_out;
-    Buf<unsigned long long> d_counter;
+    Buf<unsigned int> d_counter;
     OscParams* h_params = nullptr;  // pinned staging
     bool params_dirty = true;
 
-    int R = 1, blocks_per_sm = 0, beam_chunk = 4;
+    int rows_per_tile = 2, blocks_per_sm = 0, beam_chunk = 4;
     long long total_a = 0, total_b = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev_params = nullptr, ev0 = nullptr, ev1 = nullptr;
@@ -145,10 +144,8 @@ int bcuda(cp3_batch* b, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return bcuda(b, e_, where);      \
     } while (0)
 
-int occupancy(int R, int* blocks) {
-    cudaError_t e = R == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batch_kernel<1>, 128, 0)
-                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batch_kernel<2>, 256, 0);
-    return e == cudaSuccess ? 0 : 1;
+int occupancy(int* blocks) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batch_kernel, kBlock, 0) == cudaSuccess ? 0 : 1;
 }
 
 // Tile counts for the current shape, the device header and the graph.
@@ -156,27 +153,24 @@ int configure(cp3_batch* b) {
     const int n = (int)b->probs.size();
     std::vector<long long> a(n + 1, 0), bb(n + 1, 0);
     for (int p = 0; p < n; p++) {
-        const Problem& P = b->probs[p];
-        const long long nchunk = (P.ne + kTileE - 1) / kTileE;
-        if (P.kind == 0) {
-            a[p + 1] = a[p] + nchunk * ((P.ncls + b->R - 1) / b->R);
-            bb[p + 1] = bb[p] + nchunk * ((P.nrows + b->R - 1) / b->R);
-        } else {
-            a[p + 1] = a[p];
-            const long long per = 128LL * b->R * b->beam_chunk;
-            bb[p + 1] = bb[p] + (P.ne + per - 1) / per;
-        }
+        long long na = 0, nb = 0;
+        problem_tiles(b->probs[p], b->rows_per_tile, b->beam_chunk, &na, &nb);
+        a[p + 1] = a[p] + na;
+        bb[p + 1] = bb[p] + nb;
     }
+    if (a[n] + bb[n] > kMaxTiles)
+        return bfail(b, CP3_ERR_BAD_SIZE, "batch too large for one launch: split it or use larger tiles");
     b->total_a = a[n];
     b->total_b = bb[n];
-    Header h{n, b->beam_chunk, a[n], bb[n]};
-    B_CUDA(b, cudaMemcpyAsync(b->d_astart.ptr, a.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
-    B_CUDA(b, cudaMemcpyAsync(b->d_bstart.ptr, bb.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
+    const std::vector<int> ai(a.begin(), a.end()), bi(bb.begin(), bb.end());
+    Header h{n, b->rows_per_tile, b->beam_chunk, (int)a[n], (int)bb[n]};
+    B_CUDA(b, cudaMemcpyAsync(b->d_astart.ptr, ai.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
+    B_CUDA(b, cudaMemcpyAsync(b->d_bstart.ptr, bi.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
     B_CUDA(b, cudaMemcpyAsync(b->d_hdr.ptr, &h, sizeof(Header), cudaMemcpyHostToDevice, b->stream), "upload header");
     B_CUDA(b, cudaStreamSynchronize(b->stream), "configure");
 
     int occ = 0;
-    if (occupancy(b->R, &occ) || occ < 1) return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
+    if (occupancy(&occ) || occ < 1) return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
     const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, occ) : occ;
     const int grid = std::max(1, b->sms * bps);
     Args args{b->d_hdr.ptr, b->d_probs.ptr, b->d_astart.ptr, b->d_bstart.ptr, b->d_params.ptr,
@@ -191,14 +185,11 @@ int configure(cp3_batch* b) {
     B_CUDA(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
     cudaGraph_t g;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter.ptr, 0, sizeof(unsigned long long), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter.ptr, 0, sizeof(unsigned int), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_done.ptr, 0, sizeof(int) * std::max(n, 1), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_status.ptr, 0, sizeof(int), cs);
     if (e == cudaSuccess) {
-        if (b->R == 1)
-            batch_kernel<1><<<grid, 128, 0, cs>>>(args);
-        else
-            batch_kernel<2><<<grid, 256, 0, cs>>>(args);
+        batch_kernel<<<grid, kBlock, 0, cs>>>(args);
         e = cudaGetLastError();
     }
     const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
@@ -213,9 +204,8 @@ int configure(cp3_batch* b) {
 int commit(cp3_batch* b) {
     const int n = (int)b->hp.size();
     if (n == 0) return bfail(b, CP3_ERR_NOT_SET, "the batch has no problems");
-    std::vector<double> energies, cls_rho;
     std::vector<int> row_off, seg_cls;
-    std::vector<float2> seg_len, baselines;
+    std::vector<float2> energies, cls_rho, seg_len, baselines;
     b->probs.assign(n, Problem{});
     b->out_off.assign(n, 0);
     size_t tab = 0, out = 0;
@@ -233,7 +223,7 @@ int commit(cp3_batch* b) {
         P.ne_pad = pad_energies(P.ne);
         P.param = p;
         P.e_off = (long long)energies.size();
-        energies.insert(energies.end(), H.en.begin(), H.en.end());
+        for (double x : H.en) energies.push_back(split(x));
         if (H.kind == 0) {
             if (!b->model_set) return bfail(b, CP3_ERR_NOT_SET, "atmospheric problems need cp3_batch_set_earth first");
             TrajectoryTable t;
@@ -250,8 +240,8 @@ int commit(cp3_batch* b) {
                 seg_cls.push_back(t.cls[i]);
             }
             P.cls_off = (long long)cls_rho.size();
-            cls_rho.push_back(0.0);
-            for (int c = 1; c < P.ncls; c++) cls_rho.push_back(b->model.rho[c - 1] * b->model.ye[c - 1]);
+            cls_rho.push_back(split(0.0));
+            for (int c = 1; c < P.ncls; c++) cls_rho.push_back(split(b->model.rho[c - 1] * b->model.ye[c - 1]));
             P.tab_off = (long long)tab;
             tab += align_up((size_t)P.ncls * P.ne_pad * kMixFields, 64);
             P.out_off = (long long)out;
@@ -261,7 +251,9 @@ int commit(cp3_batch* b) {
             P.nrows = (int)H.L.size();
             P.row_off = (long long)baselines.size();
             for (double L : H.L) baselines.push_back(split(L));
-            P.rho_e = H.rho * kDensityConvert;
+            const float2 r = split(H.rho * kDensityConvert);
+            P.rho_e[0] = r.x;
+            P.rho_e[1] = r.y;
             P.out_off = (long long)out;
             out += align_up((size_t)9 * P.nrows * P.ne, 32);
             b->total_bins += (long long)P.nrows * P.ne;
@@ -334,7 +326,8 @@ std::string tune_key(cp3_batch* b) {
     const int lg = (int)std::log2((double)std::max<long long>(1, b->total_bins));
     std::string name(prop.name);
     std::replace(name.begin(), name.end(), ' ', '_');
-    return name + ":a" + std::to_string(na > 0) + "b" + std::to_string(nb > 0) + ":bins2^" + std::to_string(lg);
+    // "w32": shapes of the warp-tiled kernel (entries of other kernels are never matched)
+    return "w32:" + name + ":a" + std::to_string(na > 0) + "b" + std::to_string(nb > 0) + ":bins2^" + std::to_string(lg);
 }
 
 }  // namespace
@@ -455,9 +448,10 @@ int cp3_batch_commit(cp3_batch* b) {
 
 int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int beam_chunk) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
-    if ((rows_per_tile != 1 && rows_per_tile != 2) || blocks_per_sm < 0 || beam_chunk < 1 || beam_chunk > 64)
-        return bfail(b, CP3_ERR_BAD_ARGUMENT, "shape: rows_per_tile 1|2, blocks_per_sm >= 0, beam_chunk 1..64");
-    b->R = rows_per_tile;
+    if (rows_per_tile < 1 || rows_per_tile > kMaxRowsPerTile || blocks_per_sm < 0 || beam_chunk < 1 ||
+        beam_chunk > kMaxBeamChunk)
+        return bfail(b, CP3_ERR_BAD_ARGUMENT, "shape: rows_per_tile 1..16, blocks_per_sm >= 0, beam_chunk 1..64");
+    b->rows_per_tile = rows_per_tile;
     b->blocks_per_sm = blocks_per_sm;
     b->beam_chunk = beam_chunk;
     if (!b->committed) return CP3_OK;
@@ -467,7 +461,7 @@ int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int 
 
 int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_sm, int* beam_chunk) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
-    if (rows_per_tile) *rows_per_tile = b->R;
+    if (rows_per_tile) *rows_per_tile = b->rows_per_tile;
     if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
     if (beam_chunk) *beam_chunk = b->beam_chunk;
     return CP3_OK;
@@ -504,22 +498,26 @@ int cp3_batch_tune(cp3_batch* b, int use_cache) {
         while (f >> k >> R >> bps >> bc)
             if (k == key) return cp3_batch_set_shape(b, R, bps, bc);
     }
-    int occ1 = 0, occ2 = 0;
-    occupancy(1, &occ1);
-    occupancy(2, &occ2);
+    int occ = 0;
+    occupancy(&occ);
+    bool has_a = false, has_b = false;
+    for (const Problem& P : b->probs) (P.kind == 0 ? has_a : has_b) = true;
     struct Shape {
-        int R, bps, bc;
+        int rows, bps, bc;
     };
+    // Only the dimensions the batch's problem kinds use are swept.
+    std::vector<int> rows = has_a ? std::vector<int>{1, 2, 4, 8} : std::vector<int>{2};
+    std::vector<int> chunks = has_b ? std::vector<int>{1, 4, 16} : std::vector<int>{4};
+    std::vector<int> bps = {0};
+    if (occ > 1) bps.push_back(std::max(1, occ / 2));
     std::vector<Shape> cand;
-    for (int bc : {1, 4, 16}) {
-        cand.push_back({1, 0, bc});
-        cand.push_back({2, 0, bc});
-        if (occ1 > 1) cand.push_back({1, std::max(1, occ1 / 2), bc});
-    }
+    for (int r : rows)
+        for (int bc : chunks)
+            for (int k : bps) cand.push_back({r, k, bc});
     double best = 1e30;
     Shape pick = cand[0];
     for (const Shape& s : cand) {
-        int rc = cp3_batch_set_shape(b, s.R, s.bps, s.bc);
+        int rc = cp3_batch_set_shape(b, s.rows, s.bps, s.bc);
         if (rc) return rc;
         double total = 0;
         for (int it = 0; it < 4; it++) {
@@ -534,11 +532,11 @@ int cp3_batch_tune(cp3_batch* b, int use_cache) {
             pick = s;
         }
     }
-    int rc = cp3_batch_set_shape(b, pick.R, pick.bps, pick.bc);
+    int rc = cp3_batch_set_shape(b, pick.rows, pick.bps, pick.bc);
     if (rc) return rc;
     if (use_cache) {
         std::ofstream f(path, std::ios::app);
-        if (f) f << key << " " << pick.R << " " << pick.bps << " " << pick.bc << "\n";
+        if (f) f << key << " " << pick.rows << " " << pick.bps << " " << pick.bc << "\n";
     }
     return CP3_OK;
 }

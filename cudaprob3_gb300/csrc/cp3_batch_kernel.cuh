@@ -1,5 +1,14 @@
 // cp3_batch_kernel.cuh -- the persistent many-problem kernel, shared by batches
 // (cp3_batch.cu) and the serving loop (cp3_serve.cu).  See cp3_batch.cu for the design.
+//
+// Scheduling is per warp, not per block: every warp pulls its own tiles from the shared
+// counter (the next tile's index is fetched while the current one runs) and never waits at a
+// block barrier.  A tile is 32 energies, one per lane:
+//   * table tile:        one density class of one atmospheric problem;
+//   * atmospheric tile:  rows_per_tile cosine rows, walked one after the other;
+//   * beam tile:         beam_chunk consecutive groups of 32 energies, every baseline.
+// Each warp stages the trajectory it is walking (segment lengths and classes) in its own
+// slice of shared memory; warps synchronise only with themselves (__syncwarp).
 #pragma once
 
 #include "cp3_mixed.cuh"
@@ -7,8 +16,14 @@
 namespace cp3 {
 namespace batchk {
 
-constexpr int kTileE = 128;             // energies per atmospheric tile row
+constexpr int kTileE = 32;                  // energies per tile (one per lane)
+constexpr int kBlock = 128;                 // threads per block (4 independent warps)
+constexpr int kMaxRowsPerTile = 16;
+constexpr int kMaxBeamChunk = 64;
 constexpr long long kSpinLimit = 20000000;  // ~seconds with the nanosleep back-off
+// Tile indices are 32-bit: a launch holds fewer tiles than this (every warp also takes one
+// index past the end).  At 32 bins per tile that is far more output than device memory.
+constexpr long long kMaxTiles = (1LL << 31) - (1LL << 24);
 
 struct Problem {
     int kind;          // 0 atmospheric, 1 beam
@@ -16,42 +31,58 @@ struct Problem {
     int nrows;         // atmospheric: cosines; beam: baselines
     int ncls;          // atmospheric: density classes
     int param;         // index into the parameter arena
-    long long e_off;   // energies arena (doubles)
+    long long e_off;   // energies arena
     long long row_off; // atmospheric: first of nrows + 1 row offsets; beam: first baseline
     long long cls_off; // atmospheric: first class density
     long long tab_off; // atmospheric: float offset of the table [ncls][ne_pad][16]
     long long out_off; // float offset of the result
-    double rho_e;      // beam: electron density (rho * 0.5)
+    float rho_e[2];    // beam: electron density (rho * 0.5) as a float pair (hi, lo)
 };
 
 struct Header {
     int nprob;
+    int rows_per_tile;
     int beam_chunk;
-    long long total_a, total_b;
+    int total_a, total_b;  // table tiles, bin tiles
 };
 
 struct Args {
     const Header* hdr;
     const Problem* probs;
-    const long long* a_start;  // nprob + 1 (table tiles)
-    const long long* b_start;  // nprob + 1 (bin tiles)
+    const int* a_start;        // nprob + 1 (table tiles)
+    const int* b_start;        // nprob + 1 (bin tiles)
     const OscParams* params;
-    const double* energies;
+    const float2* energies;    // float pairs (hi, lo) of the energies
     const int* row_off;
     const float2* seg_len;
     const int* seg_cls;
-    const double* cls_rho;
+    const float2* cls_rho;     // float pairs of the class densities rho * Ye
     const float2* baselines;
     float* tables;
     float* out;
     int* done_a;
-    unsigned long long* counter;
+    unsigned int* counter;
     int* status;
 };
 
-// Largest p with prefix[p] <= t (prefix[n] = total > t); skips empty ranges.
-__device__ __forceinline__ int find_problem(const long long* __restrict__ prefix, int n, long long t) {
-    int lo = 0, hi = n;  // invariant: prefix[lo] <= t < prefix[hi]
+// Table and bin tiles of one problem for a tile shape.
+CP3_HD void problem_tiles(const Problem& P, int rows_per_tile, int beam_chunk, long long* na,
+                          long long* nb) {
+    const long long nchunk = (P.ne + kTileE - 1) / kTileE;
+    if (P.kind == 0) {
+        *na = nchunk * P.ncls;
+        *nb = nchunk * ((P.nrows + rows_per_tile - 1) / rows_per_tile);
+    } else {
+        const long long per = (long long)kTileE * beam_chunk;
+        *na = 0;
+        *nb = (P.ne + per - 1) / per;
+    }
+}
+
+// Largest p in [lo, n) with prefix[p] <= t, given prefix[lo] <= t < prefix[n]; skips empty
+// ranges.
+__device__ __forceinline__ int find_problem(const int* __restrict__ prefix, int lo, int n, int t) {
+    int hi = n;
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(prefix + mid) <= t)
@@ -62,36 +93,51 @@ __device__ __forceinline__ int find_problem(const long long* __restrict__ prefix
     return lo;
 }
 
-template <int R>
-// 64 registers per thread (the budget of the standalone per-bin kernel): 8 blocks of 128
-// or 4 of 256 threads per SM.
-__global__ void __launch_bounds__(128 * R, 8 / R) batch_kernel(const Args a) {
-    constexpr int T = 128 * R;
-    __shared__ long long s_tile;
-    __shared__ float2 s_len[R][kMaxSegments];
-    __shared__ int s_cls[R][kMaxSegments];
-    const int r = threadIdx.x >> 7;
-    const int lane = threadIdx.x & 127;
+// 64 registers per thread (the budget of the standalone per-bin kernel): 8 blocks per SM.
+// Internal linkage: each translation unit that launches it (batches, the server) has its own.
+static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
+    constexpr int kWarps = kBlock / 32;
+    __shared__ float2 s_len[kWarps][kMaxSegments];  // one trajectory per warp
+    __shared__ int s_cls[kWarps][kMaxSegments];
+    const unsigned lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
     const Header hdr = *a.hdr;
-    const long long total = hdr.total_a + hdr.total_b;
-    for (;;) {
-        __syncthreads();  // previous tile finished with the shared staging
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(a.counter, 1ULL);
-        __syncthreads();
-        const long long t = s_tile;
-        if (t >= total) return;
-        if (t < hdr.total_a) {
-            // ---- eigen-table tile: R classes x 128 energies of one atmospheric problem ----
-            const int p = find_problem(a.a_start, hdr.nprob, t);
-            const Problem P = a.probs[p];
-            const long long local = t - a.a_start[p];
+    const int total = hdr.total_a + hdr.total_b;
+
+    // The warp's current problem: tiles arrive in increasing order, so a warp's problems do
+    // too and the lookup resumes from the last one.  The descriptor itself is re-read per
+    // tile (a broadcast load that hits L1), which keeps registers free for the bins.
+    int p = 0, phase = -1, ready = -1, p_lo = 0, p_hi = 0;
+
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(a.counter, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    while (t < total) {
+        int next = 0;
+        if (lane == 0) next = (int)atomicAdd(a.counter, 1u);  // in flight while this tile runs
+
+        const int ph = t < hdr.total_a ? 0 : 1;
+        const int tt = ph == 0 ? t : t - hdr.total_a;
+        if (ph != phase || tt >= p_hi) {
+            const int* pre = ph == 0 ? a.a_start : a.b_start;
+            p = find_problem(pre, ph == phase ? p : 0, hdr.nprob, tt);
+            p_lo = __ldg(pre + p);
+            p_hi = __ldg(pre + p + 1);
+            phase = ph;
+        }
+        const Problem P = a.probs[p];
+        const int local = tt - p_lo;
+        const OscParams* prm = a.params + P.param;
+
+        if (ph == 0) {
+            // ---- eigen-table tile: one class x 32 energies ----------------------------
             const int nchunk = (P.ne + kTileE - 1) / kTileE;
-            const int c = (int)(local / nchunk) * R + r;
-            const int e = (int)(local % nchunk) * kTileE + lane;
-            if (c < P.ncls && e < P.ne) {
+            const int c = local / nchunk;
+            const int e = (local % nchunk) * kTileE + (int)lane;
+            if (e < P.ne) {
                 float Pp[2][6], om[2][2];
-                rotated_eigen_mixed(a.params + P.param, a.energies[P.e_off + e],
-                                    a.cls_rho[P.cls_off + c], Pp, om);
+                const float2 E2 = a.energies[P.e_off + e], r2 = a.cls_rho[P.cls_off + c];
+                rotated_eigen_mixed(prm, df{E2.x, E2.y}, df{r2.x, r2.y}, Pp, om);
                 float4* d = reinterpret_cast<float4*>(a.tables + P.tab_off +
                                                       ((size_t)c * P.ne_pad + e) * kMixFields);
                 d[0] = make_float4(Pp[0][0], Pp[0][1], Pp[0][2], Pp[0][3]);
@@ -100,61 +146,67 @@ __global__ void __launch_bounds__(128 * R, 8 / R) batch_kernel(const Args a) {
                 d[3] = make_float4(om[0][0], om[0][1], om[1][0], om[1][1]);
             }
             __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0) atomicAdd(a.done_a + p, 1);
-            continue;
-        }
-        // ---- bin tile --------------------------------------------------------------------
-        const long long tb = t - hdr.total_a;
-        const int p = find_problem(a.b_start, hdr.nprob, tb);
-        const Problem P = a.probs[p];
-        const long long local = tb - a.b_start[p];
-        const OscParams* prm = a.params + P.param;
-        const WParams w{(float)prm->w[0], (float)prm->w[1], (float)prm->w[2], (float)prm->w[3]};
-        if (P.kind == 0) {
-            if (threadIdx.x == 0) {
-                const int need = (int)(a.a_start[p + 1] - a.a_start[p]);
-                const volatile int* done = a.done_a + p;
-                long long it = 0;
-                while (*done < need) {
-                    __nanosleep(256);
-                    if (++it > kSpinLimit) {
-                        atomicExch(a.status, 1);  // tables never completed: report, do not hang
-                        break;
+            __syncwarp();
+            if (lane == 0) atomicAdd(a.done_a + p, 1);
+        } else if (P.kind == 0) {
+            // ---- atmospheric bin tile: rows_per_tile rows x 32 energies ------------------
+            if (ready != p) {
+                // This problem's table tiles were all handed out before this tile, to warps
+                // that are running them, so the wait ends; it is bounded all the same.
+                if (lane == 0) {
+                    const int need = __ldg(a.a_start + p + 1) - __ldg(a.a_start + p);
+                    const volatile int* done = a.done_a + p;
+                    long long it = 0;
+                    while (*done < need) {
+                        __nanosleep(256);
+                        if (++it > kSpinLimit) {
+                            atomicExch(a.status, 1);  // tables never completed: report
+                            break;
+                        }
                     }
+                    __threadfence();
                 }
-                __threadfence();
+                __syncwarp();
+                ready = p;
             }
+            const WParams w = wparams(*prm);
             const int nchunk = (P.ne + kTileE - 1) / kTileE;
-            const int ic = (int)(local / nchunk) * R + r;
-            const int e = (int)(local % nchunk) * kTileE + lane;
-            int nseg = 0;
-            if (ic < P.nrows) {
-                const int s0 = a.row_off[P.row_off + ic];
-                nseg = a.row_off[P.row_off + ic + 1] - s0;
-                for (int i = lane; i < nseg; i += 128) {
-                    s_len[r][i] = a.seg_len[s0 + i];
-                    s_cls[r][i] = a.seg_cls[s0 + i];
+            const int ic0 = (local / nchunk) * hdr.rows_per_tile;
+            const int ic1 = min(ic0 + hdr.rows_per_tile, P.nrows);
+            const int e = (local % nchunk) * kTileE + (int)lane;
+            const int* ro = a.row_off + P.row_off;
+            for (int ic = ic0; ic < ic1; ic++) {
+                const int s0 = __ldg(ro + ic);
+                const int nseg = __ldg(ro + ic + 1) - s0;
+                __syncwarp();  // the previous row is done with the staging
+                for (int i = (int)lane; i < nseg; i += 32) {
+                    s_len[wid][i] = __ldg(a.seg_len + s0 + i);
+                    s_cls[wid][i] = __ldg(a.seg_cls + s0 + i);
                 }
-            }
-            __syncthreads();
-            if (ic < P.nrows && e < P.ne)
-                atmos_bin_mixed<true>(a.tables + P.tab_off + (size_t)e * kMixFields,
-                                      (size_t)kMixFields * P.ne_pad, s_len[r], s_cls[r], nseg - 1,
-                                      w, a.out + P.out_off + (size_t)ic * P.ne + e,
-                                      (size_t)P.nrows * P.ne);
-        } else {
-            const long long e0 = local * (long long)T * hdr.beam_chunk;
-            for (int k = 0; k < hdr.beam_chunk; k++) {
-                const long long e = e0 + (long long)k * T + threadIdx.x;
+                __syncwarp();
                 if (e < P.ne)
-                    beam_bin_mixed(prm, w, a.energies[P.e_off + e], P.rho_e, a.baselines + P.row_off,
-                                   P.nrows, a.out + P.out_off + e, (size_t)P.ne, (size_t)9 * P.ne);
+                    atmos_bin_mixed<true>(a.tables + P.tab_off + (size_t)e * kMixFields,
+                                          (size_t)kMixFields * P.ne_pad, s_len[wid], s_cls[wid],
+                                          nseg - 1, w, a.out + P.out_off + (size_t)ic * P.ne + e,
+                                          (size_t)P.nrows * P.ne);
+            }
+        } else {
+            // ---- beam tile: beam_chunk x 32 energies, every baseline --------------------
+            const WParams w = wparams(*prm);
+            const long long e0 = (long long)local * kTileE * hdr.beam_chunk;
+            const df rho{P.rho_e[0], P.rho_e[1]};
+            for (int k = 0; k < hdr.beam_chunk; k++) {
+                const long long e = e0 + (long long)k * kTileE + lane;
+                if (e < P.ne) {
+                    const float2 E2 = a.energies[P.e_off + e];
+                    beam_bin_mixed(prm, w, df{E2.x, E2.y}, rho, a.baselines + P.row_off, P.nrows,
+                                   a.out + P.out_off + e, (size_t)P.ne, (size_t)9 * P.ne);
+                }
             }
         }
+        t = __shfl_sync(0xffffffffu, next, 0);
     }
 }
-
 
 }  // namespace batchk
 }  // namespace cp3

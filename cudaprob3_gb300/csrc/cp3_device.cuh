@@ -384,6 +384,10 @@ CP3_HD df df_from(double x) {
     const float h = (float)x;
     return df{h, (float)(x - (double)h)};
 }
+#ifdef __CUDACC__
+CP3_HD df to_df(double x) { return df_from(x); }
+CP3_HD df to_df(float2 x) { return df{x.x, x.y}; }  // already split on the host
+#endif
 CP3_HD df df_fast2sum(float a, float b) {  // |a| >= |b|
     const float s = CP3_FADD(a, b);
     return df{s, CP3_FADD(b, -CP3_FADD(s, -a))};
@@ -423,12 +427,13 @@ CP3_HD df df_recip(df x) {
 //      omega_k = 2.534 (m_k - m_0) / E in df64 (hi, lo).
 // Where two refined roots lie closer than 1e-4 of the spread (exactly degenerate vacuum
 // masses, the reference's 5e-9 eV^2 degeneracy break) the FP64 reference cubic takes over.
-CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
-                                                    double rho, float P[2][6], float om[2][2]) {
+// E and rho arrive as float pairs (split once on the host), so the common path runs no FP64
+// instruction at all -- conversions included, which issue on the narrow FP64 pipe.
+CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed, df rhod, float P[2][6],
+                                float om[2][2]) {
     // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos
-    const df Ed = df_from(E);
     const df tw = df{1.52588e-4f, -7.040322e-12f};  // kTwoRtTwoGf = hi + lo
-    df V = df_mul(df_mul(tw, Ed), df_from(rho));
+    df V = df_mul(df_mul(tw, Ed), rhod);
     if (p->anti) V = df_neg(V);
     // det(l - H) = l^3 - c2 l^2 + c1 l - c0 with H = H0 + V e0 e0^T (OscParams::cpoly)
     const df c2 = df_add(df{p->cpolyf[0][0], p->cpolyf[0][1]}, V);
@@ -461,7 +466,7 @@ CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
     const float gap = fminf(fabsf(r[0].hi - r[1].hi), fminf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     if (!(gap > 1e-4f * spread)) {
         double Pd[2][6], omd[2];
-        rotated_eigen_f64(p, E, rho, Pd, omd);
+        rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
 #pragma unroll
         for (int k = 0; k < 2; k++) {
 #pragma unroll
@@ -506,6 +511,11 @@ CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
         om[kk][0] = w.hi;
         om[kk][1] = w.lo;
     }
+}
+
+CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E, double rho,
+                                float P[2][6], float om[2][2]) {
+    rotated_eigen_mixed(p, df_from(E), df_from(rho), P, om);
 }
 
 CP3_HD cf cmulf(cf a, cf b) {

@@ -121,6 +121,7 @@ void build_osc_params(const MixingInput& m, int antineutrino, OscParams* o) {
     o->w[1] = s23;
     o->w[2] = cd;
     o->w[3] = sd;
+    for (int k = 0; k < 4; k++) o->wf[k] = (float)o->w[k];
     o->anti = antineutrino ? 1 : 0;
 }
 

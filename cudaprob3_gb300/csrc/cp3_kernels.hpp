@@ -21,6 +21,9 @@ cudaError_t launch_table_f64(const OscParams& p, const double* energies, int ne,
                              const double* cls_rho, int ncls, double* table, cudaStream_t s);
 cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int ne,
                                const double* cls_rho, int ncls, float* table, cudaStream_t s);
+// The same from float pairs (hi, lo) split on the host: no FP64 instruction on the device.
+cudaError_t launch_table_mixed(const OscParams& p, const float2* energies, int ne,
+                               const float2* cls_rho, int ncls, float* table, cudaStream_t s);
 
 // Production-height averaging inputs of the FP64 kernels (n_bins == 0: fixed height).
 struct AvgArrays {
@@ -48,7 +51,7 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
 // Beam bins: rho_e = rho * 0.5 (electron density), L in km.
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,
                             double L_km, double* out, cudaStream_t s);
-cudaError_t launch_beam_mixed(const OscParams& p, const double* energies, int ne, double rho_e,
+cudaError_t launch_beam_mixed(const OscParams& p, const float2* energies, int ne, double rho_e,
                               double L_km, float* out, cudaStream_t s);
 
 }  // namespace cp3

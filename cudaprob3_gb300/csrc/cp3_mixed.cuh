@@ -170,8 +170,8 @@ struct WParams {
     float c, s, er, ei;
 };
 
-inline WParams wparams(const OscParams& p) {
-    return WParams{(float)p.w[0], (float)p.w[1], (float)p.w[2], (float)p.w[3]};
+CP3_HD WParams wparams(const OscParams& p) {
+    return WParams{p.wf[0], p.wf[1], p.wf[2], p.wf[3]};
 }
 
 // One atmospheric bin over M+1 segments, generic in where each segment's layer matrix comes
@@ -251,10 +251,12 @@ __device__ __forceinline__ void segment_matrix_inline(const OscParams* __restric
     layer_matrix(z, P[0], P[1], S);
 }
 
-// One beam energy: eigen-decomposition (double-float refined), then for each baseline
-// L[j] the layer matrix and the nine probabilities at out + j * baseline_stride + ch * plane.
+// One beam energy (E, rho_e as double or float pair): eigen-decomposition (double-float
+// refined), then for each baseline L[j] the layer matrix and the nine probabilities at
+// out + j * baseline_stride + ch * plane.
+template <class Real>
 __device__ __forceinline__ void beam_bin_mixed(const OscParams* __restrict__ p, const WParams& w,
-                                               double E, double rho_e, const float2* L, int nL,
+                                               Real E, Real rho_e, const float2* L, int nL,
                                                float* __restrict__ out, size_t plane,
                                                size_t baseline_stride) {
     float P[2][6], om[2][2];

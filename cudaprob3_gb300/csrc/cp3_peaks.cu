@@ -5,6 +5,9 @@
 // kernel measures them live, under the same clocks as the bench: every thread runs eight
 // independent dependent FMA chains (enough to cover the pipe latency), and the device time
 // of a launch that fills every SM several times over gives FLOP/s = 2 x FMAs / time.
+// A third variant runs the chains on float pairs with the paired FP32 FMA of sm_100+
+// (__ffma2_rn, two FMAs per instruction), the FP32 pipe's throughput when instruction issue
+// is not the limit.
 #include <cuda_runtime.h>
 
 namespace {
@@ -27,8 +30,37 @@ __global__ void __launch_bounds__(kThreads) fma_chains(T* out, int iters, T b, T
     if (s == (T)-12345.0) out[blockIdx.x * kThreads + threadIdx.x] = s;  // keeps the chains live
 }
 
+__global__ void __launch_bounds__(kThreads) fma2_chains(float* out, int iters, float b, float c) {
+    float2 a[kChains];
+#pragma unroll
+    for (int k = 0; k < kChains; k++)
+        a[k] = make_float2((float)(threadIdx.x + k) * 1e-3f, (float)(threadIdx.x + k + 1) * 1e-3f);
+    const float2 b2 = make_float2(b, b), c2 = make_float2(c, c);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < kChains; k++) a[k] = __ffma2_rn(a[k], b2, c2);
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < kChains; k++) s += a[k].x + a[k].y;
+    if (s == -12345.0f) out[blockIdx.x * kThreads + threadIdx.x] = s;
+}
+
 template <typename T>
-int run(int device, int iters, double* tflops, double* ms_out) {
+void launch_chains(bool paired, int blocks, T* out, int iters, T b, T c, cudaStream_t s) {
+    fma_chains<T><<<blocks, kThreads, 0, s>>>(out, iters, b, c);
+}
+template <>
+void launch_chains<float>(bool paired, int blocks, float* out, int iters, float b, float c,
+                          cudaStream_t s) {
+    if (paired)
+        fma2_chains<<<blocks, kThreads, 0, s>>>(out, iters, b, c);
+    else
+        fma_chains<float><<<blocks, kThreads, 0, s>>>(out, iters, b, c);
+}
+
+template <typename T>
+int run(int device, int iters, bool paired, double* tflops, double* ms_out) {
     if (cudaSetDevice(device) != cudaSuccess) return 1;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -41,11 +73,11 @@ int run(int device, int iters, double* tflops, double* ms_out) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const T b = (T)0.999999, c = (T)1e-7;
-    for (int w = 0; w < 3; w++) fma_chains<T><<<blocks, kThreads, 0, s>>>(out, iters, b, c);
+    for (int w = 0; w < 3; w++) launch_chains<T>(paired, blocks, out, iters, b, c, s);
     float best = 1e30f;
     for (int r = 0; r < 5; r++) {
         cudaEventRecord(e0, s);
-        fma_chains<T><<<blocks, kThreads, 0, s>>>(out, iters, b, c);
+        launch_chains<T>(paired, blocks, out, iters, b, c, s);
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
         float ms = 0.f;
@@ -53,7 +85,7 @@ int run(int device, int iters, double* tflops, double* ms_out) {
         if (ms < best) best = ms;
     }
     const int err = cudaGetLastError() != cudaSuccess ? 3 : 0;
-    const double flops = 2.0 * kChains * (double)iters * blocks * kThreads;
+    const double flops = (paired ? 4.0 : 2.0) * kChains * (double)iters * blocks * kThreads;
     *tflops = flops / (best * 1e-3) / 1e12;
     *ms_out = best;
     cudaEventDestroy(e0);
@@ -65,6 +97,8 @@ int run(int device, int iters, double* tflops, double* ms_out) {
 
 }  // namespace
 
-extern "C" int cp3peaks_fma_tflops(int fp64, int device, int iters, double* tflops, double* ms) {
-    return fp64 ? run<double>(device, iters, tflops, ms) : run<float>(device, iters, tflops, ms);
+// mode 0: FP32 FMA, 1: FP64 FMA, 2: paired FP32 FMA (__ffma2_rn).
+extern "C" int cp3peaks_fma_tflops(int mode, int device, int iters, double* tflops, double* ms) {
+    if (mode == 1) return run<double>(device, iters, false, tflops, ms);
+    return run<float>(device, iters, mode == 2, tflops, ms);
 }

@@ -39,6 +39,14 @@ int64_t now_ns() {
 }
 
 constexpr size_t kUnit = 64;  // pool granularity in floats (256 bytes)
+constexpr int kServeRows = 2;       // tile shape of the serving launches: cosine rows per tile
+constexpr int kServeBeamChunk = 2;  // and 32-energy groups per beam tile
+
+// x as a float pair (hi, lo), hi + lo = x to ~48 bits.
+float2 split_pair(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
 
 template <class T>
 struct DBuf {
@@ -60,7 +68,7 @@ struct HBuf {  // pinned
 struct Template {
     int kind = 0, ne = 0, ne_pad = 0, nrows = 0, ncls = 0;
     long long e_off = 0, row_off = 0, cls_off = 0;
-    double rho_e = 0.0;
+    float rho_e[2] = {0.f, 0.f};  // beam: rho * 0.5 as a float pair
     size_t tab_floats = 0, out_floats = 0;
     long long bins = 0;
 };
@@ -117,13 +125,13 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     DBuf<Problem> d_probs;
-    DBuf<long long> d_a, d_b;
+    DBuf<int> d_a, d_b;
     DBuf<Header> d_hdr;
     DBuf<OscParams> d_params;
     DBuf<int> d_done, d_status;
-    DBuf<unsigned long long> d_counter;
+    DBuf<unsigned int> d_counter;
     HBuf<Problem> h_probs;
-    HBuf<long long> h_a, h_b;
+    HBuf<int> h_a, h_b;
     HBuf<Header> h_hdr;
     HBuf<OscParams> h_params;
     std::vector<std::shared_ptr<Request>> reqs;
@@ -148,12 +156,10 @@ struct cp3_server {
 
     // registration (host), then resident device arenas
     std::vector<Template> tmpls;
-    std::vector<double> h_energies, h_cls_rho;
     std::vector<int> h_row_off, h_seg_cls;
-    std::vector<float2> h_seg_len, h_baselines;
-    DBuf<double> d_energies, d_cls_rho;
+    std::vector<float2> h_energies, h_cls_rho, h_seg_len, h_baselines;
     DBuf<int> d_row_off, d_seg_cls;
-    DBuf<float2> d_seg_len, d_baselines;
+    DBuf<float2> d_energies, d_cls_rho, d_seg_len, d_baselines;
     DBuf<float> d_pool;
     Pool pool;
     Slot slots[2];
@@ -263,27 +269,25 @@ void launch_slot(cp3_server* s, Slot& slot) {
         P.cls_off = T.cls_off;
         P.tab_off = (long long)(r.pool_off * kUnit);
         P.out_off = P.tab_off + (long long)T.tab_floats;
-        P.rho_e = T.rho_e;
+        P.rho_e[0] = T.rho_e[0];
+        P.rho_e[1] = T.rho_e[1];
         slot.h_probs.ptr[i] = P;
         slot.h_params.ptr[i] = r.params;
-        const long long nchunk = (T.ne + kTileE - 1) / kTileE;
-        if (T.kind == 0) {
-            a += nchunk * T.ncls;
-            b += nchunk * T.nrows;
-        } else {
-            b += (T.ne + 127) / 128;  // beam_chunk 1, R 1
-        }
-        slot.h_a.ptr[i + 1] = a;
-        slot.h_b.ptr[i + 1] = b;
+        long long na = 0, nb = 0;
+        problem_tiles(P, kServeRows, kServeBeamChunk, &na, &nb);
+        a += na;
+        b += nb;
+        slot.h_a.ptr[i + 1] = (int)a;  // < kMaxTiles: a launch holds at most max_bins bins
+        slot.h_b.ptr[i + 1] = (int)b;  // besides its first request, and requests fit the pool
         r.t_start = t0;
         r.state.store(kRunning);
     }
-    *slot.h_hdr.ptr = Header{n, 1, a, b};
+    *slot.h_hdr.ptr = Header{n, kServeRows, kServeBeamChunk, (int)a, (int)b};
     cudaStream_t st = slot.stream;
     cudaMemcpyAsync(slot.d_probs.ptr, slot.h_probs.ptr, sizeof(Problem) * n, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(slot.d_params.ptr, slot.h_params.ptr, sizeof(OscParams) * n, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(slot.d_a.ptr, slot.h_a.ptr, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(slot.d_b.ptr, slot.h_b.ptr, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(slot.d_a.ptr, slot.h_a.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(slot.d_b.ptr, slot.h_b.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(slot.d_hdr.ptr, slot.h_hdr.ptr, sizeof(Header), cudaMemcpyHostToDevice, st);
     cudaGraphLaunch(slot.graph, st);
     slot.finished.store(0);
@@ -337,7 +341,7 @@ int capture_slot(cp3_server* s, Slot& sl) {
     S_CUDA(s, sl.h_params.alloc(cap), "pinned");
     S_CUDA(s, cudaMemset(sl.d_status.ptr, 0, sizeof(int)), "memset");
     int occ = 0;
-    S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<1>, 128, 0), "occupancy");
+    S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kBlock, 0), "occupancy");
     const int grid = std::max(1, s->sms * std::max(occ, 1));
     Args args{sl.d_hdr.ptr, sl.d_probs.ptr, sl.d_a.ptr, sl.d_b.ptr, sl.d_params.ptr,
               s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr, s->d_seg_cls.ptr,
@@ -347,10 +351,10 @@ int capture_slot(cp3_server* s, Slot& sl) {
     S_CUDA(s, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
     cudaGraph_t g;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, sizeof(unsigned long long), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, sizeof(unsigned int), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_done.ptr, 0, sizeof(int) * cap, cs);
     if (e == cudaSuccess) {
-        batch_kernel<1><<<grid, 128, 0, cs>>>(args);
+        batch_kernel<<<grid, kBlock, 0, cs>>>(args);
         e = cudaGetLastError();
     }
     const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
@@ -449,18 +453,18 @@ int cp3_server_add_atmos_grid(cp3_server* s, const double* cosines, int nc, cons
     T.nrows = nc;
     T.ncls = 1 + *std::max_element(t.maxlayers.begin(), t.maxlayers.end());
     T.e_off = (long long)s->h_energies.size();
-    s->h_energies.insert(s->h_energies.end(), energies, energies + ne);
+    for (int i = 0; i < ne; i++) s->h_energies.push_back(split_pair(energies[i]));
     T.row_off = (long long)s->h_row_off.size();
     const int base = (int)s->h_seg_len.size();
     for (int v : t.offset) s->h_row_off.push_back(base + v);
     for (size_t i = 0; i < t.len_km.size(); i++) {
-        const float h = (float)t.len_km[i];
-        s->h_seg_len.push_back(make_float2(h, (float)(t.len_km[i] - (double)h)));
+        s->h_seg_len.push_back(split_pair(t.len_km[i]));
         s->h_seg_cls.push_back(t.cls[i]);
     }
     T.cls_off = (long long)s->h_cls_rho.size();
-    s->h_cls_rho.push_back(0.0);
-    for (int c = 1; c < T.ncls; c++) s->h_cls_rho.push_back(s->model.rho[c - 1] * s->model.ye[c - 1]);
+    s->h_cls_rho.push_back(split_pair(0.0));
+    for (int c = 1; c < T.ncls; c++)
+        s->h_cls_rho.push_back(split_pair(s->model.rho[c - 1] * s->model.ye[c - 1]));
     T.tab_floats = (size_t)T.ncls * T.ne_pad * kMixFields;  // multiple of kUnit (ne_pad % 32 == 0)
     T.out_floats = ((size_t)9 * nc * ne + kUnit - 1) / kUnit * kUnit;
     T.bins = (long long)nc * ne;
@@ -480,13 +484,12 @@ int cp3_server_add_beam_grid(cp3_server* s, const double* energies, int ne, doub
     T.ne_pad = pad_energies(ne);
     T.nrows = n_baselines;
     T.e_off = (long long)s->h_energies.size();
-    s->h_energies.insert(s->h_energies.end(), energies, energies + ne);
+    for (int i = 0; i < ne; i++) s->h_energies.push_back(split_pair(energies[i]));
     T.row_off = (long long)s->h_baselines.size();
-    for (int j = 0; j < n_baselines; j++) {
-        const float h = (float)path_km[j];
-        s->h_baselines.push_back(make_float2(h, (float)(path_km[j] - (double)h)));
-    }
-    T.rho_e = rho * kDensityConvert;
+    for (int j = 0; j < n_baselines; j++) s->h_baselines.push_back(split_pair(path_km[j]));
+    const float2 r = split_pair(rho * kDensityConvert);
+    T.rho_e[0] = r.x;
+    T.rho_e[1] = r.y;
     T.tab_floats = 0;
     T.out_floats = ((size_t)9 * n_baselines * ne + kUnit - 1) / kUnit * kUnit;
     T.bins = (long long)n_baselines * ne;

@@ -48,15 +48,17 @@ __global__ void __launch_bounds__(kTableBlock)
 // double-float; FP64 only where two roots nearly coincide).  One 64-byte entry per
 // (class c, energy e) at table[(c * ne_pad + e) * 16]: P1 (00,01,02,11,12,22), P2, then
 // omega_1 hi/lo, omega_2 hi/lo -- four 16-byte words a thread reads with vector loads.
+// Real = double (split on the device) or float2 (pairs split on the host: no FP64 at all).
+template <class Real>
 __global__ void __launch_bounds__(kTableBlock)
-    table_mixed_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
-                       int ne, int ne_pad, const double* __restrict__ cls_rho,
+    table_mixed_kernel(const __grid_constant__ OscParams p, const Real* __restrict__ energies,
+                       int ne, int ne_pad, const Real* __restrict__ cls_rho,
                        float* __restrict__ table) {
     const int ie = blockIdx.x * kTableBlock + threadIdx.x;
     const int c = blockIdx.y;
     if (ie >= ne) return;
     float P[2][6], om[2][2];
-    rotated_eigen_mixed(&p, energies[ie], cls_rho[c], P, om);
+    rotated_eigen_mixed(&p, to_df(energies[ie]), to_df(cls_rho[c]), P, om);
     float4* t = reinterpret_cast<float4*>(table + ((size_t)c * ne_pad + ie) * kMixFields);
     t[0] = make_float4(P[0][0], P[0][1], P[0][2], P[0][3]);
     t[1] = make_float4(P[0][4], P[0][5], P[1][0], P[1][1]);
@@ -89,12 +91,23 @@ cudaError_t launch_table_f64(const OscParams& p, const double* energies, int ne,
     return cudaGetLastError();
 }
 
-cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int ne,
-                               const double* cls_rho, int ncls, float* table, cudaStream_t s) {
+template <class Real>
+static cudaError_t table_mixed(const OscParams& p, const Real* energies, int ne,
+                               const Real* cls_rho, int ncls, float* table, cudaStream_t s) {
     if (ne <= 0 || ncls <= 0) return cudaSuccess;
     dim3 grid((ne + kTableBlock - 1) / kTableBlock, ncls);
-    table_mixed_kernel<<<grid, kTableBlock, 0, s>>>(p, energies, ne, pad_energies(ne), cls_rho, table);
+    table_mixed_kernel<Real><<<grid, kTableBlock, 0, s>>>(p, energies, ne, pad_energies(ne), cls_rho, table);
     return cudaGetLastError();
+}
+
+cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int ne,
+                               const double* cls_rho, int ncls, float* table, cudaStream_t s) {
+    return table_mixed(p, energies, ne, cls_rho, ncls, table, s);
+}
+
+cudaError_t launch_table_mixed(const OscParams& p, const float2* energies, int ne,
+                               const float2* cls_rho, int ncls, float* table, cudaStream_t s) {
+    return table_mixed(p, energies, ne, cls_rho, ncls, table, s);
 }
 
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,

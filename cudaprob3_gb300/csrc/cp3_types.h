@@ -37,7 +37,7 @@ struct alignas(16) OscParams {
     float cpolyf[5][2];
     int order[3];        // root order from the vacuum cubic (prepare_getMfast)
     int anti;            // 1: antineutrino sign of the matter potential
-    int pad[4];
+    float wf[4];         // w rounded to float (the mixed kernels' W)
 };
 
 }  // namespace cp3

@@ -201,8 +201,8 @@ int cp3_kernel_times(cp3_propagator* h, double* eigen_ms, double* bins_ms);
 
 /* ---- batches: many problems, one persistent launch --------------------------------------- */
 
-/* No reference counterpart (the reference propagates one grid per call; SURVEY C2-C4 ask
- * for many parameter sets with uneven grids in one launch).  A batch holds atmospheric
+/* No reference counterpart (the reference propagates one grid per call; a fit evaluates many
+ * parameter sets with uneven grids, here in one launch).  A batch holds atmospheric
  * problems (one Earth model and production height per batch, own cosine/energy grid each)
  * and beam problems (own energies, density and baselines), each with its own oscillation
  * parameters and neutrino type, computed in MIXED precision by one persistent kernel
@@ -230,8 +230,9 @@ int cp3_batch_set_params(cp3_batch* b, int id, double theta12, double theta13, d
                          int neutrino_type);
 /* Freezes the problem list: trajectories, device arenas, the CUDA graph. */
 int cp3_batch_commit(cp3_batch* b);
-/* Tile shape of the persistent kernel (results do not depend on it): cosine rows per tile
- * (1 or 2), resident blocks per SM (0 = as many as fit), beam energy chunks per tile. */
+/* Tile shape of the persistent kernel (results do not depend on it): cosine rows per
+ * atmospheric tile (1..16; a tile is 32 energies), resident blocks per SM (0 = as many as
+ * fit), 32-energy groups per beam tile (1..64). */
 int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int beam_chunk);
 int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_sm,
                         int* beam_chunk);
@@ -252,7 +253,7 @@ int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins,
 
 /* ---- serving: continuous batching ------------------------------------------------------- */
 
-/* No reference counterpart (SURVEY C4).  A request is one registered grid + one parameter set
+/* No reference counterpart.  A request is one registered grid + one parameter set
  * + a neutrino type; submit returns at once.  A scheduler thread admits queued requests in
  * arrival order as device memory (a pool of pool_bytes for their tables and results) and one
  * of two launch slots free up, packs up to max_batch requests / max_bins_per_launch bins

@@ -84,7 +84,7 @@ def test_batch_results_do_not_depend_on_tile_shape():
     rng = np.random.default_rng(4)
     b, probs = build_batch(earth.gaussian_sets(3, seed=13), rng)
     ref = None
-    for shape in [(1, 0, 4), (2, 0, 1), (1, 2, 16), (2, 1, 4)]:
+    for shape in [(1, 0, 4), (2, 0, 1), (1, 2, 16), (4, 1, 4), (8, 0, 2), (16, 0, 64)]:
         b.set_shape(*shape)
         b.run()
         b.synchronize()
@@ -140,3 +140,6 @@ def test_batch_errors():
         b.add_beam([1.0], 2.6, [810.0])
     with pytest.raises(CP3Error, match="no such problem"):
         b.result_ptr(7)
+    for bad in [(0, 0, 4), (17, 0, 4), (1, -1, 4), (1, 0, 0), (1, 0, 65)]:
+        with pytest.raises(CP3Error, match="shape"):
+            b.set_shape(*bad)

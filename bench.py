@@ -463,8 +463,8 @@ def run_ours(args, rank, world):
     cz_pinned = (torch.from_numpy(np.asarray(w["cz"], dtype=np.float64)).pin_memory()
                  if w["kind"] == "atmos" else None)
 
-    # neutrino and antineutrino on their own streams: one type's download overlaps the other's
-    # compute
+    # neutrino and antineutrino on their own streams, each computed in row pieces whose
+    # downloads overlap the next piece's compute (cp3_calculate_to_host_async)
     e2e_streams = [torch.cuda.Stream() for _ in props]
 
     def e2e_step():
@@ -473,8 +473,7 @@ def run_ours(args, rank, world):
             if cz_pinned is not None:
                 p.setCosineList(cz_pinned.numpy())
             sp = e2e_streams[t].cuda_stream
-            p.calculate_async(t, sp)
-            p.copy_result_async(host_out[t].data_ptr(), sp)
+            p.calculate_to_host_async(t, host_out[t].data_ptr(), 0, sp)
         for st in e2e_streams:
             st.synchronize()
 

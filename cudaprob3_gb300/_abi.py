@@ -17,6 +17,7 @@ EXPORTS = (
     "cp3_set_layers_poly", "cp3_set_density_file", "cp3_set_chemical_composition",
     "cp3_set_production_height", "cp3_set_beam_density", "cp3_set_beam_path_length",
     "cp3_set_production_height_averaging", "cp3_calculate", "cp3_calculate_async",
+    "cp3_calculate_to_host_async",
     "cp3_synchronize", "cp3_get_probability", "cp3_get_probability_beam",
     "cp3_get_probability_arr", "cp3_device_result", "cp3_copy_result_async",
     "cp3_trajectory_table", "cp3_set_profiling", "cp3_kernel_times", "cp3_atmos_mixed_noalloc",
@@ -59,6 +60,7 @@ _SIGS = {
     "cp3_set_production_height_averaging": ([_h, C.c_int, _dp, _dp], C.c_int),
     "cp3_calculate": ([_h, C.c_int], C.c_int),
     "cp3_calculate_async": ([_h, C.c_int, C.c_void_p], C.c_int),
+    "cp3_calculate_to_host_async": ([_h, C.c_int, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "cp3_synchronize": ([_h], C.c_int),
     "cp3_get_probability": ([_h, C.c_int, C.c_int, C.c_int, _dp], C.c_int),
     "cp3_get_probability_beam": ([_h, C.c_int, C.c_int, _dp], C.c_int),

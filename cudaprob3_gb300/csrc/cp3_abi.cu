@@ -104,6 +104,10 @@ struct cp3_propagator {
 
 namespace {
 
+// Pieces of a pipelined compute-and-copy: enough to hide most of the computation behind the
+// copy, few enough that each piece's kernel still fills the GPU.
+constexpr int kDefaultCopyChunks = 4;
+
 // x[i] as float pairs (hi, lo), hi + lo = x[i] to ~48 bits (the device's df_from, done once).
 std::vector<float2> split_pairs(const double* x, size_t n) {
     std::vector<float2> out(n);
@@ -258,7 +262,10 @@ int prepare_averaging(cp3_propagator* h, AvgArrays* av) {
     return CP3_OK;
 }
 
-int launch(cp3_propagator* h, int type, cudaStream_t s) {
+// One computation on stream s.  With host_dst, the result is also copied to host memory:
+// atmospheric rows in n_chunks pieces, each piece's copy queued right after its kernel, so
+// the copy of one piece overlaps the computation of the next.
+int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr, int n_chunks = 1) {
     if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
         return fail(h, CP3_ERR_BAD_ARGUMENT, "neutrino type must be Neutrino or Antineutrino");
     if (!h->energies_set) return fail(h, CP3_ERR_NOT_SET, "energy list was not set");
@@ -270,9 +277,11 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
     build_osc_params(h->mix, type == CP3_ANTINEUTRINO, &p);
     cudaError_t e = cudaSuccess;
     h->timed = false;
+    const bool profile = h->profiling && !host_dst;  // kernel times only without copies
     auto mark = [&](int i) {
-        if (h->profiling && e == cudaSuccess) e = cudaEventRecord(h->ev[i], s);
+        if (profile && e == cudaSuccess) e = cudaEventRecord(h->ev[i], s);
     };
+    const size_t esz = h->precision == CP3_FP64 ? sizeof(double) : sizeof(float);
     if (h->kind == 0) {
         if (!h->model_set) return fail(h, CP3_ERR_NOT_SET, "density model was not set");
         if (!h->height_set)
@@ -289,28 +298,46 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
         rc = prepare_averaging(h, &av);
         if (rc) return rc;
         mark(0);
-        if (h->model.poly) {
-            mark(1);
-            const bool mixed = h->precision == CP3_MIXED;
-            e = launch_atmos_inline(p, mixed, h->d_energies.ptr, h->ne, h->d_seg_off.ptr,
-                                    mixed ? (const void*)h->d_seg_len_df.ptr : (const void*)h->d_seg_len.ptr,
-                                    h->d_seg_rho.ptr, h->nc, av, h->d_result.ptr, s);
-        } else if (h->precision == CP3_FP64) {
-            e = launch_table_f64(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
-                                 h->d_table64.ptr, s);
-            mark(1);
-            if (e == cudaSuccess)
-                e = launch_atmos_f64(p, h->d_energies.ptr, h->ne, h->d_table64.ptr,
-                                     h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
-                                     av, (double*)h->d_result.ptr, s);
+        const bool mixed = h->precision == CP3_MIXED;
+        if (!h->model.poly) {
+            if (mixed)
+                e = launch_table_mixed(p, h->d_energies_df.ptr, h->ne, h->d_cls_rho_df.ptr,
+                                       h->ncls_used, h->d_table32.ptr, s);
+            else
+                e = launch_table_f64(p, h->d_energies.ptr, h->ne, h->d_cls_rho.ptr, h->ncls_used,
+                                     h->d_table64.ptr, s);
+        }
+        mark(1);
+        auto bins = [&](RowRange rr) {
+            if (h->model.poly)
+                return launch_atmos_inline(p, mixed, h->d_energies.ptr, h->ne, h->d_seg_off.ptr,
+                                           mixed ? (const void*)h->d_seg_len_df.ptr
+                                                 : (const void*)h->d_seg_len.ptr,
+                                           h->d_seg_rho.ptr, h->nc, av, h->d_result.ptr, s, rr);
+            if (mixed)
+                return launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
+                                          h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc,
+                                          (float*)h->d_result.ptr, s, rr);
+            return launch_atmos_f64(p, h->d_energies.ptr, h->ne, h->d_table64.ptr,
+                                    h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
+                                    av, (double*)h->d_result.ptr, s, rr);
+        };
+        if (!host_dst) {
+            if (e == cudaSuccess) e = bins(RowRange{});
         } else {
-            e = launch_table_mixed(p, h->d_energies_df.ptr, h->ne, h->d_cls_rho_df.ptr,
-                                   h->ncls_used, h->d_table32.ptr, s);
-            mark(1);
-            if (e == cudaSuccess)
-                e = launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
-                                       h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc,
-                                       (float*)h->d_result.ptr, s);
+            // each piece: rows [r0, r1) of all 9 channel planes, one 2-D copy
+            const int chunks = std::max(1, std::min(n_chunks, h->nc));
+            const size_t plane = (size_t)h->nc * h->ne * esz, row = (size_t)h->ne * esz;
+            for (int c = 0; c < chunks && e == cudaSuccess; c++) {
+                const int r0 = (int)((long long)h->nc * c / chunks);
+                const int r1 = (int)((long long)h->nc * (c + 1) / chunks);
+                if (r1 <= r0) continue;
+                e = bins(RowRange{r0, r1});
+                if (e == cudaSuccess)
+                    e = cudaMemcpy2DAsync((char*)host_dst + r0 * row, plane,
+                                          h->d_result.ptr + r0 * row, plane, (r1 - r0) * row, 9,
+                                          cudaMemcpyDeviceToHost, s);
+            }
         }
         mark(2);
         h->timed_table = true;
@@ -327,13 +354,15 @@ int launch(cp3_propagator* h, int type, cudaStream_t s) {
             e = launch_beam_mixed(p, h->d_energies_df.ptr, h->ne, rho_e, h->beam_L,
                                   (float*)h->d_result.ptr, s);
         mark(2);
+        if (host_dst && e == cudaSuccess)
+            e = cudaMemcpyAsync(host_dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost, s);
         h->timed_table = false;
     }
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     h->result_on_host = false;
     h->computed = true;
     h->last_stream = s;
-    h->timed = h->profiling;
+    h->timed = profile;
     return CP3_OK;
 }
 
@@ -576,6 +605,13 @@ int cp3_calculate(cp3_propagator* h, int type) {
 int cp3_calculate_async(cp3_propagator* h, int type, void* stream) {
     if (int rc = check_handle(h)) return rc;
     return launch(h, type, stream ? (cudaStream_t)stream : h->stream);
+}
+
+int cp3_calculate_to_host_async(cp3_propagator* h, int type, void* dst, int n_chunks, void* stream) {
+    if (int rc = check_handle(h)) return rc;
+    if (!dst) return fail(h, CP3_ERR_BAD_ARGUMENT, "null destination");
+    if (n_chunks <= 0) n_chunks = kDefaultCopyChunks;
+    return launch(h, type, stream ? (cudaStream_t)stream : h->stream, dst, n_chunks);
 }
 
 int cp3_synchronize(cp3_propagator* h) {

@@ -350,13 +350,13 @@ __global__ void __launch_bounds__(kBlock)
 cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
                              const double* table, const int* seg_off, const double* seg_len,
                              const int* seg_cls, int n_cosines, const AvgArrays& avg, double* out,
-                             cudaStream_t s) {
-    (void)p;
+                             cudaStream_t s, RowRange rr) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
     const AvgInput av{avg.prob, avg.shift, avg.air_cm, avg.n_bins, p.anti};
-    for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
-        const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
+    const int end = rr.end < 0 ? n_cosines : rr.end;
+    for (int ic0 = rr.begin; ic0 < end; ic0 += kMaxGridY) {
+        const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_f64_kernel<<<grid, kBlock, 0, s>>>(energies, ne, ne_pad, table, seg_off, seg_len,
                                                  seg_cls, ic0, n_cosines, av, out);
@@ -366,12 +366,13 @@ cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
 
 cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
                                const int* seg_off, const float2* seg_len, const int* seg_cls,
-                               int n_cosines, float* out, cudaStream_t s) {
+                               int n_cosines, float* out, cudaStream_t s, RowRange rr) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
     const WParams w = wparams(p);
-    for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
-        const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
+    const int end = rr.end < 0 ? n_cosines : rr.end;
+    for (int ic0 = rr.begin; ic0 < end; ic0 += kMaxGridY) {
+        const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_mixed_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
                                                    seg_cls, ic0, n_cosines, out);
@@ -381,11 +382,13 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
 
 cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
                                 const int* seg_off, const void* seg_len, const double* seg_rho,
-                                int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s) {
+                                int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s,
+                                RowRange rr) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const AvgInput av{avg.prob, avg.shift, avg.air_cm, avg.n_bins, p.anti};
-    for (int ic0 = 0; ic0 < n_cosines; ic0 += kMaxGridY) {
-        const int rows = n_cosines - ic0 < kMaxGridY ? n_cosines - ic0 : kMaxGridY;
+    const int end = rr.end < 0 ? n_cosines : rr.end;
+    for (int ic0 = rr.begin; ic0 < end; ic0 += kMaxGridY) {
+        const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         if (mixed)
             atmos_mixed_inline_kernel<<<grid, kBlock, 0, s>>>(p, wparams(p), energies, ne, seg_off,

@@ -33,20 +33,27 @@ struct AvgArrays {
     int n_bins = 0;
 };
 
-// Atmospheric bins of an n_cosines-row result.
+// Cosine rows [begin, end) of a result (end < 0: through the last row).
+struct RowRange {
+    int begin = 0, end = -1;
+};
+
+// Atmospheric bins of an n_cosines-row result ([9][n_cosines][ne]), rows rr only.
 cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
                              const double* table, const int* seg_off, const double* seg_len,
                              const int* seg_cls, int n_cosines, const AvgArrays& avg, double* out,
-                             cudaStream_t s);
+                             cudaStream_t s, RowRange rr = RowRange{});
 cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
                                const int* seg_off, const float2* seg_len, const int* seg_cls,
-                               int n_cosines, float* out, cudaStream_t s);
+                               int n_cosines, float* out, cudaStream_t s,
+                               RowRange rr = RowRange{});
 
 // Atmospheric bins whose segments each carry their own electron density (quadratic model):
 // per-segment eigen-solve.  seg_len: double[] (FP64) or float2[] hi/lo (mixed).
 cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
                                 const int* seg_off, const void* seg_len, const double* seg_rho,
-                                int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s);
+                                int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s,
+                                RowRange rr = RowRange{});
 
 // Beam bins: rho_e = rho * 0.5 (electron density), L in km.
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,

@@ -69,6 +69,13 @@ class Propagator:
         self._check(self._lib.cp3_calculate_async(self._h, int(type),
                                                   C.c_void_p(stream) if stream else None))
 
+    def calculate_to_host_async(self, type, dst_ptr: int, n_chunks: int = 0, stream=None):
+        """Compute and copy the whole result (device layout) to page-locked host memory at
+        dst_ptr, in n_chunks pipelined pieces (0: the library's default)."""
+        self._check(self._lib.cp3_calculate_to_host_async(
+            self._h, int(type), C.c_void_p(dst_ptr), int(n_chunks),
+            C.c_void_p(stream) if stream else None))
+
     def synchronize(self):
         self._check(self._lib.cp3_synchronize(self._h))
 

@@ -79,6 +79,13 @@ public:
         detail::check(cp3_calculate_async(h_, type == Antineutrino ? CP3_ANTINEUTRINO : CP3_NEUTRINO,
                                           cuda_stream), h_);
     }
+    // Compute and copy the result (device layout) to page-locked host memory, pipelined.
+    void calculateProbabilitiesToHostAsync(NeutrinoType type, void* host_dst, int n_chunks = 0,
+                                           void* cuda_stream = nullptr) {
+        detail::check(cp3_calculate_to_host_async(
+                          h_, type == Antineutrino ? CP3_ANTINEUTRINO : CP3_NEUTRINO, host_dst,
+                          n_chunks, cuda_stream), h_);
+    }
     void waitForCompletion() { detail::check(cp3_synchronize(h_), h_); }
     cp3_propagator* handle() { return h_; }
 

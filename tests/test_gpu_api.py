@@ -136,3 +136,39 @@ def test_unitarity_mixed_large():
     P = p.result().astype(np.float64).reshape(3, 3, 300, 200)  # [a][b][ic][ie]
     assert np.abs(P.sum(axis=1) - 1).max() < 1e-5
     assert np.abs(P.sum(axis=0) - 1).max() < 1e-5
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("model", ["shells", "quadratic"])
+def test_calculate_to_host_matches_device_result(prec, model):
+    import torch
+    nc, ne = 37, 29
+    p = configured(nc=nc, ne=ne, prec=prec)
+    if model == "quadratic":
+        p.setDensity(*earth.PREM_4LAYER_QUAD_V2)
+    for t in (NeutrinoType.Neutrino, NeutrinoType.Antineutrino):
+        p.calculateProbabilities(t)
+        want = p.result().copy()
+        dtype = torch.float64 if prec == "fp64" else torch.float32
+        for chunks in (0, 1, 3, 7, nc, nc + 5):
+            host = torch.full((9 * nc * ne,), -1.0, dtype=dtype, pin_memory=True)
+            p.calculate_to_host_async(t, host.data_ptr(), chunks)
+            p.synchronize()
+            assert np.array_equal(host.numpy().reshape(want.shape), want), chunks
+
+
+def test_calculate_to_host_beam():
+    import torch
+    ne = 101
+    b = BeamCudaPropagatorSingle(0, ne, 1, precision="mixed")
+    b.setEnergyList(earth.lin_energy_grid(ne))
+    b.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, 1)
+    b.setNeutrinoMasses(NOM.dm12sq, NOM.dm23sq)
+    b.setDensity(2.6)
+    b.setPathLength(1300.0)
+    b.calculateProbabilities(NeutrinoType.Neutrino)
+    want = b.result().copy()
+    host = torch.full((9 * ne,), -1.0, dtype=torch.float32, pin_memory=True)
+    b.calculate_to_host_async(NeutrinoType.Neutrino, host.data_ptr())
+    b.synchronize()
+    assert np.array_equal(host.numpy().reshape(want.shape), want)

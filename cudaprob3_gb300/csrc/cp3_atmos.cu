@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(kBlock)
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
     const double E = energies[ie];
-    atmos_bin_mixed_with([&](int l, cs6& S) { segment_matrix_inline(&p, E, s_rho[l], s_len[l], S); },
+    atmos_bin_mixed_with([&](int l, Layer& F) { segment_layer_inline(&p, E, s_rho[l], s_len[l], F); },
                          nseg - 1, w, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
 

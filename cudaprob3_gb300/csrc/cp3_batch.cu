@@ -144,8 +144,20 @@ int bcuda(cp3_batch* b, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return bcuda(b, e_, where);      \
     } while (0)
 
-int occupancy(int* blocks) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, batch_kernel, kBlock, 0) == cudaSuccess ? 0 : 1;
+using KernelFn = void (*)(Args);
+
+KernelFn kernel_for(int kinds) {
+    return kinds == kAtmos ? batch_kernel<kAtmos> : kinds == kBeam ? batch_kernel<kBeam> : batch_kernel<kBoth>;
+}
+
+int occupancy(int kinds, int* blocks) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kernel_for(kinds), kBlock, 0) == cudaSuccess ? 0 : 1;
+}
+
+int batch_kinds(const std::vector<Problem>& probs) {
+    bool a = false, b = false;
+    for (const Problem& P : probs) (P.kind == 0 ? a : b) = true;
+    return launch_kinds(a, b);
 }
 
 // Tile counts for the current shape, the device header and the graph.
@@ -170,7 +182,8 @@ int configure(cp3_batch* b) {
     B_CUDA(b, cudaStreamSynchronize(b->stream), "configure");
 
     int occ = 0;
-    if (occupancy(&occ) || occ < 1) return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
+    const int kinds = batch_kinds(b->probs);
+    if (occupancy(kinds, &occ) || occ < 1) return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
     const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, occ) : occ;
     const int grid = std::max(1, b->sms * bps);
     Args args{b->d_hdr.ptr, b->d_probs.ptr, b->d_astart.ptr, b->d_bstart.ptr, b->d_params.ptr,
@@ -189,7 +202,7 @@ int configure(cp3_batch* b) {
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_done.ptr, 0, sizeof(int) * std::max(n, 1), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_status.ptr, 0, sizeof(int), cs);
     if (e == cudaSuccess) {
-        batch_kernel<<<grid, kBlock, 0, cs>>>(args);
+        kernel_for(kinds)<<<grid, kBlock, 0, cs>>>(args);
         e = cudaGetLastError();
     }
     const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
@@ -483,7 +496,8 @@ int cp3_batch_synchronize(cp3_batch* b, double* ms) {
     }
     int st = 0;
     B_CUDA(b, cudaMemcpy(&st, b->d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost), "status");
-    if (st) return bfail(b, CP3_ERR_CUDA, "batch kernel: eigen tables did not complete (wait limit)");
+    if (st == 1) return bfail(b, CP3_ERR_CUDA, "batch kernel: eigen tables did not complete (wait limit)");
+    if (st) return bfail(b, CP3_ERR_CUDA, "batch kernel: a tile of a kind the launch was not built for");
     return CP3_OK;
 }
 
@@ -499,7 +513,7 @@ int cp3_batch_tune(cp3_batch* b, int use_cache) {
             if (k == key) return cp3_batch_set_shape(b, R, bps, bc);
     }
     int occ = 0;
-    occupancy(&occ);
+    occupancy(batch_kinds(b->probs), &occ);
     bool has_a = false, has_b = false;
     for (const Problem& P : b->probs) (P.kind == 0 ? has_a : has_b) = true;
     struct Shape {

@@ -34,7 +34,7 @@ struct Problem {
     long long e_off;   // energies arena
     long long row_off; // atmospheric: first of nrows + 1 row offsets; beam: first baseline
     long long cls_off; // atmospheric: first class density
-    long long tab_off; // atmospheric: float offset of the table [ncls][ne_pad][16]
+    long long tab_off; // atmospheric: float offset of the table [ncls][ne_pad][12]
     long long out_off; // float offset of the result
     float rho_e[2];    // beam: electron density (rho * 0.5) as a float pair (hi, lo)
 };
@@ -93,8 +93,17 @@ __device__ __forceinline__ int find_problem(const int* __restrict__ prefix, int 
     return lo;
 }
 
+// Which problem kinds a launch contains (bit set): the kernel is compiled once per set, so a
+// launch of one kind carries neither the code nor the register pressure of the other.
+constexpr int kAtmos = 1, kBeam = 2, kBoth = 3;
+
+CP3_HD int launch_kinds(bool has_atmos, bool has_beam) {
+    return (has_atmos ? kAtmos : 0) | (has_beam ? kBeam : 0);
+}
+
 // 64 registers per thread (the budget of the standalone per-bin kernel): 8 blocks per SM.
 // Internal linkage: each translation unit that launches it (batches, the server) has its own.
+template <int kKinds>
 static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
     constexpr int kWarps = kBlock / 32;
     __shared__ float2 s_len[kWarps][kMaxSegments];  // one trajectory per warp
@@ -130,25 +139,29 @@ static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
         const OscParams* prm = a.params + P.param;
 
         if (ph == 0) {
+            if (!(kKinds & kAtmos)) {  // cannot happen: the host picks kKinds from the problems
+                if (lane == 0) atomicExch(a.status, 2);
+                break;
+            }
             // ---- eigen-table tile: one class x 32 energies ----------------------------
             const int nchunk = (P.ne + kTileE - 1) / kTileE;
             const int c = local / nchunk;
             const int e = (local % nchunk) * kTileE + (int)lane;
             if (e < P.ne) {
-                float Pp[2][6], om[2][2];
+                float u[2][3], om[2][2];
                 const float2 E2 = a.energies[P.e_off + e], r2 = a.cls_rho[P.cls_off + c];
-                rotated_eigen_mixed(prm, df{E2.x, E2.y}, df{r2.x, r2.y}, Pp, om);
-                float4* d = reinterpret_cast<float4*>(a.tables + P.tab_off +
-                                                      ((size_t)c * P.ne_pad + e) * kMixFields);
-                d[0] = make_float4(Pp[0][0], Pp[0][1], Pp[0][2], Pp[0][3]);
-                d[1] = make_float4(Pp[0][4], Pp[0][5], Pp[1][0], Pp[1][1]);
-                d[2] = make_float4(Pp[1][2], Pp[1][3], Pp[1][4], Pp[1][5]);
-                d[3] = make_float4(om[0][0], om[0][1], om[1][0], om[1][1]);
+                rotated_eigen_vectors(prm, df{E2.x, E2.y}, df{r2.x, r2.y}, u, om);
+                store_table_entry(a.tables + P.tab_off + ((size_t)c * P.ne_pad + e) * kMixFields,
+                                  u, om);
             }
             __threadfence();
             __syncwarp();
             if (lane == 0) atomicAdd(a.done_a + p, 1);
         } else if (P.kind == 0) {
+            if (!(kKinds & kAtmos)) {
+                if (lane == 0) atomicExch(a.status, 2);
+                break;
+            }
             // ---- atmospheric bin tile: rows_per_tile rows x 32 energies ------------------
             if (ready != p) {
                 // This problem's table tiles were all handed out before this tile, to warps
@@ -191,6 +204,10 @@ static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
                                           (size_t)P.nrows * P.ne);
             }
         } else {
+            if (!(kKinds & kBeam)) {
+                if (lane == 0) atomicExch(a.status, 2);
+                break;
+            }
             // ---- beam tile: beam_chunk x 32 energies, every baseline --------------------
             const WParams w = wparams(*prm);
             const long long e0 = (long long)local * kTileE * hdr.beam_chunk;

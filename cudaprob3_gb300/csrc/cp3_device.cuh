@@ -418,19 +418,71 @@ CP3_HD df df_recip(df x) {
     const df one_minus = df_sub(df{1.0f, 0.0f}, df_mulf(x, r));  // 1 - x r, small
     return df_add(df{r, 0.0f}, df_mulf(one_minus, r));
 }
+// sqrt(x) to df64 accuracy for x > 0: float square root r, then one Newton correction
+// (x - r^2) / (2 r) with r^2 exact through TwoProduct (Dekker/Karp-Markstein form).
+CP3_HD df df_sqrt(df x) {
+    const float r = sqrtf(x.hi);
+    const float p = CP3_FMUL(r, r);
+    const float pe = fmaf(r, r, -p);
+    const float d = CP3_FADD(CP3_FADD(CP3_FADD(x.hi, -p), -pe), x.lo);  // x.hi - p is exact
+    return df_fast2sum(r, d * (0.5f / r));
+}
+
+// Symmetric (Loewdin-style, first order) orthonormalisation of two nearly orthonormal
+// vectors: a -= (a.b)/2 b, b -= (a.b)/2 a, then both normalised.
+//
+// Why the FP64 fallback of the eigenvector tables needs it: the three projectors of a
+// computed spectrum sum to the identity exactly whatever the root errors (they are the
+// Lagrange basis polynomials of H at the computed roots), so where two levels nearly
+// coincide, the errors of their two projectors cancel in S = 1 + z1 P1 + z2 P2 (z1 ~ z2).
+// Unit vectors taken from each projector separately lose that cancellation: u1.u2 departs
+// from 0 at first order in (root error / gap), and the reference cubic's roots of a nearly
+// double root are off by ~sqrt(eps) of the spread.  Restoring orthogonality leaves only a
+// rotation inside the near-degenerate plane, whose effect is multiplied by the small phase
+// difference z1 - z2.
+template <class T>
+CP3_HD void orthonormalize_pair(T a[3], T b[3]) {
+    const T h = (T)0.5 * (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+    T x[3], y[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        x[i] = a[i] - h * b[i];
+        y[i] = b[i] - h * a[i];
+    }
+    const T nx = (T)1 / sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    const T ny = (T)1 / sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        a[i] = x[i] * nx;
+        b[i] = y[i] * ny;
+    }
+}
 
 // The mixed kernels' eigen-decomposition without FP64 on the common path:
 //   1. V = -fac (matter potential in 2E.H units, eV^2) and the cubic's coefficients in df64;
 //   2. the three roots from the trigonometric solution in FP32;
 //   3. two Newton steps per root on the df64 polynomial (the third root from the trace);
-//   4. P1, P2 = (H - m_a)(H - m_b)/((m_k - m_a)(m_k - m_b)) in df64, rounded to float;
+//   4. P1, P2 = (H - m_a)(H - m_b)/((m_k - m_a)(m_k - m_b)) in df64, rounded to float, with
+//      the numerator as H^2 - (m_a + m_b) H + m_a m_b from H0^2 split on the host;
 //      omega_k = 2.534 (m_k - m_0) / E in df64 (hi, lo).
-// Where two refined roots lie closer than 1e-4 of the spread (exactly degenerate vacuum
-// masses, the reference's 5e-9 eV^2 degeneracy break) the FP64 reference cubic takes over.
+// Where two refined roots lie closer than 5e-3 of the spread the FP64 reference cubic takes
+// over.  Below that the double-float Newton steps are not reliably in their quadratic regime
+// (FP32 starting roots near a double root are off by ~sqrt(eps) of the spread, and Newton
+// then converges only linearly), so neither the roots nor the gap test itself can be
+// trusted there.  Physical parameters stay well above it: a scan of 2.4e6 (E, rho)
+// points, 0.1-100 GeV, 0-6.6 g/cm^3 electron density, Gaussian parameter sets in both
+// orderings, nu and nubar, has min gap/spread = 0.022 (100 GeV through the core); exactly
+// degenerate vacuum masses (the reference's 5e-9 eV^2 degeneracy break) are the cases it
+// catches.
 // E and rho arrive as float pairs (split once on the host), so the common path runs no FP64
 // instruction at all -- conversions included, which issue on the narrow FP64 pipe.
-CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed, df rhod, float P[2][6],
-                                float om[2][2]) {
+//
+// kVectors: instead of the projectors, out[k][0..2] = u_k, the unit eigenvector with
+// P_k = u_k u_k^T (sign arbitrary), taken from the column j of P_k with the largest diagonal:
+// u_k = P_k e_j / sqrt(P_k[j][j]), in double-float before the final rounding.
+template <bool kVectors>
+CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rhod,
+                                  float P[2][6], float om[2][2]) {
     // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos
     const df tw = df{1.52588e-4f, -7.040322e-12f};  // kTwoRtTwoGf = hi + lo
     df V = df_mul(df_mul(tw, Ed), rhod);
@@ -452,70 +504,122 @@ CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed, df rhod,
     float l0 = fmaf(2.0f * rt, cosf(th), s);
     float l1 = fmaf(2.0f * rt, cosf(th - 2.0943951f), s);
     df r[3] = {df{l0, 0.0f}, df{l1, 0.0f}, df{0.0f, 0.0f}};
+    // Newton steps: the residual in double-float, the derivative in FP32 (its relative error,
+    // ~eps * spread / gap < 2e-5, only slows the quadratic convergence by that factor).
 #pragma unroll
     for (int k = 0; k < 2; k++)
 #pragma unroll
         for (int it = 0; it < 2; it++) {
             const df x = r[k];
             const df f = df_sub(df_mul(df_add(df_mul(df_sub(x, c2), x), c1), x), c0);
-            const df d = df_add(df_mul(df_sub(df_mulf(x, 3.0f), df_mulf(c2, 2.0f)), x), c1);
-            r[k] = df_sub(x, df{f.hi / d.hi, 0.0f});
+            const float d = fmaf(fmaf(3.0f, x.hi, -2.0f * c2.hi), x.hi, c1.hi);
+            r[k] = df_sub(x, df{f.hi / d, 0.0f});
         }
     r[2] = df_sub(df_sub(c2, r[0]), r[1]);
     const float spread = fmaxf(fabsf(r[0].hi - r[1].hi), fmaxf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     const float gap = fminf(fabsf(r[0].hi - r[1].hi), fminf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
-    if (!(gap > 1e-4f * spread)) {
+    if (!(gap > 5e-3f * spread)) {
         double Pd[2][6], omd[2];
         rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
 #pragma unroll
         for (int k = 0; k < 2; k++) {
+            if (kVectors) {
+                const double d0 = Pd[k][0], d1 = Pd[k][3], d2 = Pd[k][5];
+                const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
+                const double c0 = j == 0 ? d0 : (j == 1 ? Pd[k][1] : Pd[k][2]);
+                const double c1 = j == 0 ? Pd[k][1] : (j == 1 ? d1 : Pd[k][4]);
+                const double c2 = j == 0 ? Pd[k][2] : (j == 1 ? Pd[k][4] : d2);
+                const double rs = 1.0 / sqrt(j == 0 ? d0 : (j == 1 ? d1 : d2));
+                Pd[k][0] = c0 * rs;  // u_k in place (the projector is no longer needed)
+                Pd[k][1] = c1 * rs;
+                Pd[k][2] = c2 * rs;
+            } else {
 #pragma unroll
-            for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
+                for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
+            }
             om[k][0] = (float)omd[k];
             om[k][1] = (float)(omd[k] - (double)om[k][0]);
         }
+        if (kVectors) {
+            orthonormalize_pair(Pd[0], Pd[1]);
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+#pragma unroll
+                for (int i = 0; i < 3; i++) P[k][i] = (float)Pd[k][i];
+        }
         return;
     }
-    df h[6];
+    // H = H0 + V e0 e0^T and H^2 = H0^2 + V (e0 a^T + a e0^T) + V^2 e0 e0^T (a = H0 e0): only
+    // the first row and column of H0^2 (from the host) change.
+    df h[6], H2[6];
 #pragma unroll
-    for (int q = 0; q < 6; q++) h[q] = df{p->h0f[q][0], p->h0f[q][1]};
+    for (int q = 0; q < 6; q++) {
+        h[q] = df{p->h0f[q][0], p->h0f[q][1]};
+        H2[q] = df{p->h2f[q][0], p->h2f[q][1]};
+    }
+    H2[0] = df_add(H2[0], df_mul(V, df_add(df_add(h[0], h[0]), V)));
+    H2[1] = df_add(H2[1], df_mul(V, h[1]));
+    H2[2] = df_add(H2[2], df_mul(V, h[2]));
     h[0] = df_add(h[0], V);
     const df loe = df_mul(df{2.534f, 8.010864e-08f}, df_recip(Ed));  // kLoEFac (= hi + lo) / E
 #pragma unroll
     for (int kk = 0; kk < 2; kk++) {
         const int k = kk + 1, a = 0, b = k == 1 ? 2 : 1;
-        df A[6], B[6];
+        // (H - m_a)(H - m_b) = H^2 - (m_a + m_b) H + m_a m_b
+        const df sab = df_add(r[a], r[b]), pab = df_mul(r[a], r[b]);
+        const df inv = df_recip(df_mul(df_sub(r[k], r[a]), df_sub(r[k], r[b])));
+        df Pk[6];
 #pragma unroll
         for (int q = 0; q < 6; q++) {
-            A[q] = h[q];
-            B[q] = h[q];
+            df n = df_sub(H2[q], df_mul(sab, h[q]));
+            if (q == 0 || q == 3 || q == 5) n = df_add(n, pab);
+            Pk[q] = df_mul(n, inv);
         }
-        A[0] = df_sub(A[0], r[a]);
-        A[3] = df_sub(A[3], r[a]);
-        A[5] = df_sub(A[5], r[a]);
-        B[0] = df_sub(B[0], r[b]);
-        B[3] = df_sub(B[3], r[b]);
-        B[5] = df_sub(B[5], r[b]);
-        const df inv = df_recip(df_mul(df_sub(r[k], r[a]), df_sub(r[k], r[b])));
+        if (kVectors) {
+            // column j with the largest diagonal (>= 1/3), selected without indexing
+            const float d0 = Pk[0].hi, d1 = Pk[3].hi, d2 = Pk[5].hi;
+            const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
+            const df c0 = j == 0 ? Pk[0] : (j == 1 ? Pk[1] : Pk[2]);
+            const df c1 = j == 0 ? Pk[1] : (j == 1 ? Pk[3] : Pk[4]);
+            const df c2 = j == 0 ? Pk[2] : (j == 1 ? Pk[4] : Pk[5]);
+            const df t = df_sqrt(j == 0 ? c0 : (j == 1 ? c1 : c2));  // sqrt(P_jj)
+            const df it = df_recip(t);
+            const df u0 = j == 0 ? t : df_mul(c0, it);
+            const df u1 = j == 1 ? t : df_mul(c1, it);
+            const df u2 = j == 2 ? t : df_mul(c2, it);
+            P[kk][0] = u0.hi + u0.lo;
+            P[kk][1] = u1.hi + u1.lo;
+            P[kk][2] = u2.hi + u2.lo;
+        } else {
 #pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = i; j < 3; j++) {
-                df acc = df_mul(A[sidx(i, 0)], B[sidx(0, j)]);
-                acc = df_add(acc, df_mul(A[sidx(i, 1)], B[sidx(1, j)]));
-                acc = df_add(acc, df_mul(A[sidx(i, 2)], B[sidx(2, j)]));
-                const df pv = df_mul(acc, inv);
-                P[kk][sidx(i, j)] = pv.hi + pv.lo;
-            }
+            for (int q = 0; q < 6; q++) P[kk][q] = Pk[q].hi + Pk[q].lo;
+        }
         const df w = df_mul(df_sub(r[k], r[0]), loe);
         om[kk][0] = w.hi;
         om[kk][1] = w.lo;
     }
+    // (No orthonormalisation here: with converged roots the double-float vectors are
+    // orthogonal to rounding, and an FP32 correction step would only add a rounding.)
 }
 
+// Projectors P1, P2 (00,01,02,11,12,22) and phase rates.
+CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed, df rhod, float P[2][6],
+                                float om[2][2]) {
+    rotated_eigen_mixed_t<false>(p, Ed, rhod, P, om);
+}
 CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E, double rho,
                                 float P[2][6], float om[2][2]) {
-    rotated_eigen_mixed(p, df_from(E), df_from(rho), P, om);
+    rotated_eigen_mixed_t<false>(p, df_from(E), df_from(rho), P, om);
+}
+// Unit eigenvectors u1, u2 (P_k = u_k u_k^T) and phase rates.
+CP3_HD void rotated_eigen_vectors(const OscParams* __restrict__ p, df Ed, df rhod,
+                                  float u[2][3], float om[2][2]) {
+    float out[2][6];
+    rotated_eigen_mixed_t<true>(p, Ed, rhod, out, om);
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) u[k][i] = out[k][i];
 }
 
 CP3_HD cf cmulf(cf a, cf b) {

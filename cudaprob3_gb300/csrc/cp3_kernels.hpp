@@ -10,8 +10,8 @@ namespace cp3 {
 
 // Fields of one (density class, energy) entry of the eigen tables.
 constexpr int kF64Fields = 57;  // C_k[a][b] re/im (54) + dmMatVac[k][0] (3)
-constexpr int kMixFields = 16;  // P1 (6), P2 (6) real symmetric; omega_1, omega_2 double-float
-                                // (one 64-byte entry per (class, energy))
+constexpr int kMixFields = 12;  // u1 (3), u2 (3) real unit eigenvectors; omega_1, omega_2
+                                // double-float; 2 unused (one 48-byte entry per (class, energy))
 
 inline int pad_energies(int ne) { return (ne + 31) / 32 * 32; }
 

@@ -9,10 +9,13 @@ namespace cp3 {
 
 // ------------------------------------------------------------------------------------
 // Mixed: the same physics, rearranged for FP32.
-//   T_l = W S_l W^+,  S_l = 1 + z1 P1 + z2 P2,  z_k = e^{-i omega_k L_l} - 1   (symmetric)
+//   T_l = W S_l W^+,  S_l = 1 + z1 u1 u1^T + z2 u2 u2^T,  z_k = e^{-i omega_k L_l} - 1,
+// with u_k the real unit eigenvectors of H0 + V e0 e0^T (S_l is complex symmetric), and
 //   A   = W (S_1..S_{M-1}) S_M (S_{M-1}..S_1) S_0 W^+ = W (B^T S_M B) S_0 W^+,
-// with B = S_{M-1}..S_1, because S_l^T = S_l.  That is M+1 complex 3x3 products per bin
-// instead of the reference's 2M-1, on symmetric factors.
+// with B = S_{M-1}..S_1, because S_l^T = S_l.  That is M+1 layer applications per bin
+// instead of the reference's 2M-1 products; each applies S as two rank-1 updates,
+// G += z_k u_k (u_k^T G), 96 FMA-pipe instructions against 132 for forming S and a
+// symmetric-by-general product.
 
 struct cs6 {  // complex symmetric 3x3
     cf a[6];
@@ -21,7 +24,13 @@ struct cg9 {  // complex general 3x3
     cf a[3][3];
 };
 
-// S = 1 + z1 P1 + z2 P2 from the two phase factors and the real projectors.
+// One layer in factored form.
+struct Layer {
+    float u[2][3];  // unit eigenvectors u1, u2
+    float z[2][2];  // z_k = e^{-i omega_k L} - 1 (re, im)
+};
+
+// S = 1 + z1 P1 + z2 P2 from the two phase factors and the real projectors (beam).
 __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1[6],
                                              const float P2[6], cs6& S) {
 #pragma unroll
@@ -32,31 +41,102 @@ __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1
     }
 }
 
-// t points at this bin's 64-byte table entry: P1[6], P2[6], omega_1 (hi, lo), omega_2.
-// kL2Only: load through L2 only (__ldcg), for tables written earlier in the same launch.
+// t points at this bin's 48-byte table entry: u1 (3), u2 (3), omega_1 (hi, lo), omega_2
+// (hi, lo), 2 unused.  kL2Only: load through L2 only (__ldcg), for tables written earlier in
+// the same launch.
 template <bool kL2Only = false>
-__device__ __forceinline__ void segment_matrix_mixed(const float* __restrict__ t, float2 L, cs6& S) {
+__device__ __forceinline__ void layer_from_table(const float* __restrict__ t, float2 L, Layer& f) {
     const float4* t4 = reinterpret_cast<const float4*>(t);
-    float4 a, b, c, w;
+    float4 a, b, c;
     if (kL2Only) {
         a = __ldcg(t4);
         b = __ldcg(t4 + 1);
         c = __ldcg(t4 + 2);
-        w = __ldcg(t4 + 3);
     } else {
         a = __ldg(t4);
         b = __ldg(t4 + 1);
         c = __ldg(t4 + 2);
-        w = __ldg(t4 + 3);
     }
-    const float P1[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
-    const float P2[6] = {b.z, b.w, c.x, c.y, c.z, c.w};
-    float z[2][2], lo;
-    float r = reduced_phase(w.x, w.y, L.x, L.y, lo);
-    unit_phase_minus_one(r, lo, z[0][0], z[0][1]);
-    r = reduced_phase(w.z, w.w, L.x, L.y, lo);
-    unit_phase_minus_one(r, lo, z[1][0], z[1][1]);
-    layer_matrix(z, P1, P2, S);
+    f.u[0][0] = a.x;
+    f.u[0][1] = a.y;
+    f.u[0][2] = a.z;
+    f.u[1][0] = a.w;
+    f.u[1][1] = b.x;
+    f.u[1][2] = b.y;
+    float lo;
+    float r = reduced_phase(b.z, b.w, L.x, L.y, lo);
+    unit_phase_minus_one(r, lo, f.z[0][0], f.z[0][1]);
+    r = reduced_phase(c.x, c.y, L.x, L.y, lo);
+    unit_phase_minus_one(r, lo, f.z[1][0], f.z[1][1]);
+}
+
+// The table entry of one (class, energy): eigenvectors and phase rates, three float4.
+__device__ __forceinline__ void store_table_entry(float* __restrict__ t, const float u[2][3],
+                                                  const float om[2][2]) {
+    float4* d = reinterpret_cast<float4*>(t);
+    d[0] = make_float4(u[0][0], u[0][1], u[0][2], u[1][0]);
+    d[1] = make_float4(u[1][1], u[1][2], om[0][0], om[0][1]);
+    d[2] = make_float4(om[1][0], om[1][1], 0.f, 0.f);
+}
+
+// G <- S G
+__device__ __forceinline__ void apply_left(const Layer& f, cg9& G) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float* u = f.u[k];
+        const float zr = f.z[k][0], zi = f.z[k][1];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            float wr = u[0] * G.a[0][j].re, wi = u[0] * G.a[0][j].im;
+            wr = fmaf(u[1], G.a[1][j].re, wr);
+            wi = fmaf(u[1], G.a[1][j].im, wi);
+            wr = fmaf(u[2], G.a[2][j].re, wr);
+            wi = fmaf(u[2], G.a[2][j].im, wi);
+            const float yr = fmaf(zr, wr, -zi * wi), yi = fmaf(zr, wi, zi * wr);
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                G.a[i][j].re = fmaf(u[i], yr, G.a[i][j].re);
+                G.a[i][j].im = fmaf(u[i], yi, G.a[i][j].im);
+            }
+        }
+    }
+}
+
+// G <- G S
+__device__ __forceinline__ void apply_right(const Layer& f, cg9& G) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float* u = f.u[k];
+        const float zr = f.z[k][0], zi = f.z[k][1];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            float wr = G.a[i][0].re * u[0], wi = G.a[i][0].im * u[0];
+            wr = fmaf(G.a[i][1].re, u[1], wr);
+            wi = fmaf(G.a[i][1].im, u[1], wi);
+            wr = fmaf(G.a[i][2].re, u[2], wr);
+            wi = fmaf(G.a[i][2].im, u[2], wi);
+            const float yr = fmaf(zr, wr, -zi * wi), yi = fmaf(zr, wi, zi * wr);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                G.a[i][j].re = fmaf(yr, u[j], G.a[i][j].re);
+                G.a[i][j].im = fmaf(yi, u[j], G.a[i][j].im);
+            }
+        }
+    }
+}
+
+// G = S = 1 + z1 u1 u1^T + z2 u2 u2^T
+__device__ __forceinline__ void layer_to_gen(const Layer& f, cg9& G) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+            const float p0 = f.u[0][i] * f.u[0][j], p1 = f.u[1][i] * f.u[1][j];
+            const cf v{fmaf(f.z[1][0], p1, fmaf(f.z[0][0], p0, i == j ? 1.0f : 0.0f)),
+                       fmaf(f.z[1][1], p1, f.z[0][1] * p0)};
+            G.a[i][j] = v;
+            G.a[j][i] = v;
+        }
 }
 
 // One Newton-Schulz step toward the nearest unitary matrix, A <- A (3 - A^+ A) / 2.  The
@@ -93,42 +173,6 @@ __device__ __forceinline__ void newton_schulz(cg9& A) {
             R.a[i][j] = acc;
         }
     A = R;
-}
-
-// R = S . G (S symmetric)
-__device__ __forceinline__ void mul_sg(const cs6& S, const cg9& G, cg9& R) {
-    cg9 t;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cf acc = cmulf(S.a[sidx(i, 0)], G.a[0][j]);
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                const cf s = S.a[sidx(i, k)], g = G.a[k][j];
-                acc.re = fmaf(s.re, g.re, fmaf(-s.im, g.im, acc.re));
-                acc.im = fmaf(s.re, g.im, fmaf(s.im, g.re, acc.im));
-            }
-            t.a[i][j] = acc;
-        }
-    R = t;
-}
-
-// R = G . S (S symmetric)
-__device__ __forceinline__ void mul_gs(const cg9& G, const cs6& S, cg9& R) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cf acc = cmulf(G.a[i][0], S.a[sidx(0, j)]);
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                const cf g = G.a[i][k], s = S.a[sidx(k, j)];
-                acc.re = fmaf(g.re, s.re, fmaf(-g.im, s.im, acc.re));
-                acc.im = fmaf(g.re, s.im, fmaf(g.im, s.re, acc.im));
-            }
-            R.a[i][j] = acc;
-        }
 }
 
 __device__ __forceinline__ void sym_to_gen(const cs6& S, cg9& G) {
@@ -174,34 +218,29 @@ CP3_HD WParams wparams(const OscParams& p) {
     return WParams{p.wf[0], p.wf[1], p.wf[2], p.wf[3]};
 }
 
-// One atmospheric bin over M+1 segments, generic in where each segment's layer matrix comes
-// from: seg(l, S) fills S for segment l (0 = air, then shells inwards).
+// One atmospheric bin over M+1 segments, generic in where each segment's layer comes from:
+// seg(l, F) fills F for segment l (0 = air, then shells inwards).
 template <class SegFn>
 __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WParams& w,
                                                      float* __restrict__ out, size_t plane) {
-    cs6 S0;
-    seg(0, S0);
     cg9 A2;
+    Layer F;
     if (M == 0) {
-        sym_to_gen(S0, A2);
+        seg(0, F);
+        layer_to_gen(F, A2);
     } else {
-        cs6 S;
-        cg9 B;
-        if (M == 1) {
-            seg(1, S);
-            sym_to_gen(S, B);  // B = S_1, Q = S_1
-            mul_gs(B, S0, A2);
-        } else {
-            seg(1, S);
-            sym_to_gen(S, B);
+        seg(1, F);
+        layer_to_gen(F, A2);  // B = S_1
+        if (M > 1) {
+            cg9& B = A2;
             for (int l = 2; l < M; l++) {
-                seg(l, S);
-                mul_sg(S, B, B);
+                seg(l, F);
+                apply_left(F, B);
             }
-            seg(M, S);
-            cg9 X;
-            mul_sg(S, B, X);  // X = S_M B
-            cs6 Q;            // Q = B^T X (symmetric)
+            seg(M, F);
+            cg9 X = B;
+            apply_left(F, X);  // X = S_M B
+            cs6 Q;             // Q = B^T X (symmetric)
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -215,9 +254,10 @@ __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WPa
                     }
                     Q.a[sidx(i, j)] = acc;
                 }
-            sym_to_gen(Q, B);
-            mul_gs(B, S0, A2);
+            sym_to_gen(Q, A2);
         }
+        seg(0, F);
+        apply_right(F, A2);  // ... S_0
     }
     newton_schulz(A2);
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
@@ -232,23 +272,22 @@ __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, s
                                                 const WParams& w, float* __restrict__ out,
                                                 size_t plane) {
     atmos_bin_mixed_with(
-        [&](int l, cs6& S) { segment_matrix_mixed<kL2Only>(tab + s_cls[l] * cls_stride, s_len[l], S); },
+        [&](int l, Layer& F) { layer_from_table<kL2Only>(tab + s_cls[l] * cls_stride, s_len[l], F); },
         M, w, out, plane);
 }
 
-// Layer matrix of a segment whose density is its own (quadratic density model): the
+// Layer of a segment whose density is its own (quadratic density model): the
 // eigen-decomposition is solved for this segment (double-float refined).
-__device__ __forceinline__ void segment_matrix_inline(const OscParams* __restrict__ p, double E,
-                                                      double rho_e, float2 L, cs6& S) {
-    float P[2][6], om[2][2], z[2][2];
-    rotated_eigen_mixed(p, E, rho_e, P, om);
+__device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict__ p, double E,
+                                                     double rho_e, float2 L, Layer& f) {
+    float om[2][2];
+    rotated_eigen_vectors(p, df_from(E), df_from(rho_e), f.u, om);
 #pragma unroll
     for (int k = 0; k < 2; k++) {
         float lo;
         const float r = reduced_phase(om[k][0], om[k][1], L.x, L.y, lo);
-        unit_phase_minus_one(r, lo, z[k][0], z[k][1]);
+        unit_phase_minus_one(r, lo, f.z[k][0], f.z[k][1]);
     }
-    layer_matrix(z, P[0], P[1], S);
 }
 
 // One beam energy (E, rho_e as double or float pair): eigen-decomposition (double-float

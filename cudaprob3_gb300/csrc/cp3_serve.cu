@@ -123,7 +123,7 @@ struct Request {
 struct Slot {
     struct cp3_server* owner = nullptr;
     cudaStream_t stream = nullptr;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};  // by launch kinds (1..3)
     DBuf<Problem> d_probs;
     DBuf<int> d_a, d_b;
     DBuf<Header> d_hdr;
@@ -289,7 +289,9 @@ void launch_slot(cp3_server* s, Slot& slot) {
     cudaMemcpyAsync(slot.d_a.ptr, slot.h_a.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(slot.d_b.ptr, slot.h_b.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(slot.d_hdr.ptr, slot.h_hdr.ptr, sizeof(Header), cudaMemcpyHostToDevice, st);
-    cudaGraphLaunch(slot.graph, st);
+    bool has_atmos = false, has_beam = false;
+    for (int i = 0; i < n; i++) (slot.h_probs.ptr[i].kind == 0 ? has_atmos : has_beam) = true;
+    cudaGraphLaunch(slot.graph[launch_kinds(has_atmos, has_beam)], st);
     slot.finished.store(0);
     slot.busy = true;
     cudaLaunchHostFunc(st, on_launch_done, &slot);
@@ -340,29 +342,34 @@ int capture_slot(cp3_server* s, Slot& sl) {
     S_CUDA(s, sl.h_hdr.alloc(1), "pinned");
     S_CUDA(s, sl.h_params.alloc(cap), "pinned");
     S_CUDA(s, cudaMemset(sl.d_status.ptr, 0, sizeof(int)), "memset");
-    int occ = 0;
-    S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kBlock, 0), "occupancy");
-    const int grid = std::max(1, s->sms * std::max(occ, 1));
     Args args{sl.d_hdr.ptr, sl.d_probs.ptr, sl.d_a.ptr, sl.d_b.ptr, sl.d_params.ptr,
               s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr, s->d_seg_cls.ptr,
               s->d_cls_rho.ptr, s->d_baselines.ptr, s->d_pool.ptr, s->d_pool.ptr,
               sl.d_done.ptr, sl.d_counter.ptr, sl.d_status.ptr};
-    cudaStream_t cs;
-    S_CUDA(s, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
-    cudaGraph_t g;
-    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, sizeof(unsigned int), cs);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_done.ptr, 0, sizeof(int) * cap, cs);
-    if (e == cudaSuccess) {
-        batch_kernel<<<grid, kBlock, 0, cs>>>(args);
-        e = cudaGetLastError();
+    // one graph per kernel instance; a launch replays the one for the kinds it holds
+    for (int kinds = 1; kinds <= 3; kinds++) {
+        void (*kern)(Args) = kinds == kAtmos ? batch_kernel<kAtmos>
+                             : kinds == kBeam ? batch_kernel<kBeam> : batch_kernel<kBoth>;
+        int occ = 0;
+        S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlock, 0), "occupancy");
+        const int grid = std::max(1, s->sms * std::max(occ, 1));
+        cudaStream_t cs;
+        S_CUDA(s, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+        cudaGraph_t g;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, sizeof(unsigned int), cs);
+        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_done.ptr, 0, sizeof(int) * cap, cs);
+        if (e == cudaSuccess) {
+            kern<<<grid, kBlock, 0, cs>>>(args);
+            e = cudaGetLastError();
+        }
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.graph[kinds], g, 0);
+        if (e2 == cudaSuccess) cudaGraphDestroy(g);
+        cudaStreamDestroy(cs);
+        if (e != cudaSuccess) return scuda(s, e, "graph capture");
     }
-    const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-    if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.graph, g, 0);
-    if (e2 == cudaSuccess) cudaGraphDestroy(g);
-    cudaStreamDestroy(cs);
-    if (e != cudaSuccess) return scuda(s, e, "graph capture");
     return CP3_OK;
 }
 
@@ -383,7 +390,8 @@ cp3_server::~cp3_server() {
     cudaSetDevice(device);
     for (Slot& sl : slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
-        if (sl.graph) cudaGraphExecDestroy(sl.graph);
+        for (cudaGraphExec_t gx : sl.graph)
+            if (gx) cudaGraphExecDestroy(gx);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
 }

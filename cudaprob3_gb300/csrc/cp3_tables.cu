@@ -7,6 +7,7 @@
 // bits where the eigen-system is ill-conditioned.  The table work is O(classes x energies),
 // amortised over every cosine, so the missing contraction costs nothing that matters.
 #include "cp3_device.cuh"
+#include "cp3_mixed.cuh"
 #include "cp3_kernels.hpp"
 
 namespace cp3 {
@@ -43,11 +44,11 @@ __global__ void __launch_bounds__(kTableBlock)
     for (int k = 0; k < 3; k++) t[(size_t)(54 + k) * ne_pad] = mm[k] - p.dm[0];
 }
 
-// Mixed table: real projectors P1, P2 of H0 + V e0 e0^T and the phase rates
-// omega_k = 2.534 (m_k - m_0) / E as float pairs (rotated_eigen_mixed: FP32 roots refined in
-// double-float; FP64 only where two roots nearly coincide).  One 64-byte entry per
-// (class c, energy e) at table[(c * ne_pad + e) * 16]: P1 (00,01,02,11,12,22), P2, then
-// omega_1 hi/lo, omega_2 hi/lo -- four 16-byte words a thread reads with vector loads.
+// Mixed table: real unit eigenvectors u1, u2 of H0 + V e0 e0^T (P_k = u_k u_k^T) and the
+// phase rates omega_k = 2.534 (m_k - m_0) / E as float pairs (rotated_eigen_vectors: FP32
+// roots refined in double-float; FP64 only where two roots nearly coincide).  One 48-byte
+// entry per (class c, energy e) at table[(c * ne_pad + e) * 12]: u1, u2, omega_1 hi/lo,
+// omega_2 hi/lo, 2 unused -- three 16-byte words a thread reads with vector loads.
 // Real = double (split on the device) or float2 (pairs split on the host: no FP64 at all).
 template <class Real>
 __global__ void __launch_bounds__(kTableBlock)
@@ -57,13 +58,9 @@ __global__ void __launch_bounds__(kTableBlock)
     const int ie = blockIdx.x * kTableBlock + threadIdx.x;
     const int c = blockIdx.y;
     if (ie >= ne) return;
-    float P[2][6], om[2][2];
-    rotated_eigen_mixed(&p, to_df(energies[ie]), to_df(cls_rho[c]), P, om);
-    float4* t = reinterpret_cast<float4*>(table + ((size_t)c * ne_pad + ie) * kMixFields);
-    t[0] = make_float4(P[0][0], P[0][1], P[0][2], P[0][3]);
-    t[1] = make_float4(P[0][4], P[0][5], P[1][0], P[1][1]);
-    t[2] = make_float4(P[1][2], P[1][3], P[1][4], P[1][5]);
-    t[3] = make_float4(om[0][0], om[0][1], om[1][0], om[1][1]);
+    float u[2][3], om[2][2];
+    rotated_eigen_vectors(&p, to_df(energies[ie]), to_df(cls_rho[c]), u, om);
+    store_table_entry(table + ((size_t)c * ne_pad + ie) * kMixFields, u, om);
 }
 
 // physics::calculate_beam (physics.hpp:1153-1260), one thread per energy; result [9][ne].

@@ -35,6 +35,7 @@ struct alignas(16) OscParams {
     // eigen-solver of the mixed kernels.
     float h0f[6][2];
     float cpolyf[5][2];
+    float h2f[6][2];     // H0^2 (00,01,02,11,12,22) as float pairs
     int order[3];        // root order from the vacuum cubic (prepare_getMfast)
     int anti;            // 1: antineutrino sign of the matter potential
     float wf[4];         // w rounded to float (the mixed kernels' W)

@@ -36,6 +36,30 @@ sys.path.insert(0, ROOT)
 N_TYPES = 2  # neutrino + antineutrino per step
 BATCH_SETS = 0  # --batch-sets: fewer parameter sets for the batched workloads (profiling)
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from one
+# ncu capture each, summarised under profiles/: (bytes, the captured launch's result bytes,
+# summary).  A launch of another size is scaled by its result bytes, since traffic is the
+# output stream plus a small table/descriptor read that grows with it.
+NCU_TRAFFIC = {
+    ("atmos59", "mixed"): (5.979904e6 + 85.276672e6, 144.0e6,
+                           "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
+    ("batch_atmos", "mixed"): (31.19872e6 + 897.908224e6, 912.332288e6,
+                               "profiles/batch_kernel_prem12_48problems.md"),
+    ("batch_beam", "mixed"): (105.65504e6 + 915.776512e6, 921.6e6,
+                              "profiles/batch_kernel_beam_128problems.md"),
+}
+
+
+def ncu_traffic(workload, prec, result_bytes):
+    """(traffic bytes of one launch of result_bytes, note) from the committed capture."""
+    t = NCU_TRAFFIC.get((workload, prec))
+    if t is None:
+        return None, None
+    note = f"ncu dram read+write of a captured launch with {t[1]:.4g} result bytes ({t[2]})"
+    if abs(result_bytes - t[1]) > 1:
+        note += ", scaled by result bytes"
+    return round(t[0] * result_bytes / t[1]), note
+
 
 def f_bin(M):
     """Canonical algorithmic flops of one (cos, E) bin crossing M shells: eigen-solve 40 +
@@ -153,7 +177,9 @@ def run_batch(args, w, rank, world):
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
                      "peak": round(peaks["fp32"], 3), "unit": "TFLOP/s",
-                     "frac": round(achieved / peaks["fp32"], 4), "traffic": None,
+                     "frac": round(achieved / peaks["fp32"], 4),
+                     "traffic": ncu_traffic(args.workload, "mixed", info["result_bytes"])[0],
+                     "traffic_note": ncu_traffic(args.workload, "mixed", info["result_bytes"])[1],
                      "kernel": "batch_kernel (one persistent launch per step)",
                      "flops_per_launch": flops,
                      "hbm_gbs_output": round(info["result_bytes"] / (t_ms * 1e-3) / 1e9, 1)},
@@ -500,7 +526,8 @@ def run_ours(args, rank, world):
         "peak": round(peak32 if prec == "mixed" else peaks.get("fp64"), 3),
         "unit": "TFLOP/s",
         "frac": round(achieved / (peak32 if prec == "mixed" else peaks.get("fp64")), 4),
-        "traffic": None,
+        "traffic": ncu_traffic(args.workload, prec, bytes_out_launch)[0],
+        "traffic_note": ncu_traffic(args.workload, prec, bytes_out_launch)[1],
         "peak_source": "live FMA-chain microbenchmark in this run (cp3_peaks.cu); the pool's "
                        "measured HBM/bf16 peaks do not apply to scalar FP pipes",
         "kernel": "atmos_mixed_kernel" if (w["kind"] == "atmos" and prec == "mixed") else

@@ -17,6 +17,8 @@ namespace cp3 {
 namespace batchk {
 
 constexpr int kTileE = 32;                  // energies per tile (one per lane)
+// Bin tiles read their problem's table, written by this launch's table tiles, from L2.
+constexpr int kTableLoad = kLoadL2;
 constexpr int kBlock = 128;                 // threads per block (4 independent warps)
 constexpr int kMaxRowsPerTile = 16;
 constexpr int kMaxBeamChunk = 64;
@@ -198,7 +200,7 @@ static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
                 }
                 __syncwarp();
                 if (e < P.ne)
-                    atmos_bin_mixed<true>(a.tables + P.tab_off + (size_t)e * kMixFields,
+                    atmos_bin_mixed<kTableLoad>(a.tables + P.tab_off + (size_t)e * kMixFields,
                                           (size_t)kMixFields * P.ne_pad, s_len[wid], s_cls[wid],
                                           nseg - 1, w, a.out + P.out_off + (size_t)ic * P.ne + e,
                                           (size_t)P.nrows * P.ne);

@@ -458,6 +458,39 @@ CP3_HD void orthonormalize_pair(T a[3], T b[3]) {
     }
 }
 
+// The FP64 branch of the mixed eigen-solver (the reference cubic), kept out of line: inlined,
+// the compiler may hoist part of it (the double conversions of E and rho) above the branch,
+// and on GB300's narrow FP64 pipe even one such instruction per call costs more than the
+// whole double-float path.  vectors: P[k][0..2] = u_k (orthonormalised), else projectors.
+__host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams* __restrict__ p,
+                                                                df Ed, df rhod, bool vectors,
+                                                                float P[2][6], float om[2][2]) {
+    double Pd[2][6], omd[2];
+    rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
+    for (int k = 0; k < 2; k++) {
+        if (vectors) {
+            const double d0 = Pd[k][0], d1 = Pd[k][3], d2 = Pd[k][5];
+            const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
+            const double c0 = j == 0 ? d0 : (j == 1 ? Pd[k][1] : Pd[k][2]);
+            const double c1 = j == 0 ? Pd[k][1] : (j == 1 ? d1 : Pd[k][4]);
+            const double c2 = j == 0 ? Pd[k][2] : (j == 1 ? Pd[k][4] : d2);
+            const double rs = 1.0 / sqrt(j == 0 ? d0 : (j == 1 ? d1 : d2));
+            Pd[k][0] = c0 * rs;  // u_k in place (the projector is no longer needed)
+            Pd[k][1] = c1 * rs;
+            Pd[k][2] = c2 * rs;
+        } else {
+            for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
+        }
+        om[k][0] = (float)omd[k];
+        om[k][1] = (float)(omd[k] - (double)om[k][0]);
+    }
+    if (vectors) {
+        orthonormalize_pair(Pd[0], Pd[1]);
+        for (int k = 0; k < 2; k++)
+            for (int i = 0; i < 3; i++) P[k][i] = (float)Pd[k][i];
+    }
+}
+
 // The mixed kernels' eigen-decomposition without FP64 on the common path:
 //   1. V = -fac (matter potential in 2E.H units, eV^2) and the cubic's coefficients in df64;
 //   2. the three roots from the trigonometric solution in FP32;
@@ -519,34 +552,7 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
     const float spread = fmaxf(fabsf(r[0].hi - r[1].hi), fmaxf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     const float gap = fminf(fabsf(r[0].hi - r[1].hi), fminf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     if (!(gap > 5e-3f * spread)) {
-        double Pd[2][6], omd[2];
-        rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            if (kVectors) {
-                const double d0 = Pd[k][0], d1 = Pd[k][3], d2 = Pd[k][5];
-                const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
-                const double c0 = j == 0 ? d0 : (j == 1 ? Pd[k][1] : Pd[k][2]);
-                const double c1 = j == 0 ? Pd[k][1] : (j == 1 ? d1 : Pd[k][4]);
-                const double c2 = j == 0 ? Pd[k][2] : (j == 1 ? Pd[k][4] : d2);
-                const double rs = 1.0 / sqrt(j == 0 ? d0 : (j == 1 ? d1 : d2));
-                Pd[k][0] = c0 * rs;  // u_k in place (the projector is no longer needed)
-                Pd[k][1] = c1 * rs;
-                Pd[k][2] = c2 * rs;
-            } else {
-#pragma unroll
-                for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
-            }
-            om[k][0] = (float)omd[k];
-            om[k][1] = (float)(omd[k] - (double)om[k][0]);
-        }
-        if (kVectors) {
-            orthonormalize_pair(Pd[0], Pd[1]);
-#pragma unroll
-            for (int k = 0; k < 2; k++)
-#pragma unroll
-                for (int i = 0; i < 3; i++) P[k][i] = (float)Pd[k][i];
-        }
+        eigen_fallback_f64(p, Ed, rhod, kVectors, P, om);
         return;
     }
     // H = H0 + V e0 e0^T and H^2 = H0^2 + V (e0 a^T + a e0^T) + V^2 e0 e0^T (a = H0 e0): only

@@ -41,14 +41,17 @@ __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1
     }
 }
 
+// How a kernel reads the eigen table: the read-only path (__ldg) for tables an earlier
+// launch wrote, L2 only (__ldcg) for tables written earlier in the same launch.
+enum TableLoad { kLoadReadOnly = 0, kLoadL2 = 1 };
+
 // t points at this bin's 48-byte table entry: u1 (3), u2 (3), omega_1 (hi, lo), omega_2
-// (hi, lo), 2 unused.  kL2Only: load through L2 only (__ldcg), for tables written earlier in
-// the same launch.
-template <bool kL2Only = false>
+// (hi, lo), 2 unused.
+template <int kLoad = kLoadReadOnly>
 __device__ __forceinline__ void layer_from_table(const float* __restrict__ t, float2 L, Layer& f) {
     const float4* t4 = reinterpret_cast<const float4*>(t);
     float4 a, b, c;
-    if (kL2Only) {
+    if (kLoad == kLoadL2) {
         a = __ldcg(t4);
         b = __ldcg(t4 + 1);
         c = __ldcg(t4 + 2);
@@ -259,20 +262,22 @@ __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WPa
         seg(0, F);
         apply_right(F, A2);  // ... S_0
     }
-    newton_schulz(A2);
+    // One or two FP32 layer matrices are unitary to ~1e-7 already; the correction pays off
+    // from the longer chains on (it removes the drift accumulated over ~2M products).
+    if (M >= 2) newton_schulz(A2);
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
 }
 
 // One atmospheric bin from the eigen table: the trajectory's segment lengths and classes are
 // in shared memory (s_len[0..M], s_cls[0..M]); tab points at this bin's energy column of the
 // table (entry of class c at tab + c * cls_stride); probabilities go to out[ch * plane].
-template <bool kL2Only = false>
+template <int kLoad = kLoadReadOnly>
 __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, size_t cls_stride,
                                                 const float2* s_len, const int* s_cls, int M,
                                                 const WParams& w, float* __restrict__ out,
                                                 size_t plane) {
     atmos_bin_mixed_with(
-        [&](int l, Layer& F) { layer_from_table<kL2Only>(tab + s_cls[l] * cls_stride, s_len[l], F); },
+        [&](int l, Layer& F) { layer_from_table<kLoad>(tab + s_cls[l] * cls_stride, s_len[l], F); },
         M, w, out, plane);
 }
 

@@ -19,56 +19,144 @@ constexpr int kBlock = 128;
 constexpr int kMaxGridY = 65535;
 
 // ------------------------------------------------------------------------------------
-// FP64: physics::calculate_atmos (physics.hpp:789-1150) for the fixed production height.
+// FP64: physics::calculate_atmos (physics.hpp:789-1150), within 1e-12 of the reference.
+//
+// The same physics as the reference in the rotated real basis of the mixed kernels
+// (cp3_mixed.cuh), in double precision: every layer is S = sum_k e^{i arg_k} P_k with the
+// reference's own phases arg_k = -2.534 dmMatVac[k][0] L / E (getArg, physics.hpp:439-450)
+// and the rotated-basis projectors P_k = u_k u_k^T; dropping the global phase e^{i arg_0},
+//   S ~ 1 + z1 u1 u1^T + z2 u2 u2^T,  z_k = e^{i arg_k} conj(e^{i arg_0}) - 1,
+// applied as two rank-1 updates, and the palindrome (physics.hpp:956-990) as
+// W (B^T S_M B) S_0 W^+ with B = S_{M-1}..S_1: M+1 layer applications instead of 2M-1
+// complex 3x3 products.  The phases are formed exactly as the reference forms them, so
+// their roundings -- which matter over ~120 layers of up to ~800 rad -- are the reference's.
 
 struct cm3 {
     cd a[3][3];
 };
 
-__device__ __forceinline__ void mul3(const cm3& A, const cm3& B, cm3& R) {
-    // math::multiply_complex_matrix (math.hpp:84-96): R = A . B, summed over k in order.
-    cm3 t;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            double re = 0.0, im = 0.0;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                re += A.a[i][k].re * B.a[k][j].re - A.a[i][k].im * B.a[k][j].im;
-                im += A.a[i][k].im * B.a[k][j].re + A.a[i][k].re * B.a[k][j].im;
-            }
-            t.a[i][j] = cd{re, im};
-        }
-    R = t;
-}
+// One FP64 layer in factored form.
+struct Layer64 {
+    double u[2][3];  // unit eigenvectors u1, u2 (rotated basis)
+    cd z[2];         // e^{i (arg_k - arg_0)} - 1, k = 1, 2
+};
 
-// T = sum_k e^{i arg_k} C_k for one segment (multiply_phase_matrix, math.hpp:59-75), with
-// arg_k = -2.534 dmMatVac[k][0] L / E evaluated as in getArg (physics.hpp:439-450).
-__device__ __forceinline__ void segment_matrix_f64(const double* __restrict__ t, int ne_pad,
-                                                   double L, double E, cm3& T) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) T.a[i][j] = cd{0.0, 0.0};
+// The phases of one layer from dmMatVac[k][0], as getArg and multiply_phase_matrix
+// (math.hpp:59-75) evaluate them; arg[] receives arg_k.
+__device__ __forceinline__ void layer64_phases(const double dmv[3], double L, double E,
+                                               Layer64& f, double arg[3]) {
+    double s[3], c[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const double dmv = __ldg(t + (size_t)(54 + k) * ne_pad);
-        double s, c;
-        sincos(-kLoEFac * dmv * L / E, &s, &c);
+        arg[k] = -kLoEFac * dmv[k] * L / E;
+        sincos(arg[k], &s[k], &c[k]);
+    }
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const double re = __ldg(t + (size_t)((k * 9 + q) * 2) * ne_pad);
-            const double im = __ldg(t + (size_t)((k * 9 + q) * 2 + 1) * ne_pad);
-            T.a[q / 3][q % 3].re += c * re - s * im;
-            T.a[q / 3][q % 3].im += c * im + s * re;
+    for (int kk = 0; kk < 2; kk++) {
+        const int k = kk + 1;
+        f.z[kk] = cd{c[k] * c[0] + s[k] * s[0] - 1.0, s[k] * c[0] - c[k] * s[0]};
+    }
+}
+
+// Table entry (10 doubles, five 16-byte words): u1, u2, dmMatVac[0..2][0], 1 unused.
+__device__ __forceinline__ void layer64_from_table(const double* __restrict__ t, double L,
+                                                   double E, Layer64& f, double arg[3]) {
+    const double2* t2 = reinterpret_cast<const double2*>(t);
+    const double2 a = __ldg(t2), b = __ldg(t2 + 1), c = __ldg(t2 + 2), d = __ldg(t2 + 3),
+                  e = __ldg(t2 + 4);
+    f.u[0][0] = a.x;
+    f.u[0][1] = a.y;
+    f.u[0][2] = b.x;
+    f.u[1][0] = b.y;
+    f.u[1][1] = c.x;
+    f.u[1][2] = c.y;
+    const double dmv[3] = {d.x, d.y, e.x};
+    layer64_phases(dmv, L, E, f, arg);
+}
+
+// G <- S G
+__device__ __forceinline__ void apply_left64(const Layer64& f, cm3& G) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const double* u = f.u[k];
+        const cd z = f.z[k];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const double wr = u[0] * G.a[0][j].re + u[1] * G.a[1][j].re + u[2] * G.a[2][j].re;
+            const double wi = u[0] * G.a[0][j].im + u[1] * G.a[1][j].im + u[2] * G.a[2][j].im;
+            const double yr = z.re * wr - z.im * wi, yi = z.re * wi + z.im * wr;
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                G.a[i][j].re += u[i] * yr;
+                G.a[i][j].im += u[i] * yi;
+            }
         }
+    }
+}
+
+// G <- G S
+__device__ __forceinline__ void apply_right64(const Layer64& f, cm3& G) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const double* u = f.u[k];
+        const cd z = f.z[k];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const double wr = G.a[i][0].re * u[0] + G.a[i][1].re * u[1] + G.a[i][2].re * u[2];
+            const double wi = G.a[i][0].im * u[0] + G.a[i][1].im * u[1] + G.a[i][2].im * u[2];
+            const double yr = wr * z.re - wi * z.im, yi = wr * z.im + wi * z.re;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                G.a[i][j].re += yr * u[j];
+                G.a[i][j].im += yi * u[j];
+            }
+        }
+    }
+}
+
+// G = S
+__device__ __forceinline__ void layer_to_gen64(const Layer64& f, cm3& G) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+            const double p0 = f.u[0][i] * f.u[0][j], p1 = f.u[1][i] * f.u[1][j];
+            const cd v{(i == j ? 1.0 : 0.0) + f.z[0].re * p0 + f.z[1].re * p1,
+                       f.z[0].im * p0 + f.z[1].im * p1};
+            G.a[i][j] = v;
+            G.a[j][i] = v;
+        }
+}
+
+// Flavour-basis amplitude A = W A2 W^+, W = [[1,0,0],[0,c,s e],[0,-s,c e]], e = e^{i d}.
+__device__ __forceinline__ void to_flavour64(const cm3& A2, const double* w, cm3& A) {
+    const double c = w[0], s = w[1], er = w[2], ei = w[3];
+    cm3 Y;  // A2 W^+
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const cd a1 = A2.a[i][1], a2 = A2.a[i][2];
+        const cd f{a2.re * er + a2.im * ei, a2.im * er - a2.re * ei};  // e* a2
+        Y.a[i][0] = A2.a[i][0];
+        Y.a[i][1] = cd{c * a1.re + s * f.re, c * a1.im + s * f.im};
+        Y.a[i][2] = cd{-s * a1.re + c * f.re, -s * a1.im + c * f.im};
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const cd y1 = Y.a[1][j], y2 = Y.a[2][j];
+        const cd g{y2.re * er - y2.im * ei, y2.re * ei + y2.im * er};  // e y2
+        A.a[0][j] = Y.a[0][j];
+        A.a[1][j] = cd{c * y1.re + s * g.re, c * y1.im + s * g.im};
+        A.a[2][j] = cd{-s * y1.re + c * g.re, -s * y1.im + c * g.im};
     }
 }
 
 // Production-height averaging (physics.hpp:997-1067), the reference's shift factors for the
 // pairs (k, q) = (1,0), (2,0), (2,1) and each initial flavour f: sf[pair][f] = sum over bins
 // of prob * sinc(d hw / 2) e^{i d hm}, d = darg0[k] - darg0[q]; the diagonal is 1.
+struct WParams64 {
+    double w[4];  // c23, s23, cos d, sin d
+};
+
 struct AvgInput {
     const double* prob;    // [2][3][ne][nc][nb]
     const double* shift;   // [nc][nb + 1] path-length shifts at the bin edges, cm
@@ -115,41 +203,49 @@ __device__ __forceinline__ void avg_shift_factors(const AvgInput& av, int ic, in
     }
 }
 
-// Probabilities from fin and the air layer's projectors (physics.hpp:1102-1130); with
-// averaging the cross terms carry the shift factors, without they carry 1 + 0i.
-template <class CatmFn>
-__device__ __forceinline__ void store_prob_f64(const cm3& fin, CatmFn catm, const cd (*sf)[3],
-                                               double* __restrict__ out, size_t plane) {
-    const int pair[3][3] = {{-1, -1, -1}, {0, -1, -1}, {1, 2, -1}};  // (k, q) -> index, q < k
+// With production-height averaging, the reference's probability (physics.hpp:1102-1130):
+// the amplitude split over the air layer's eigencomponents, Product_k = fin C_atm[k] =
+// W G P_k e_k W^+ (e_0 = 1 once the global phase is dropped), |Product_k|^2 summed and the
+// cross terms weighted by the shift factors sf.  The eigen labels are the reference's (the
+// FP64 layer data keep its mass order), so each pair (k, q) meets its own shift factor.
+// Out of line: it is the rare path and keeps its registers out of the common one.
+__device__ __noinline__ void finish_averaged64(const cm3& G, const Layer64& F0, const double* w,
+                                               const cd (*sf)[3], double* __restrict__ out,
+                                               size_t plane) {
+    cm3 Prod[3];
+    cm3 Y0 = G;
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+    for (int kk = 0; kk < 2; kk++) {
+        const double* u = F0.u[kk];
+        const cd e{1.0 + F0.z[kk].re, F0.z[kk].im};
+        cm3 Y;
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cd P[3];
+        for (int i = 0; i < 3; i++) {
+            const cd gu{G.a[i][0].re * u[0] + G.a[i][1].re * u[1] + G.a[i][2].re * u[2],
+                        G.a[i][0].im * u[0] + G.a[i][1].im * u[1] + G.a[i][2].im * u[2]};
+            const cd ge{gu.re * e.re - gu.im * e.im, gu.re * e.im + gu.im * e.re};
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                double re = 0.0, im = 0.0;
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    const cd c = catm(k, q, j);
-                    re += fin.a[i][q].re * c.re - fin.a[i][q].im * c.im;
-                    im += fin.a[i][q].im * c.re + fin.a[i][q].re * c.im;
-                }
-                P[k] = cd{re, im};
+            for (int j = 0; j < 3; j++) {
+                Y.a[i][j] = cd{ge.re * u[j], ge.im * u[j]};
+                Y0.a[i][j].re -= gu.re * u[j];
+                Y0.a[i][j].im -= gu.im * u[j];
             }
+        }
+        to_flavour64(Y, w, Prod[kk + 1]);
+    }
+    to_flavour64(Y0, w, Prod[0]);
+    const int pair[3][3] = {{-1, -1, -1}, {0, -1, -1}, {1, 2, -1}};  // (k, q) -> index, q < k
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
             double prob = 0.0;
-#pragma unroll
             for (int k = 0; k < 3; k++) {
-                prob += P[k].re * P[k].re + P[k].im * P[k].im;
-#pragma unroll
+                const cd Pk = Prod[k].a[i][j];
+                prob += Pk.re * Pk.re + Pk.im * Pk.im;
                 for (int q = 0; q < k; q++) {
-                    if (sf) {
-                        const cd t = sf[pair[k][q]][j];
-                        prob += 2. * P[q].re * P[k].re * t.re + 2. * P[q].im * P[k].im * t.re +
-                                2. * P[q].im * P[k].re * t.im - 2. * P[q].re * P[k].im * t.im;
-                    } else {
-                        prob += 2. * P[q].re * P[k].re + 2. * P[q].im * P[k].im;  // shift 1 + 0i
-                    }
+                    const cd Pq = Prod[q].a[i][j];
+                    const cd t = sf[pair[k][q]][j];
+                    prob += 2. * Pq.re * Pk.re * t.re + 2. * Pq.im * Pk.im * t.re +
+                            2. * Pq.im * Pk.re * t.im - 2. * Pq.re * Pk.im * t.im;
                 }
             }
             // Prob[i][j] (i final, j initial) is P(j -> i): channel j*3+i.
@@ -157,32 +253,67 @@ __device__ __forceinline__ void store_prob_f64(const cm3& fin, CatmFn catm, cons
         }
 }
 
-// T = sum_k e^{i arg_k} C_k for a segment of its own density (quadratic model): the
-// reference's per-segment getMfast + get_product + getC, then the same phase sum.
-__device__ __forceinline__ void segment_matrix_inline_f64(const OscParams* __restrict__ p, double E,
-                                                          double rho, double L, cm3& T) {
-    double mm[3];
-    matter_masses_f64(p, E, rho, mm);
-    cd C[3][3][3];
-    flavour_projectors_f64(p, E, rho, mm, C);
+// One FP64 bin over M+1 layers; seg(l, F, arg) fills layer l (0 = air) and its phases.
+template <class SegFn>
+__device__ __forceinline__ void atmos_bin_f64(SegFn seg, int M, const double* w,
+                                              const AvgInput& av, int ic, int nc, int ie, int ne,
+                                              double* __restrict__ out, size_t plane) {
+    cm3 G;
+    Layer64 F;
+    double arg[3];
+    if (M == 0) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) G.a[i][j] = cd{i == j ? 1.0 : 0.0, 0.0};
+    } else {
+        seg(1, F, arg);
+        layer_to_gen64(F, G);  // B = S_1
+        if (M > 1) {
+            for (int l = 2; l < M; l++) {
+                seg(l, F, arg);
+                apply_left64(F, G);
+            }
+            seg(M, F, arg);
+            cm3 X = G;
+            apply_left64(F, X);  // X = S_M B
+            cm3 Q;               // Q = B^T X (symmetric)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = i; j < 3; j++) {
+                    double re = 0.0, im = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        const cd b = G.a[k][i], x = X.a[k][j];
+                        re += b.re * x.re - b.im * x.im;
+                        im += b.re * x.im + b.im * x.re;
+                    }
+                    Q.a[i][j] = cd{re, im};
+                    Q.a[j][i] = cd{re, im};
+                }
+            G = Q;
+        }
+    }
+    seg(0, F, arg);  // the air layer, applied last: A2 = G S_0
+    if (av.nb > 0) {
+        cd sf[3][3];
+        avg_shift_factors(av, ic, nc, ie, ne, arg, sf);
+        finish_averaged64(G, F, w, sf, out, plane);
+        return;
+    }
+    apply_right64(F, G);
+    cm3 A;
+    to_flavour64(G, w, A);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) T.a[i][j] = cd{0.0, 0.0};
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        double s, c;
-        sincos(-kLoEFac * (mm[k] - p->dm[0]) * L / E, &s, &c);
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const cd v = C[k][q / 3][q % 3];
-            T.a[q / 3][q % 3].re += c * v.re - s * v.im;
-            T.a[q / 3][q % 3].im += c * v.im + s * v.re;
-        }
-    }
+        for (int j = 0; j < 3; j++)
+            out[(size_t)(j * 3 + i) * plane] = A.a[i][j].re * A.a[i][j].re + A.a[i][j].im * A.a[i][j].im;
 }
 
-// FP64 atmospheric bins, quadratic density: every segment carries its own density.
+// FP64 atmospheric bins, quadratic density: every segment carries its own density, so its
+// eigen-system is solved per segment (the reference's getMfast, then the rotated projectors).
 __global__ void __launch_bounds__(kBlock)
     atmos_f64_inline_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
                             int ne, const int* __restrict__ seg_off,
@@ -201,43 +332,21 @@ __global__ void __launch_bounds__(kBlock)
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
     const double E = energies[ie];
-    const int M = nseg - 1;
-    cm3 fin, mantle, T;
-    segment_matrix_inline_f64(&p, E, s_rho[0], s_len[0], fin);
-    for (int l = 1; l <= M; l++) {
-        segment_matrix_inline_f64(&p, E, s_rho[l], s_len[l], T);
-        mul3(T, fin, fin);
-        if (l < M) {
-            if (l == 1)
-                mantle = T;
-            else
-                mul3(mantle, T, mantle);
-        }
-    }
-    if (M >= 2) mul3(mantle, fin, fin);
-    double mm[3];
-    matter_masses_f64(&p, E, s_rho[0], mm);
-    cd Catm[3][3][3];
-    flavour_projectors_f64(&p, E, s_rho[0], mm, Catm);
-    auto catm = [&](int k, int q, int j) { return Catm[k][q][j]; };
-    double* o = out + (size_t)ic * ne + ie;
-    if (av.nb > 0) {
-        double arg0[3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) arg0[k] = -kLoEFac * (mm[k] - p.dm[0]) * s_len[0] / E;
-        cd sf[3][3];
-        avg_shift_factors(av, ic, nc, ie, ne, arg0, sf);
-        store_prob_f64(fin, catm, sf, o, (size_t)nc * ne);
-    } else {
-        store_prob_f64(fin, catm, (const cd(*)[3]) nullptr, o, (size_t)nc * ne);
-    }
+    atmos_bin_f64(
+        [&](int l, Layer64& F, double arg[3]) {
+            double dmv[3];
+            rotated_layer_f64(&p, E, s_rho[l], F.u, dmv);
+            layer64_phases(dmv, s_len[l], E, F, arg);
+        },
+        nseg - 1, p.w, av, ic, nc, ie, ne, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
 
 __global__ void __launch_bounds__(kBlock)
     atmos_f64_kernel(const double* __restrict__ energies, int ne, int ne_pad,
                      const double* __restrict__ table, const int* __restrict__ seg_off,
                      const double* __restrict__ seg_len, const int* __restrict__ seg_cls,
-                     int ic0, int nc, AvgInput av, double* __restrict__ out) {
+                     int ic0, int nc, const __grid_constant__ WParams64 w, AvgInput av,
+                     double* __restrict__ out) {
     __shared__ double s_len[kMaxSegments];
     __shared__ int s_cls[kMaxSegments];
     const int ic = ic0 + blockIdx.y;
@@ -252,40 +361,12 @@ __global__ void __launch_bounds__(kBlock)
     if (ie >= ne) return;
     const double E = energies[ie];
     const size_t cls_stride = (size_t)kF64Fields * ne_pad;
-    const double* tab = table + ie;
-    const int M = nseg - 1;
-
-    cm3 fin, mantle, T;
-    segment_matrix_f64(tab + s_cls[0] * cls_stride, ne_pad, s_len[0], E, fin);
-    for (int l = 1; l <= M; l++) {
-        segment_matrix_f64(tab + s_cls[l] * cls_stride, ne_pad, s_len[l], E, T);
-        mul3(T, fin, fin);
-        if (l < M) {
-            if (l == 1)
-                mantle = T;  // identity . T is exact
-            else
-                mul3(mantle, T, mantle);
-        }
-    }
-    if (M >= 2) mul3(mantle, fin, fin);
-
-    // Probabilities: Product_k = fin . C_atm[k] with the air layer's projectors from the table.
-    const double* ta = tab + s_cls[0] * cls_stride;
-    auto catm = [&](int k, int q, int j) {
-        return cd{__ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2) * ne_pad),
-                  __ldg(ta + (size_t)((k * 9 + q * 3 + j) * 2 + 1) * ne_pad)};
-    };
-    double* o = out + (size_t)ic * ne + ie;
-    if (av.nb > 0) {
-        double arg0[3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) arg0[k] = -kLoEFac * __ldg(ta + (size_t)(54 + k) * ne_pad) * s_len[0] / E;
-        cd sf[3][3];
-        avg_shift_factors(av, ic, nc, ie, ne, arg0, sf);
-        store_prob_f64(fin, catm, sf, o, (size_t)nc * ne);
-    } else {
-        store_prob_f64(fin, catm, (const cd(*)[3]) nullptr, o, (size_t)nc * ne);
-    }
+    const double* tab = table + (size_t)ie * kF64Fields;
+    atmos_bin_f64(
+        [&](int l, Layer64& F, double arg[3]) {
+            layer64_from_table(tab + s_cls[l] * cls_stride, s_len[l], E, F, arg);
+        },
+        nseg - 1, w.w, av, ic, nc, ie, ne, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
 
 // Mixed atmospheric bins (the physics of calculate_atmos rearranged for FP32: see
@@ -354,12 +435,13 @@ cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
     const AvgInput av{avg.prob, avg.shift, avg.air_cm, avg.n_bins, p.anti};
+    const WParams64 w{{p.w[0], p.w[1], p.w[2], p.w[3]}};
     const int end = rr.end < 0 ? n_cosines : rr.end;
     for (int ic0 = rr.begin; ic0 < end; ic0 += kMaxGridY) {
         const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_f64_kernel<<<grid, kBlock, 0, s>>>(energies, ne, ne_pad, table, seg_off, seg_len,
-                                                 seg_cls, ic0, n_cosines, av, out);
+                                                 seg_cls, ic0, n_cosines, w, av, out);
     }
     return cudaGetLastError();
 }

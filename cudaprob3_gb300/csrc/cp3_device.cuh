@@ -262,10 +262,10 @@ __host__ __device__ constexpr int sidx(int i, int j) {
 //   P_k = (H - m_a)(H - m_b) / ((m_k - m_a)(m_k - m_b)),  {a, b} = the other two,
 // (P_0 = 1 - P_1 - P_2), and the phase rates relative to eigenvalue 0 are
 //   omega_k = 2.534 (m_k - m_0) / E   [rad / km].
-CP3_HD void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
-                                                  double rho, double P[2][6], double om[2]) {
-    double mm[3];
-    matter_masses_f64(p, E, rho, mm);
+// Projectors P1, P2 (00,01,02,11,12,22) of the rotated H for the matter masses mm (in the
+// reference's mass order).
+CP3_HD void rotated_projectors_f64(const OscParams* __restrict__ p, double E, double rho,
+                                   const double mm[3], double P[2][6]) {
     const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
     double h[6];
 #pragma unroll
@@ -274,7 +274,7 @@ CP3_HD void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
 #pragma unroll
     for (int kk = 0; kk < 2; kk++) {
         const int k = kk + 1;
-        const int a = k == 1 ? 0 : 0;
+        const int a = 0;
         const int b = k == 1 ? 2 : 1;
         double A[6], B[6];
 #pragma unroll
@@ -298,8 +298,31 @@ CP3_HD void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
                 for (int m = 0; m < 3; m++) s += A[sidx(i, m)] * B[sidx(m, j)];
                 P[kk][sidx(i, j)] = s * inv;
             }
-        om[kk] = kLoEFac * (mm[k] - mm[0]) / E;
     }
+}
+
+CP3_HD void rotated_eigen_f64(const OscParams* __restrict__ p, double E,
+                                                  double rho, double P[2][6], double om[2]) {
+    double mm[3];
+    matter_masses_f64(p, E, rho, mm);
+    rotated_projectors_f64(p, E, rho, mm, P);
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++) om[kk] = kLoEFac * (mm[kk + 1] - mm[0]) / E;
+}
+
+// Unit vector u with P = u u^T from a rank-one projector P (sign arbitrary): the column j of
+// P with the largest diagonal, over sqrt(P[j][j]).
+template <class T>
+CP3_HD void projector_vector(const T P[6], T u[3]) {
+    const T d0 = P[0], d1 = P[3], d2 = P[5];
+    const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
+    const T c0 = j == 0 ? d0 : (j == 1 ? P[1] : P[2]);
+    const T c1 = j == 0 ? P[1] : (j == 1 ? d1 : P[4]);
+    const T c2 = j == 0 ? P[2] : (j == 1 ? P[4] : d2);
+    const T rs = (T)1 / sqrt(j == 0 ? d0 : (j == 1 ? d1 : d2));
+    u[0] = c0 * rs;
+    u[1] = c1 * rs;
+    u[2] = c2 * rs;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -458,6 +481,21 @@ CP3_HD void orthonormalize_pair(T a[3], T b[3]) {
     }
 }
 
+// FP64 layer data of one (density, energy) in the rotated basis: the unit eigenvectors u1,
+// u2 (P_k = u_k u_k^T, orthonormalised) and the reference's dmMatVac[k][0] = m_k - DM(0,0),
+// from which the phases are formed exactly as the reference forms them.
+CP3_HD void rotated_layer_f64(const OscParams* __restrict__ p, double E, double rho,
+                              double u[2][3], double dmv[3]) {
+    double mm[3], P[2][6];
+    matter_masses_f64(p, E, rho, mm);
+    rotated_projectors_f64(p, E, rho, mm, P);
+    projector_vector(P[0], u[0]);
+    projector_vector(P[1], u[1]);
+    orthonormalize_pair(u[0], u[1]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) dmv[k] = mm[k] - p->dm[0];
+}
+
 // The FP64 branch of the mixed eigen-solver (the reference cubic), kept out of line: inlined,
 // the compiler may hoist part of it (the double conversions of E and rho) above the branch,
 // and on GB300's narrow FP64 pipe even one such instruction per call costs more than the
@@ -469,15 +507,9 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
     rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
     for (int k = 0; k < 2; k++) {
         if (vectors) {
-            const double d0 = Pd[k][0], d1 = Pd[k][3], d2 = Pd[k][5];
-            const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
-            const double c0 = j == 0 ? d0 : (j == 1 ? Pd[k][1] : Pd[k][2]);
-            const double c1 = j == 0 ? Pd[k][1] : (j == 1 ? d1 : Pd[k][4]);
-            const double c2 = j == 0 ? Pd[k][2] : (j == 1 ? Pd[k][4] : d2);
-            const double rs = 1.0 / sqrt(j == 0 ? d0 : (j == 1 ? d1 : d2));
-            Pd[k][0] = c0 * rs;  // u_k in place (the projector is no longer needed)
-            Pd[k][1] = c1 * rs;
-            Pd[k][2] = c2 * rs;
+            double u[3];
+            projector_vector(Pd[k], u);
+            for (int i = 0; i < 3; i++) Pd[k][i] = u[i];  // u_k in place (P is no longer needed)
         } else {
             for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
         }

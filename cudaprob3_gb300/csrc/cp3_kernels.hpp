@@ -9,7 +9,8 @@
 namespace cp3 {
 
 // Fields of one (density class, energy) entry of the eigen tables.
-constexpr int kF64Fields = 57;  // C_k[a][b] re/im (54) + dmMatVac[k][0] (3)
+constexpr int kF64Fields = 10;  // u1 (3), u2 (3) rotated-basis unit eigenvectors,
+                                // dmMatVac[k][0] (3), 1 unused (one 80-byte entry)
 constexpr int kMixFields = 12;  // u1 (3), u2 (3) real unit eigenvectors; omega_1, omega_2
                                 // double-float; 2 unused (one 48-byte entry per (class, energy))
 

@@ -16,9 +16,10 @@ namespace {
 
 constexpr int kTableBlock = 128;
 
-// FP64 table: C_k (flavour basis) and dmMatVac[k][0] for T = sum_k C_k e^{i arg_k}
-// (physics.hpp:620-629 without the L-dependent phase).  SoA: field f of (class c, energy e)
-// at table[(c * kF64Fields + f) * ne_pad + e].
+// FP64 table: the rotated-basis unit eigenvectors u1, u2 (from the reference's getMfast
+// masses, physics.hpp:267-340, and the projectors of H0 + V e0 e0^T) and dmMatVac[k][0]
+// (physics.hpp:337-339), from which the bin kernel forms the reference's phases.  AoS: one
+// 80-byte entry per (class c, energy e) at table[(c * ne_pad + e) * 10].
 __global__ void __launch_bounds__(kTableBlock)
     table_f64_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
                      int ne, int ne_pad, const double* __restrict__ cls_rho,
@@ -26,22 +27,14 @@ __global__ void __launch_bounds__(kTableBlock)
     const int ie = blockIdx.x * kTableBlock + threadIdx.x;
     const int c = blockIdx.y;
     if (ie >= ne) return;
-    const double E = energies[ie];
-    const double rho = cls_rho[c];
-    double mm[3];
-    matter_masses_f64(&p, E, rho, mm);
-    cd C[3][3][3];
-    flavour_projectors_f64(&p, E, rho, mm, C);
-    double* t = table + (size_t)c * kF64Fields * ne_pad + ie;
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            t[(size_t)((k * 9 + q) * 2) * ne_pad] = C[k][q / 3][q % 3].re;
-            t[(size_t)((k * 9 + q) * 2 + 1) * ne_pad] = C[k][q / 3][q % 3].im;
-        }
-#pragma unroll
-    for (int k = 0; k < 3; k++) t[(size_t)(54 + k) * ne_pad] = mm[k] - p.dm[0];
+    double u[2][3], dmv[3];
+    rotated_layer_f64(&p, energies[ie], cls_rho[c], u, dmv);
+    double2* t = reinterpret_cast<double2*>(table + ((size_t)c * ne_pad + ie) * kF64Fields);
+    t[0] = make_double2(u[0][0], u[0][1]);
+    t[1] = make_double2(u[0][2], u[1][0]);
+    t[2] = make_double2(u[1][1], u[1][2]);
+    t[3] = make_double2(dmv[0], dmv[1]);
+    t[4] = make_double2(dmv[2], 0.0);
 }
 
 // Mixed table: real unit eigenvectors u1, u2 of H0 + V e0 e0^T (P_k = u_k u_k^T) and the

@@ -69,7 +69,29 @@ def f_bin(M):
     return 27.0 + 230.0 * (M + 1) + 216.0 * np.maximum(2 * M - 1, 0)
 
 
-def workload(name):
+def max_over_ranks(x, world, device):
+    """x maximised over the ranks of the process group (the step time of the slowest rank)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seed(seed, rank):
+    """Seed of a rank's shard: rank 0 keeps the configuration's own sets, the others draw
+    independent ones (weak scaling: every rank propagates different parameter sets)."""
+    return seed + 7919 * rank
+
+
+def rank_parameter_set(rank, world):
+    """The oscillation parameters a rank propagates in the single-grid workloads."""
+    from cudaprob3_gb300 import earth
+    return earth.NOMINAL if rank == 0 else earth.gaussian_sets(world, seed=77)[rank]
+
+
+def workload(name, rank=0):
     from cudaprob3_gb300 import earth
     if name == "atmos59":
         r, rho, ye = earth.synthetic_shells(59)
@@ -87,21 +109,31 @@ def workload(name):
                     desc="beam, rho=2.6 g/cm^3, L=1300 km, 1e5 E (0.1-10 GeV), nu+nubar")
     if name == "batch_atmos":
         n = BATCH_SETS or 256
-        sets = earth.gaussian_sets(n, seed=2024)
-        grids = earth.uneven_grids(n, seed=2025)
+        sets = earth.gaussian_sets(n, seed=rank_seed(2024, rank))
+        grids = earth.uneven_grids(n, seed=rank_seed(2025, rank))
         return dict(kind="batch", model=earth.PREM_12LAYER, h=22.0, sets=sets, grids=grids,
                     beam=None,
                     desc="batched atmospheric: 256 Gaussian parameter sets (half inverted "
                          "ordering), own grids n_cos U[100,1000] x n_E U[100,2000], PREM "
                          "12-layer, h=22 km, nu+nubar (512 problems), one persistent launch")
     if name == "batch_beam":
-        sets = earth.gaussian_sets(BATCH_SETS or 4096, seed=2026)
+        sets = earth.gaussian_sets(BATCH_SETS or 4096, seed=rank_seed(2026, rank))
         return dict(kind="batch", model=None, h=None, sets=sets, grids=None,
                     beam=dict(en=earth.lin_energy_grid(100000), rho=2.6, L=[295.0, 1300.0]),
                     desc="batched beam: 4096 Gaussian parameter sets (half inverted ordering), "
                          "1e5 E (0.1-10 GeV), rho=2.6, L=295 and 1300 km, nu+nubar "
                          "(8192 problems), one persistent launch")
+    if name == "serve":
+        return dict(kind="serve", desc="serving: 64 closed-loop chains, requests of atm 200^2, "
+                                       "500^2, 2000^2 and beam 1e4, 1e5 bins (PREM 4-layer)")
     raise SystemExit(f"unknown workload {name}")
+
+
+def problem_bins(w):
+    """Bins of each problem of a batched workload (nu and nubar share their grid)."""
+    if w["model"] is not None:
+        return [nc * ne for nc, ne in w["grids"]]
+    return [len(w["beam"]["en"]) * len(w["beam"]["L"])] * len(w["sets"])
 
 
 def build_batch(w):
@@ -110,6 +142,7 @@ def build_batch(w):
     b = Batch(0)
     flops = 0.0
     nbins = 0
+    params = []  # (problem id, parameter set, antineutrino)
     if w["model"] is not None:
         b.set_earth(*w["model"], w["h"])
         r = np.asarray(w["model"][0], dtype=np.float64)
@@ -122,6 +155,7 @@ def build_batch(w):
             for anti in (False, True):
                 pid = b.add_atmos(cz, en)
                 b.set_params(pid, m, anti)
+                params.append((pid, m, anti))
                 flops += float(f_bin(M).sum()) * ne
                 nbins += nc * ne
     else:
@@ -130,16 +164,17 @@ def build_batch(w):
             for anti in (False, True):
                 pid = b.add_beam(bw["en"], bw["rho"], bw["L"])
                 b.set_params(pid, m, anti)
+                params.append((pid, m, anti))
                 flops += float(f_bin(0)) * len(bw["en"]) * len(bw["L"])
                 nbins += len(bw["en"]) * len(bw["L"])
     b.commit()
-    return b, flops, nbins
+    return b, flops, nbins, params
 
 
 def run_batch(args, w, rank, world):
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
-    b, flops, nbins = build_batch(w)
+    b, flops, nbins, params = build_batch(w)
     t0 = time.perf_counter()
     b.tune(use_cache=True)
     tune_s = time.perf_counter() - t0
@@ -154,12 +189,29 @@ def run_batch(args, w, rank, world):
         for _ in range(args.steps):
             b.run()
             ms.append(b.synchronize())
-    t_ms = float(np.mean(ms))
-    if world > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    t_ms = max_over_ranks(float(np.mean(ms)), world, "cuda")
     probs = 9 * nbins
+
+    # end to end through the public API: every step uploads each problem's parameters
+    # (cp3_batch_set_params), runs, and downloads every result into page-locked host memory
+    # (one reused buffer of the largest result: the bytes cross the link all the same)
+    largest = max(9 * npb for npb in problem_bins(w))
+    host = torch.empty(largest, dtype=torch.float32, pin_memory=True)
+
+    def e2e_step():
+        for pid, m, anti in params:
+            b.set_params(pid, m, anti)
+        b.run()
+        for pid, _, _ in params:
+            b.copy_result_async(pid, host.data_ptr())
+        b.synchronize_stream()
+
+    e2e_steps = min(args.steps, 3)
+    e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, world, "cuda")
     peaks = fma_peaks(dev)
     achieved = flops / (t_ms * 1e-3) / 1e12
     info = b.info()
@@ -174,6 +226,10 @@ def run_batch(args, w, rank, world):
                    "tiles": info["tiles"], "result_bytes": info["result_bytes"],
                    "tile_shape": b.shape(), "autotune_s": round(tune_s, 2),
                    "l2": f"per-run output {info['result_bytes'] / 1e9:.1f} GB exceeds L2"},
+        "e2e": {"value": world * probs / (e2e_ms * 1e-3), "unit": "probabilities/s",
+                "h2d_bytes_per_step": len(params) * b.parameter_bytes(),
+                "d2h_bytes_per_step": info["result_bytes"], "ms_per_step": e2e_ms,
+                "steps": e2e_steps},
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
                      "peak": round(peaks["fp32"], 3), "unit": "TFLOP/s",
@@ -193,6 +249,8 @@ def run_batch(args, w, rank, world):
     if rank == 0:
         line["max_abs_err_vs_oracle"] = check_batch_against_oracle(w, b)
     line["clocks"] = clk.summary()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
     return line
 
 
@@ -389,7 +447,7 @@ def run_serve(args, rank, world):
         levels.append(lv)
     sat = levels[-1]
     srv.close()
-    return {
+    line = {
         "metric": "serving: probabilities/s at saturation (64 closed-loop chains), p50/p99 latency vs load",
         "value": sat["probabilities_per_s"], "unit": "probabilities/s", "n_gpus": world,
         "steps": len(levels), "warmup": 1, "ms_per_step": args.serve_seconds * 1e3,
@@ -401,6 +459,9 @@ def run_serve(args, rank, world):
         "latency_p99_atm500_at_saturation_ms": sat.get("atm500x500", {}).get("p99_ms"),
         "levels": levels,
     }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(workload("serve"), seconds=args.cpu_seconds)
+    return line
 
 
 def run_ours(args, rank, world):
@@ -411,12 +472,12 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     if args.workload == "serve":
         return run_serve(args, rank, world)
-    w = workload(args.workload)
+    w = workload(args.workload, rank)
     if w["kind"] == "batch":
         return run_batch(args, w, rank, world)
     prec = args.precision
     # weak scaling: each rank propagates its own parameter set over the full grid
-    m = earth.NOMINAL if rank == 0 else earth.gaussian_sets(world, seed=77)[rank]
+    m = rank_parameter_set(rank, world)
     props = []
     for knu in (1, -1):
         p = make_propagator(w, prec)
@@ -471,12 +532,9 @@ def run_ours(args, rank, world):
                 bins_ms.append(b)
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    t_ms = float(np.mean(step_ms))
+    t_ms = max_over_ranks(float(np.mean(step_ms)), world, "cuda")
     if world > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.barrier()
-        t_ms = float(tt.item())
     value = world * probs_step / (t_ms * 1e-3)
     kernel_ms = float(np.mean(bins_ms))
 
@@ -509,11 +567,7 @@ def run_ours(args, rank, world):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world, "cuda")
     h2d = (len(w["en"]) + (len(w["cz"]) if w["kind"] == "atmos" else 0)) * 8 * len(props)
     d2h = bytes_out_launch * len(props)
 
@@ -619,10 +673,11 @@ def cpu_sample(w, seconds, orc=None, nthreads=1):
     return dict(w, en=w["en"][:n]), f"{n} energies, nu+nubar"
 
 
-def cpu_run(w, orc, nthreads):
+def cpu_run(w, orc, nthreads, m=None):
+    """Probabilities/s of the C restatement on one single-grid workload, nu and nubar."""
     from cudaprob3_gb300 import earth
     from oracle.oracle import Mixing as OMix
-    m = earth.NOMINAL
+    m = m or earth.NOMINAL
     t0 = time.perf_counter()
     nbins = 0
     for anti, knu in ((False, 1), (True, -1)):
@@ -632,17 +687,66 @@ def cpu_run(w, orc, nthreads):
             orc.atmos(mix, anti, w["cz"], w["en"], r, rho, ye, w["h"], nthreads=nthreads)
             nbins += len(w["cz"]) * len(w["en"])
         else:
-            orc.beam(mix, anti, w["en"], w["rho"], w["L"], nthreads=nthreads)
-            nbins += len(w["en"])
+            for L in np.atleast_1d(w["L"]):
+                orc.beam(mix, anti, w["en"], w["rho"], float(L), nthreads=nthreads)
+                nbins += len(w["en"])
     return 9 * nbins / (time.perf_counter() - t0)
+
+
+def cpu_jobs(w, seconds, orc, nthreads):
+    """The CPU's share of a workload: (list of (single-grid workload, parameter set), text).
+    Single grids are sliced by cpu_sample; batched workloads take their first parameter sets
+    on their own grids, as many as fit about ``seconds``; serving takes 500 x 500 PREM-4
+    requests (the size its latency target is quoted for)."""
+    from cudaprob3_gb300 import earth
+    if w["kind"] in ("atmos", "beam"):
+        sw, desc = cpu_sample(w, seconds, orc, nthreads)
+        return [(sw, None)], desc
+    if w["kind"] == "serve":
+        req = dict(kind="atmos", model=earth.PREM_4LAYER, cz=earth.cosine_grid(500),
+                   en=earth.log_energy_grid(500), h=22.0)
+        sets = earth.gaussian_sets(64, seed=4242)
+        cands = [(req, m) for m in sets]
+        what = "500 x 500 PREM-4 requests, one parameter set each"
+    elif w["beam"] is not None:
+        bw = w["beam"]
+        cands = [(dict(kind="beam", en=bw["en"], rho=bw["rho"], L=bw["L"]), m) for m in w["sets"]]
+        what = "beam problems (1e5 energies, both baselines), one parameter set each"
+    else:
+        cands = [(dict(kind="atmos", model=w["model"], cz=earth.cosine_grid(nc),
+                       en=earth.log_energy_grid(ne), h=w["h"]), m)
+                 for m, (nc, ne) in zip(w["sets"], w["grids"])]
+        what = "atmospheric problems on their own grids, one parameter set each"
+    jobs, t0 = [], time.perf_counter()
+    for job in cands:  # the probe is the sample itself: stop once the budget is spent
+        cpu_run(job[0], orc, nthreads, job[1])
+        jobs.append(job)
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return jobs, f"the first {len(jobs)} {what}, nu+nubar"
+
+
+def job_probs(w):
+    """Probabilities of one single-grid job, nu and nubar."""
+    if w["kind"] == "atmos":
+        return 9 * N_TYPES * len(w["cz"]) * len(w["en"])
+    return 9 * N_TYPES * len(w["en"]) * len(np.atleast_1d(w["L"]))
+
+
+def run_jobs(jobs, orc, nthreads):
+    """Probabilities/s over a list of jobs (one pass)."""
+    t0 = time.perf_counter()
+    for w, m in jobs:
+        cpu_run(w, orc, nthreads, m)
+    return sum(job_probs(w) for w, _ in jobs) / (time.perf_counter() - t0)
 
 
 def cpu_baseline(w, seconds=2.0):
     from oracle.oracle import Oracle
     orc = Oracle(fast=True)
     cores = os.cpu_count() or 1
-    sample_w, desc = cpu_sample(w, seconds, orc, cores)  # the probe run also warms up
-    rate = cpu_run(sample_w, orc, cores)
+    jobs, desc = cpu_jobs(w, seconds, orc, cores)  # the sizing run also warms up
+    rate = run_jobs(jobs, orc, cores)
     return {"value": rate, "unit": "probabilities/s", "cores": cores, "kind": "port",
             "sample": desc + "; C restatement of the reference CpuPropagator<double> "
                              "(OpenMP over cosines, -O3), all host threads"}
@@ -654,16 +758,17 @@ def run_reference(args):
     w = workload(args.workload)
     orc = Oracle(fast=True)
     cores = os.cpu_count() or 1
-    sample_w, desc = cpu_sample(w, args.cpu_seconds, orc, cores)
-    for _ in range(args.warmup):
-        cpu_run(sample_w, orc, cores)
-    rates = [cpu_run(sample_w, orc, cores) for _ in range(args.steps)]
+    jobs, desc = cpu_jobs(w, args.cpu_seconds, orc, cores)
+    for _ in range(max(0, args.warmup - 1)):  # the sizing pass was the first warm-up
+        run_jobs(jobs, orc, cores)
+    rates = [run_jobs(jobs, orc, cores) for _ in range(args.steps)]
     value = float(np.median(rates))
+    probs_step = sum(job_probs(j) for j, _ in jobs)
     return {
         "impl": "reference",
         "metric": "oscillation probabilities/s (mixed precision, max err <= 1e-5 vs FP64 oracle)",
         "value": value, "unit": "probabilities/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 9 * N_TYPES * (len(sample_w["cz"]) * len(sample_w["en"]) if w["kind"] == "atmos" else len(sample_w["en"])) / value * 1e3,
+        "warmup": args.warmup, "ms_per_step": probs_step / value * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"],
                                         "sample": desc},

@@ -89,6 +89,11 @@ class Batch:
         self._check(self._lib.cp3_batch_synchronize(self._h, C.byref(ms)))
         return ms.value
 
+    @staticmethod
+    def parameter_bytes() -> int:
+        """Bytes a run uploads per problem (its parameter block)."""
+        return int(_abi.lib().cp3_batch_parameter_bytes())
+
     def info(self):
         n, bins, nbytes, tiles = C.c_int(), C.c_longlong(), C.c_size_t(), C.c_longlong()
         self._check(self._lib.cp3_batch_info(self._h, C.byref(n), C.byref(bins), C.byref(nbytes),

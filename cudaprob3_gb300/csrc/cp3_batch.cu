@@ -577,6 +577,8 @@ int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream) {
     return CP3_OK;
 }
 
+size_t cp3_batch_parameter_bytes(void) { return sizeof(OscParams); }
+
 int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins, size_t* result_bytes,
                    long long* tiles) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");

@@ -257,6 +257,9 @@ int cp3_batch_synchronize(cp3_batch* b, double* ms);
 int cp3_batch_result(cp3_batch* b, int id, const float** ptr, size_t* count);
 /* Asynchronous copy of one problem's result to dst (count floats) on `stream`. */
 int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream);
+/* Bytes of one problem's parameter block (what a run uploads per problem after
+ * cp3_batch_set_params). */
+size_t cp3_batch_parameter_bytes(void);
 int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins,
                    size_t* result_bytes, long long* tiles);
 

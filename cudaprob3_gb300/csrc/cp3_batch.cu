@@ -487,6 +487,9 @@ int cp3_batch_run(cp3_batch* b, void* stream) {
 
 int cp3_batch_synchronize(cp3_batch* b, double* ms) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    // everything queued on the batch's own stream, result copies included
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
     if (!b->timed) return CP3_OK;
     B_CUDA(b, cudaEventSynchronize(b->ev1), "synchronize");
     if (ms) {

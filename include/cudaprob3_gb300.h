@@ -251,7 +251,8 @@ int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_
 int cp3_batch_tune(cp3_batch* b, int use_cache);
 /* One run over every problem on `stream` (NULL = the batch's own stream). */
 int cp3_batch_run(cp3_batch* b, void* stream);
-/* Waits for the last run; *ms = its device time. */
+/* Waits for the last run and for everything queued on the batch's own stream (result
+ * copies with a NULL stream); *ms = the run's device time. */
 int cp3_batch_synchronize(cp3_batch* b, double* ms);
 /* Device pointer and float count of one problem's result. */
 int cp3_batch_result(cp3_batch* b, int id, const float** ptr, size_t* count);

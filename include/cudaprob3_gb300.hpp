@@ -205,4 +205,136 @@ public:
     CudaPropagatorSingle(int n_cosines_, int n_energies_) : CudaPropagatorSingle(0, n_cosines_, n_energies_) {}
 };
 
+// ---- additions with no reference counterpart: batches and the serving loop --------------
+
+// Many problems (own grids, own parameters) in one persistent launch (cp3_batch_*).
+class PropagatorBatch {
+public:
+    explicit PropagatorBatch(int device = 0) { check(cp3_batch_create(device, &b_)); }
+    ~PropagatorBatch() { cp3_batch_destroy(b_); }
+    PropagatorBatch(const PropagatorBatch&) = delete;
+    PropagatorBatch& operator=(const PropagatorBatch&) = delete;
+
+    void setEarth(const std::vector<double>& radii, const std::vector<double>& rho,
+                  const std::vector<double>& ye, double production_height_km) {
+        if (rho.size() != radii.size() || ye.size() != radii.size())
+            throw std::runtime_error("PropagatorBatch::setEarth. radii, rho and ye differ in size");
+        check(cp3_batch_set_earth(b_, radii.data(), rho.data(), ye.data(), (int)radii.size(),
+                                  production_height_km));
+    }
+    int addAtmospheric(const std::vector<double>& cosines, const std::vector<double>& energies) {
+        int id = -1;
+        check(cp3_batch_add_atmos(b_, cosines.data(), (int)cosines.size(), energies.data(),
+                                  (int)energies.size(), &id));
+        return id;
+    }
+    int addBeam(const std::vector<double>& energies, double rho,
+                const std::vector<double>& baselines_km) {
+        int id = -1;
+        check(cp3_batch_add_beam(b_, energies.data(), (int)energies.size(), rho,
+                                 baselines_km.data(), (int)baselines_km.size(), &id));
+        return id;
+    }
+    // setMNSMatrix + setNeutrinoMasses + the neutrino type of one problem.
+    void setParameters(int id, double theta12, double theta13, double theta23, double dcp,
+                       int kNuType, double dm12sq, double dm23sq, NeutrinoType type) {
+        check(cp3_batch_set_params(b_, id, theta12, theta13, theta23, dcp, kNuType, dm12sq,
+                                   dm23sq, type == Antineutrino ? CP3_ANTINEUTRINO : CP3_NEUTRINO));
+    }
+    void commit() { check(cp3_batch_commit(b_)); }
+    void tune(bool use_cache = true) { check(cp3_batch_tune(b_, use_cache ? 1 : 0)); }
+    void run(void* cuda_stream = nullptr) { check(cp3_batch_run(b_, cuda_stream)); }
+    double synchronize() {
+        double ms = 0.0;
+        check(cp3_batch_synchronize(b_, &ms));
+        return ms;
+    }
+    // Device result of one problem: atmospheric [9][n_cosines][n_energies], beam
+    // [n_baselines][9][n_energies] floats.
+    const float* deviceResult(int id, size_t* count = nullptr) {
+        const float* p = nullptr;
+        check(cp3_batch_result(b_, id, &p, count));
+        return p;
+    }
+    std::vector<float> result(int id) {
+        size_t n = 0;
+        deviceResult(id, &n);
+        std::vector<float> out(n);
+        check(cp3_batch_copy_result(b_, id, out.data(), nullptr));
+        synchronizeCopies();
+        return out;
+    }
+    cp3_batch* handle() { return b_; }
+
+private:
+    void check(int rc) {
+        if (rc != CP3_OK) throw std::runtime_error(cp3_batch_last_error(b_));
+    }
+    void synchronizeCopies() { check(cp3_batch_synchronize(b_, nullptr)); }  // the batch stream too
+    cp3_batch* b_ = nullptr;
+};
+
+// Continuous batching for many concurrent callers (cp3_server_*).
+class PropagatorServer {
+public:
+    PropagatorServer(int device, size_t pool_bytes, int max_batch = 256,
+                     long long max_bins_per_launch = 8000000) {
+        check(cp3_server_create(device, pool_bytes, max_batch, max_bins_per_launch, &s_));
+    }
+    ~PropagatorServer() { cp3_server_destroy(s_); }
+    PropagatorServer(const PropagatorServer&) = delete;
+    PropagatorServer& operator=(const PropagatorServer&) = delete;
+
+    void setEarth(const std::vector<double>& radii, const std::vector<double>& rho,
+                  const std::vector<double>& ye, double production_height_km) {
+        if (rho.size() != radii.size() || ye.size() != radii.size())
+            throw std::runtime_error("PropagatorServer::setEarth. radii, rho and ye differ in size");
+        check(cp3_server_set_earth(s_, radii.data(), rho.data(), ye.data(), (int)radii.size(),
+                                   production_height_km));
+    }
+    int addAtmosphericGrid(const std::vector<double>& cosines, const std::vector<double>& energies) {
+        int g = -1;
+        check(cp3_server_add_atmos_grid(s_, cosines.data(), (int)cosines.size(), energies.data(),
+                                        (int)energies.size(), &g));
+        return g;
+    }
+    int addBeamGrid(const std::vector<double>& energies, double rho,
+                    const std::vector<double>& baselines_km) {
+        int g = -1;
+        check(cp3_server_add_beam_grid(s_, energies.data(), (int)energies.size(), rho,
+                                       baselines_km.data(), (int)baselines_km.size(), &g));
+        return g;
+    }
+    void start() { check(cp3_server_start(s_)); }
+    unsigned long long submit(int grid, double theta12, double theta13, double theta23,
+                              double dcp, int kNuType, double dm12sq, double dm23sq,
+                              NeutrinoType type) {
+        unsigned long long id = 0;
+        check(cp3_server_submit(s_, grid, theta12, theta13, theta23, dcp, kNuType, dm12sq, dm23sq,
+                                type == Antineutrino ? CP3_ANTINEUTRINO : CP3_NEUTRINO, &id));
+        return id;
+    }
+    bool wait(unsigned long long id, double timeout_s) {
+        int done = 0;
+        check(cp3_server_wait(s_, id, timeout_s, &done));
+        return done != 0;
+    }
+    std::vector<float> result(unsigned long long id, double* latency_ms = nullptr) {
+        const float* p = nullptr;
+        size_t n = 0;
+        check(cp3_server_result(s_, id, &p, &n, latency_ms));
+        std::vector<float> out(n);
+        check(cp3_server_copy_result(s_, id, out.data()));
+        return out;
+    }
+    void release(unsigned long long id) { check(cp3_server_release(s_, id)); }
+    cp3_server* handle() { return s_; }
+
+private:
+    void check(int rc) {
+        if (rc != CP3_OK) throw std::runtime_error(cp3_server_last_error(s_));
+    }
+    cp3_server* s_ = nullptr;
+};
+
 }  // namespace cudaprob3linear

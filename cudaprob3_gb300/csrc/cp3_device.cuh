@@ -74,99 +74,6 @@ CP3_HD void matter_masses_f64(const OscParams* __restrict__ p, double E,
     }
 }
 
-// physics::get_product (physics.hpp:345-430) + getC (:459-514): the flavour-basis projectors
-// C[k][a][b] of the expansion T = sum_k C_k exp(i arg_k).
-CP3_HD void flavour_projectors_f64(const OscParams* __restrict__ p, double E,
-                                                       double rho, const double mm[3],
-                                                       cd C[3][3][3]) {
-    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
-    double dMV[3][3], dMM[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            dMM[i][j] = mm[i] - mm[j];
-            dMV[i][j] = mm[i] - CP3_DM(p, j, 0);
-        }
-    cd h[3][3][3];
-#pragma unroll
-    for (int n = 0; n < 3; n++)
-#pragma unroll
-        for (int m = 0; m < 3; m++) {
-            const cd a = CP3_U(p, 0, n), b = CP3_U(p, 0, m);
-            const double re = -fac * (a.re * b.re + a.im * b.im);
-            const double im = -fac * (a.re * b.im - a.im * b.re);
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                h[n][m][j].re = re;
-                h[n][m][j].im = im;
-            }
-        }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        h[0][0][j].re -= dMV[j][0];
-        h[1][1][j].re -= dMV[j][1];
-        h[2][2][j].re -= dMV[j][2];
-    }
-    const double den[3] = {dMM[0][1] * dMM[0][2], dMM[1][2] * dMM[1][0], dMM[2][0] * dMM[2][1]};
-    cd prod[3][3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) prod[i][j][k] = cd{0.0, 0.0};
-#pragma unroll
-            for (int q = 0; q < 3; q++)
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    const int f = (k + 1) % 3, s = (k + 2) % 3;
-                    const cd x = h[i][q][f], y = h[q][j][s];
-                    prod[i][j][k].re += x.re * y.re - x.im * y.im;
-                    prod[i][j][k].im += x.re * y.im + x.im * y.re;
-                }
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                prod[i][j][k].re /= den[k];
-                prod[i][j][k].im /= den[k];
-            }
-        }
-    // getC: C_k = U . prod_k . U^dagger, accumulated as RR/RI/IR/II partial sums.
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            double RR[3] = {0, 0, 0}, RI[3] = {0, 0, 0}, IR[3] = {0, 0, 0}, II[3] = {0, 0, 0};
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    const cd u = CP3_U(p, a, i);
-                    RR[j] += u.re * prod[i][j][k].re;
-                    RI[j] += u.re * prod[i][j][k].im;
-                    IR[j] += u.im * prod[i][j][k].re;
-                    II[j] += u.im * prod[i][j][k].im;
-                }
-#pragma unroll
-            for (int b = 0; b < 3; b++) {
-                double re = 0., im = 0.;
-#pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    const cd u = CP3_U(p, b, j);
-                    re += RR[j] * u.re;
-                    re += RI[j] * u.im;
-                    re += IR[j] * u.im;
-                    re -= II[j] * u.re;
-                    im += II[j] * u.im;
-                    im += IR[j] * u.re;
-                    im += RI[j] * u.re;
-                    im -= RR[j] * u.im;
-                }
-                C[k][a][b] = cd{re, im};
-            }
-        }
-}
-
 // physics::get_product + getA (physics.hpp:345-430, 516-598): the beam amplitude
 // A = U (sum_k e^{i arg_k} prod_k) U^dagger through AXFAC.  A[n][m]: row = final flavour.
 CP3_HD void beam_amplitude_f64(const OscParams* __restrict__ p, double E,

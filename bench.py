@@ -254,6 +254,81 @@ def run_batch(args, w, rank, world):
     return line
 
 
+def run_batch_fp64(args, w, rank, world):
+    """The batched workload through the plain FP64 kernels: one FP64 handle per problem
+    (created before the timed region), one launch each on one stream, timed with CUDA events
+    around the whole loop.  This is the like-for-like baseline of the mixed batch."""
+    import torch
+    from cudaprob3_gb300 import earth
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    props, flops, nbins = [], 0.0, 0
+    if w["model"] is not None:
+        r = np.asarray(w["model"][0], dtype=np.float64)
+        lim = -np.sqrt(1 - np.sort(r)[::-1] ** 2 / 6371.0 ** 2)
+        lim[0] = 0.0
+        for m, (nc, ne) in zip(w["sets"], w["grids"]):
+            cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
+            M = (cz[:, None] < lim[None, :]).sum(axis=1)
+            for knu in (1, -1):
+                p = make_propagator(dict(kind="atmos", cz=cz, en=en, model=w["model"], h=w["h"]),
+                                    "fp64")
+                set_params(p, m, knu)
+                props.append((p, 0 if knu == 1 else 1))
+                flops += float(f_bin(M).sum()) * ne
+                nbins += nc * ne
+    else:
+        # the first 512 sets (2048 handles, 15 GB of FP64 results): the rate does not depend
+        # on how many sets run, and the full 8192 x 2 handles would hold 118 GB
+        bw = w["beam"]
+        for m in w["sets"][:512]:
+            for knu in (1, -1):
+                for L in bw["L"]:
+                    p = make_propagator(dict(kind="beam", en=bw["en"], rho=bw["rho"], L=L), "fp64")
+                    set_params(p, m, knu)
+                    props.append((p, 0 if knu == 1 else 1))
+                    flops += float(f_bin(0)) * len(bw["en"])
+                    nbins += len(bw["en"])
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    def step():
+        for p, t in props:
+            p.calculate_async(t, sp)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    stream.synchronize()
+    steps = max(1, min(args.steps, 3))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    t_ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, "cuda")
+    probs = 9 * nbins
+    peaks = fma_peaks(dev)
+    return {
+        "metric": "oscillation probabilities/s, plain FP64 kernels (reference tolerance 1e-12)",
+        "value": world * probs / (t_ms * 1e-3), "unit": "probabilities/s", "n_gpus": world,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": t_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded parameter sets and grids)",
+        "config": {"workload": args.workload, "description": w["desc"], "precision": "fp64",
+                   "probabilities_per_step": probs, "problems": len(props),
+                   "launches": "one FP64 handle per problem, launched back to back on one stream",
+                   "l2": "per-run output exceeds L2"},
+        "gpu_launches": steps * len(props) * (2 if w["model"] is not None else 1),
+        "roofline": {"bound": "fp64", "achieved": round(flops / (t_ms * 1e-3) / 1e12, 3),
+                     "peak": round(peaks["fp64"], 3), "unit": "TFLOP/s",
+                     "frac": round(flops / (t_ms * 1e-3) / 1e12 / peaks["fp64"], 4),
+                     "traffic": None, "flops_per_launch": flops},
+        "peaks_tflops": peaks,
+        "clocks": clk.summary(),
+    }
+
+
 def check_batch_against_oracle(w, b, n_check=4):
     """A few problems of the timed batch against the CPU oracle."""
     from cudaprob3_gb300 import earth
@@ -474,6 +549,8 @@ def run_ours(args, rank, world):
         return run_serve(args, rank, world)
     w = workload(args.workload, rank)
     if w["kind"] == "batch":
+        if args.precision == "fp64":
+            return run_batch_fp64(args, w, rank, world)
         return run_batch(args, w, rank, world)
     prec = args.precision
     # weak scaling: each rank propagates its own parameter set over the full grid

@@ -512,6 +512,34 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
         const int k = kk + 1, a = 0, b = k == 1 ? 2 : 1;
         // (H - m_a)(H - m_b) = H^2 - (m_a + m_b) H + m_a m_b
         const df sab = df_add(r[a], r[b]), pab = df_mul(r[a], r[b]);
+        if (!kVectors) {
+            // Projectors (the beam): FP32 accuracy of P is what a single layer needs, and the
+            // numerator's cancellation (terms ~spread^2, result ~gap x spread) needs ~30 bits,
+            // not 48.  Compensated FP32: the large terms meet in one FMA (a TwoSum first on the
+            // diagonal, where H^2 and m_a m_b are both large), rounded once after the
+            // cancellation; the low words add in FP32.  ~2 ulp of P.
+            const df dka = df_sub(r[k], r[a]), dkb = df_sub(r[k], r[b]);
+            const float inv = 1.0f / ((dka.hi + dka.lo) * (dkb.hi + dkb.lo));
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                const bool diag = q == 0 || q == 3 || q == 5;
+                float sum = H2[q].hi, err = 0.0f;
+                if (diag) {  // TwoSum (Knuth): sum + err = H2.hi + pab.hi exactly
+                    sum = CP3_FADD(H2[q].hi, pab.hi);
+                    const float bb = CP3_FADD(sum, -H2[q].hi);
+                    err = CP3_FADD(CP3_FADD(H2[q].hi, -CP3_FADD(sum, -bb)), CP3_FADD(pab.hi, -bb));
+                }
+                const float lead = fmaf(-sab.hi, h[q].hi, sum);
+                float low = CP3_FADD(err, H2[q].lo);
+                if (diag) low = CP3_FADD(low, pab.lo);
+                low = fmaf(-sab.lo, h[q].hi, fmaf(-sab.hi, h[q].lo, low));
+                P[kk][q] = CP3_FADD(lead, low) * inv;
+            }
+            const df w = df_mul(dka, loe);  // a = 0: dka = m_k - m_0
+            om[kk][0] = w.hi;
+            om[kk][1] = w.lo;
+            continue;
+        }
         const df inv = df_recip(df_mul(df_sub(r[k], r[a]), df_sub(r[k], r[b])));
         df Pk[6];
 #pragma unroll
@@ -520,7 +548,7 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
             if (q == 0 || q == 3 || q == 5) n = df_add(n, pab);
             Pk[q] = df_mul(n, inv);
         }
-        if (kVectors) {
+        {
             // column j with the largest diagonal (>= 1/3), selected without indexing
             const float d0 = Pk[0].hi, d1 = Pk[3].hi, d2 = Pk[5].hi;
             const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
@@ -535,9 +563,6 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
             P[kk][0] = u0.hi + u0.lo;
             P[kk][1] = u1.hi + u1.lo;
             P[kk][2] = u2.hi + u2.lo;
-        } else {
-#pragma unroll
-            for (int q = 0; q < 6; q++) P[kk][q] = Pk[q].hi + Pk[q].lo;
         }
         const df w = df_mul(df_sub(r[k], r[0]), loe);
         om[kk][0] = w.hi;

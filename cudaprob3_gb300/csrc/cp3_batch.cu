@@ -523,7 +523,7 @@ int cp3_batch_tune(cp3_batch* b, int use_cache) {
         int rows, bps, bc;
     };
     // Only the dimensions the batch's problem kinds use are swept.
-    std::vector<int> rows = has_a ? std::vector<int>{1, 2, 4, 8} : std::vector<int>{2};
+    std::vector<int> rows = has_a ? std::vector<int>{1, 2, 4, 8, 16} : std::vector<int>{2};
     std::vector<int> chunks = has_b ? std::vector<int>{1, 4, 16} : std::vector<int>{4};
     std::vector<int> bps = {0};
     if (occ > 1) bps.push_back(std::max(1, occ / 2));

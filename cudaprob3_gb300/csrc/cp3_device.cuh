@@ -473,8 +473,11 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
     // t = 2 sqrt(m) cos(a) solves t^3 + P t + Q = 0 when cos(3a) = -Q / (2 m^{3/2})
     const float carg = fminf(1.0f, fmaxf(-1.0f, (-0.5f * qq) / (mp3 * rt)));
     const float th = acosf(carg) * (1.0f / 3.0f);
-    float l0 = fmaf(2.0f * rt, cosf(th), s);
-    float l1 = fmaf(2.0f * rt, cosf(th - 2.0943951f), s);
+    // cos(th - 2 pi/3) = -cos(th)/2 + (sqrt(3)/2) sin(th): one sincos for both roots
+    float sn, cn;
+    sincosf(th, &sn, &cn);
+    float l0 = fmaf(2.0f * rt, cn, s);
+    float l1 = fmaf(2.0f * rt, fmaf(0.8660254f, sn, -0.5f * cn), s);
     df r[3] = {df{l0, 0.0f}, df{l1, 0.0f}, df{0.0f, 0.0f}};
     // Newton steps: the residual in double-float, the derivative in FP32 (its relative error,
     // ~eps * spread / gap < 2e-5, only slows the quadratic convergence by that factor).

@@ -81,6 +81,7 @@ struct cp3_propagator {
     bool avg_dirty = true;
     DevBuf<float2> d_seg_len_df;
     DevBuf<double> d_table64;
+    DevBuf<double> d_plane;  // getProbabilityArr: one channel, transposed on the device
     DevBuf<float> d_table32;
     DevBuf<char> d_result;
     size_t result_bytes = 0;
@@ -651,8 +652,28 @@ int cp3_get_probability_arr(cp3_propagator* h, int t, double* out) {
     if (int rc = check_handle(h)) return rc;
     if (int rc = check_type(h, t)) return rc;
     if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");
+    if (!h->computed) return fail(h, CP3_ERR_NOT_SET, "no probabilities computed yet");
+    const size_t cells = (size_t)h->nc * h->ne;
+    if (!h->result_on_host) {
+        // the reference downloads all nine channels and reorders on the host
+        // (atmoscudapropagator.cu:222-257); here the one channel asked for is transposed on
+        // the device and only it crosses the link
+        CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+        CP3_CUDA(h, h->d_plane.reserve(cells), "allocate");
+        cudaStream_t s = h->last_stream ? h->last_stream : h->stream;
+        const bool is_float = h->precision == CP3_MIXED;
+        const char* src = h->d_result.ptr + (size_t)t * cells * (is_float ? sizeof(float) : sizeof(double));
+        const cudaError_t e = launch_plane_transpose(src, is_float, h->nc, h->ne, h->d_plane.ptr, s);
+        if (e == cudaSuccess) {
+            CP3_CUDA(h, cudaMemcpyAsync(out, h->d_plane.ptr, cells * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s), "copy channel");
+            CP3_CUDA(h, cudaStreamSynchronize(s), "synchronize");
+            return CP3_OK;
+        }
+        cudaGetLastError();  // a grid beyond the launch limits: reorder on the host instead
+    }
     if (int rc = fetch_result(h)) return rc;
-    const double* plane = h->h_result + (size_t)t * h->nc * h->ne;
+    const double* plane = h->h_result + (size_t)t * cells;
     size_t it = 0;
     for (int ie = 0; ie < h->ne; ie++)
         for (int ic = 0; ic < h->nc; ic++) out[it++] = plane[(size_t)ic * h->ne + ie];

@@ -484,6 +484,37 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
     return cudaGetLastError();
 }
 
+// One channel plane [nc][ne] of a result, transposed to [ne][nc] doubles (the layout of
+// getProbabilityArr, atmoscudapropagator.cu:238-257): 32 x 32 tiles through shared memory,
+// coalesced on both sides.
+template <class T>
+__global__ void __launch_bounds__(32 * 8)
+    plane_transpose_kernel(const T* __restrict__ src, int nc, int ne, double* __restrict__ dst) {
+    __shared__ double tile[32][33];
+    const int e0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int c = c0 + k, e = e0 + threadIdx.x;
+        if (c < nc && e < ne) tile[k][threadIdx.x] = (double)src[(size_t)c * ne + e];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int e = e0 + k, c = c0 + threadIdx.x;
+        if (c < nc && e < ne) dst[(size_t)e * nc + c] = tile[threadIdx.x][k];
+    }
+}
+
+cudaError_t launch_plane_transpose(const void* src, bool is_float, int nc, int ne, double* dst,
+                                   cudaStream_t s) {
+    if (nc <= 0 || ne <= 0) return cudaSuccess;
+    const dim3 grid((ne + 31) / 32, (nc + 31) / 32), block(32, 8);
+    if (grid.y > 65535) return cudaErrorInvalidValue;
+    if (is_float)
+        plane_transpose_kernel<float><<<grid, block, 0, s>>>((const float*)src, nc, ne, dst);
+    else
+        plane_transpose_kernel<double><<<grid, block, 0, s>>>((const double*)src, nc, ne, dst);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_beam_mixed(const OscParams& p, const float2* energies, int ne, double rho_e,
                               double L_km, float* out, cudaStream_t s) {
     if (ne <= 0) return cudaSuccess;

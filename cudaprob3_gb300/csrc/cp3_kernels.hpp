@@ -56,6 +56,10 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
                                 int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s,
                                 RowRange rr = RowRange{});
 
+// One channel plane [nc][ne] (float or double) transposed to [ne][nc] doubles.
+cudaError_t launch_plane_transpose(const void* src, bool is_float, int nc, int ne, double* dst,
+                                   cudaStream_t s);
+
 // Beam bins: rho_e = rho * 0.5 (electron density), L in km.
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,
                             double L_km, double* out, cudaStream_t s);

@@ -172,3 +172,31 @@ def test_calculate_to_host_beam():
     b.calculate_to_host_async(NeutrinoType.Neutrino, host.data_ptr())
     b.synchronize()
     assert np.array_equal(host.numpy().reshape(want.shape), want)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_probability_arr_device_and_host_paths_agree(prec):
+    nc, ne = 67, 45
+    p = configured(nc=nc, ne=ne, prec=prec)
+    p.calculateProbabilities(NeutrinoType.Antineutrino)
+    res = p.result().astype(np.float64)
+    for t in (ProbType.e_e, ProbType.m_e, ProbType.t_t):
+        dev = p.getProbabilityArr(t)  # nothing on the host yet: the device transpose
+        assert np.array_equal(dev, res[t].T.ravel())
+    p.getProbability(0, 0, ProbType.e_e)  # downloads the whole result
+    for t in (ProbType.m_m, ProbType.e_t):
+        host = p.getProbabilityArr(t)
+        assert np.array_equal(host, res[t].T.ravel())
+
+
+def test_probability_arr_beam():
+    ne = 333
+    b = BeamCudaPropagatorSingle(0, ne, 1, precision="mixed")
+    b.setEnergyList(earth.lin_energy_grid(ne))
+    b.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, 1)
+    b.setNeutrinoMasses(NOM.dm12sq, NOM.dm23sq)
+    b.setDensity(2.6)
+    b.setPathLength(810.0)
+    b.calculateProbabilities(NeutrinoType.Neutrino)
+    res = b.result().astype(np.float64)
+    assert np.array_equal(b.getProbabilityArr(ProbType.m_e), res[ProbType.m_e])

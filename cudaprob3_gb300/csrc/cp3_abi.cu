@@ -77,7 +77,9 @@ struct cp3_propagator {
     DevBuf<float2> d_energies_df, d_cls_rho_df;  // mixed kernels: (hi, lo) pairs split here
     DevBuf<int> d_seg_off, d_seg_cls;
     DevBuf<double> d_seg_len, d_cls_rho, d_seg_rho;
-    DevBuf<double> d_ph_prob, d_ph_shift, d_air_cm;  // production-height averaging
+    DevBuf<double> d_ph_prob, d_ph_shift, d_air_cm;  // production-height averaging (FP64)
+    DevBuf<float> d_ph_prob_f, d_ph_hw;              // ... and its float form (mixed)
+    DevBuf<float2> d_ph_hm;
     bool avg_dirty = true;
     DevBuf<float2> d_seg_len_df;
     DevBuf<double> d_table64;
@@ -239,8 +241,45 @@ int prepare_atmos(cp3_propagator* h) {
 
 // Averaging inputs: the client's probabilities and, per cosine, the path-length shifts at the
 // bin edges and the air segment in cm (the reference's `dist` of layer 0).
-int prepare_averaging(cp3_propagator* h, AvgArrays* av) {
+int prepare_averaging(cp3_propagator* h, AvgArrays* av, AvgMixed* avm) {
     if (h->avg_bins == 0) return CP3_OK;
+    if (h->avg_dirty && h->precision == CP3_MIXED) {
+        // float probabilities; per (cosine, bin) the mid shift as a float pair and the width,
+        // both in km (the phase rates are per km); zero where the air segment is zero, as the
+        // reference's d0 = 0 there (physics.hpp:1030-1034)
+        std::vector<double> shifts;
+        production_height_shifts(h->cosines.data(), h->nc, h->height_cm, h->avg_edges.data(),
+                                  h->avg_bins, &shifts);
+        const int nb = h->avg_bins;
+        std::vector<float> prob(h->avg_prob.begin(), h->avg_prob.end()), hw((size_t)h->nc * nb);
+        std::vector<float2> hm((size_t)h->nc * nb);
+        for (int ic = 0; ic < h->nc; ic++)
+            for (int b = 0; b < nb; b++) {
+                const double h0 = shifts[(size_t)ic * (nb + 1) + b], h1 = shifts[(size_t)ic * (nb + 1) + b + 1];
+                const bool zero = h->traj.air_cm[ic] == 0.0;
+                const double mid_km = zero ? 0.0 : 0.5 * (h1 + h0) / kKm2Cm;
+                const float mh = (float)mid_km;
+                hm[(size_t)ic * nb + b] = make_float2(mh, (float)(mid_km - (double)mh));
+                hw[(size_t)ic * nb + b] = zero ? 0.0f : (float)((h1 - h0) / kKm2Cm);
+            }
+        CP3_CUDA(h, h->d_ph_prob_f.reserve(prob.size()), "allocate averaging");
+        CP3_CUDA(h, h->d_ph_hm.reserve(hm.size()), "allocate averaging");
+        CP3_CUDA(h, h->d_ph_hw.reserve(hw.size()), "allocate averaging");
+        CP3_CUDA(h, cudaMemcpy(h->d_ph_prob_f.ptr, prob.data(), sizeof(float) * prob.size(),
+                               cudaMemcpyHostToDevice), "upload averaging");
+        CP3_CUDA(h, cudaMemcpy(h->d_ph_hm.ptr, hm.data(), sizeof(float2) * hm.size(),
+                               cudaMemcpyHostToDevice), "upload averaging");
+        CP3_CUDA(h, cudaMemcpy(h->d_ph_hw.ptr, hw.data(), sizeof(float) * hw.size(),
+                               cudaMemcpyHostToDevice), "upload averaging");
+        h->avg_dirty = false;
+    }
+    if (h->precision == CP3_MIXED) {
+        avm->prob = h->d_ph_prob_f.ptr;
+        avm->hm = h->d_ph_hm.ptr;
+        avm->hw = h->d_ph_hw.ptr;
+        avm->nb = h->avg_bins;
+        return CP3_OK;
+    }
     if (h->avg_dirty) {
         std::vector<double> shifts;
         production_height_shifts(h->cosines.data(), h->nc, h->height_cm, h->avg_edges.data(),
@@ -288,15 +327,16 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
         if (!h->height_set)
             return fail(h, CP3_ERR_NOT_SET,
                         "CudaPropagatorSingle::calculateProbabilities. production height was not set");
-        if (h->avg_bins > 0 && h->precision != CP3_FP64)
+        if (h->avg_bins > 0 && h->precision != CP3_FP64 && h->model.poly)
             return fail(h, CP3_ERR_UNSUPPORTED,
-                        "production-height averaging runs on the FP64 kernels (create the handle with CP3_FP64)");
+                        "production-height averaging with a quadratic density model runs on the FP64 kernels (create the handle with CP3_FP64)");
         const bool traj_was_dirty = h->traj_dirty;
         int rc = prepare_atmos(h);
         if (rc) return rc;
         if (traj_was_dirty) h->avg_dirty = true;
         AvgArrays av;
-        rc = prepare_averaging(h, &av);
+        AvgMixed avm;
+        rc = prepare_averaging(h, &av, &avm);
         if (rc) return rc;
         mark(0);
         const bool mixed = h->precision == CP3_MIXED;
@@ -315,6 +355,10 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
                                            mixed ? (const void*)h->d_seg_len_df.ptr
                                                  : (const void*)h->d_seg_len.ptr,
                                            h->d_seg_rho.ptr, h->nc, av, h->d_result.ptr, s, rr);
+            if (mixed && avm.nb > 0)
+                return launch_atmos_mixed_avg(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
+                                              h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc, avm,
+                                              (float*)h->d_result.ptr, s, rr);
             if (mixed)
                 return launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
                                           h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc,

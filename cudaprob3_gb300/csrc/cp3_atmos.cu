@@ -484,6 +484,172 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------------------------
+// Mixed atmospheric bins with production-height averaging (physics.hpp:997-1130): the
+// amplitude split over the air layer's eigencomponents as in finish_averaged64, in FP32,
+// with the shift factors' phases reduced in double-float (d hm reaches hundreds of rad).
+
+__device__ __forceinline__ float sinc_reference_f(float x) {
+    // math::defined_sinc (math.hpp:49-55) as the reference evaluates it (int abs: the series
+    // branch for every |x| < 1)
+    if (fabsf(x) >= 1.0f) return sinf(x) / x;
+    return 1.0f - x * x / 6.0f + x * x * x * x / 120.0f;
+}
+
+// Flavour-basis amplitude A = W A2 W^+ in FP32 (the transform of store_probabilities).
+__device__ __forceinline__ void to_flavour_f32(const cg9& A2, const WParams& w, cg9& A) {
+    cg9 Y;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const cf a1 = A2.a[i][1], a2 = A2.a[i][2];
+        const cf f{a2.re * w.er + a2.im * w.ei, a2.im * w.er - a2.re * w.ei};  // e* a2
+        Y.a[i][0] = A2.a[i][0];
+        Y.a[i][1] = cf{fmaf(w.c, a1.re, w.s * f.re), fmaf(w.c, a1.im, w.s * f.im)};
+        Y.a[i][2] = cf{fmaf(-w.s, a1.re, w.c * f.re), fmaf(-w.s, a1.im, w.c * f.im)};
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const cf y1 = Y.a[1][j], y2 = Y.a[2][j];
+        const cf g{y2.re * w.er - y2.im * w.ei, y2.re * w.ei + y2.im * w.er};  // e y2
+        A.a[0][j] = Y.a[0][j];
+        A.a[1][j] = cf{fmaf(w.c, y1.re, w.s * g.re), fmaf(w.c, y1.im, w.s * g.im)};
+        A.a[2][j] = cf{fmaf(-w.s, y1.re, w.c * g.re), fmaf(-w.s, y1.im, w.c * g.im)};
+    }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    atmos_mixed_avg_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
+                           const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
+                           const int* __restrict__ seg_cls, int ic0, int nc, AvgMixed av,
+                           float* __restrict__ out) {
+    __shared__ float2 s_len[kMaxSegments];
+    __shared__ int s_cls[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) {
+        s_len[i] = seg_len[s0 + i];
+        s_cls[i] = seg_cls[s0 + i];
+    }
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const float* tab = table + (size_t)ie * kMixFields;
+    const size_t cls_stride = (size_t)kMixFields * ne_pad;
+    const int M = nseg - 1;
+    auto seg = [&](int l, Layer& F) { layer_from_table(tab + s_cls[l] * cls_stride, s_len[l], F); };
+    cg9 G;
+    if (M == 0) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) G.a[i][j] = cf{i == j ? 1.0f : 0.0f, 0.0f};
+    } else {
+        chain_mixed(seg, M, G);
+        if (M >= 2) newton_schulz(G);
+    }
+    Layer F0;
+    const float* t0 = tab + s_cls[0] * cls_stride;
+    layer_from_table(t0, s_len[0], F0);
+
+    // shift factors of the pairs (1,0), (2,0), (2,1): the reference's d = d0[k] - d0[q] is
+    // -(omega_k - omega_q) per km of path-length shift (omega_0 = 0)
+    const df om1{__ldg(t0 + 6), __ldg(t0 + 7)}, om2{__ldg(t0 + 8), __ldg(t0 + 9)};
+    const df dom[3] = {om1, om2, df_sub(om2, om1)};
+    cf sf[3][3];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int f = 0; f < 3; f++) sf[q][f] = cf{0.0f, 0.0f};
+    for (int b = 0; b < av.nb; b++) {
+        const float2 hm = av.hm[(size_t)ic * av.nb + b];
+        const float hw = av.hw[(size_t)ic * av.nb + b];
+        float pr[3];
+#pragma unroll
+        for (int f = 0; f < 3; f++)
+            pr[f] = av.prob[((((size_t)av.type * 3 + f) * ne + ie) * nc + ic) * av.nb + b];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            float lo;
+            const float r = reduced_phase(dom[q].hi, dom[q].lo, -hm.x, -hm.y, lo);  // d hm
+            float er, ei;
+            unit_phase_minus_one(-r, -lo, er, ei);  // e^{i d hm} - 1
+            er += 1.0f;
+            const float sc = sinc_reference_f(-0.5f * dom[q].hi * hw);
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                sf[q][f].re = fmaf(pr[f] * sc, er, sf[q][f].re);
+                sf[q][f].im = fmaf(pr[f] * sc, ei, sf[q][f].im);
+            }
+        }
+    }
+
+    // Product_k = W G P_k e_k W^+, k = 0 (the rest), 1, 2
+    cg9 Pr[3], Y0 = G;
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++) {
+        const float* u = F0.u[kk];
+        const cf e{1.0f + F0.z[kk][0], F0.z[kk][1]};
+        cg9 Y;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const cf gu{fmaf(G.a[i][0].re, u[0], fmaf(G.a[i][1].re, u[1], G.a[i][2].re * u[2])),
+                        fmaf(G.a[i][0].im, u[0], fmaf(G.a[i][1].im, u[1], G.a[i][2].im * u[2]))};
+            const cf ge = cmulf(gu, e);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                Y.a[i][j] = cf{ge.re * u[j], ge.im * u[j]};
+                Y0.a[i][j].re = fmaf(-gu.re, u[j], Y0.a[i][j].re);
+                Y0.a[i][j].im = fmaf(-gu.im, u[j], Y0.a[i][j].im);
+            }
+        }
+        to_flavour_f32(Y, w, Pr[kk + 1]);
+    }
+    to_flavour_f32(Y0, w, Pr[0]);
+    const size_t plane = (size_t)nc * ne;
+    float* o = out + (size_t)ic * ne + ie;
+    const int pair[3][3] = {{-1, -1, -1}, {0, -1, -1}, {1, 2, -1}};  // (k, q) -> index, q < k
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            float prob = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const cf Pk = Pr[k].a[i][j];
+                prob = fmaf(Pk.re, Pk.re, fmaf(Pk.im, Pk.im, prob));
+#pragma unroll
+                for (int q = 0; q < k; q++) {
+                    const cf Pq = Pr[q].a[i][j], t = sf[pair[k][q]][j];
+                    // 2 Re(conj(Pq) Pk t)
+                    const float cr = fmaf(Pq.re, Pk.re, Pq.im * Pk.im);
+                    const float ci = fmaf(Pq.re, Pk.im, -Pq.im * Pk.re);
+                    prob = fmaf(2.0f, fmaf(cr, t.re, -ci * t.im), prob);
+                }
+            }
+            o[(size_t)(j * 3 + i) * plane] = prob;  // Prob[i][j] is P(j -> i): channel j*3+i
+        }
+}
+
+cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int ne,
+                                   const int* seg_off, const float2* seg_len, const int* seg_cls,
+                                   int n_cosines, const AvgMixed& av, float* out, cudaStream_t s,
+                                   RowRange rr) {
+    if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
+    const int ne_pad = pad_energies(ne);
+    const WParams w = wparams(p);
+    AvgMixed a = av;
+    a.type = p.anti;
+    const int end = rr.end < 0 ? n_cosines : rr.end;
+    for (int ic0 = rr.begin; ic0 < end; ic0 += kMaxGridY) {
+        const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
+        dim3 grid((ne + kBlock - 1) / kBlock, rows);
+        atmos_mixed_avg_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
+                                                       seg_cls, ic0, n_cosines, a, out);
+    }
+    return cudaGetLastError();
+}
+
 // One channel plane [nc][ne] of a result, transposed to [ne][nc] doubles (the layout of
 // getProbabilityArr, atmoscudapropagator.cu:238-257): 32 x 32 tiles through shared memory,
 // coalesced on both sides.

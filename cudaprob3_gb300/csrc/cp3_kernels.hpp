@@ -49,6 +49,21 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
                                int n_cosines, float* out, cudaStream_t s,
                                RowRange rr = RowRange{});
 
+// Production-height averaging inputs of the mixed kernels (float, from AvgArrays on the host).
+struct AvgMixed {
+    const float* prob = nullptr;  // [2][3][ne][nc][n_bins]
+    const float2* hm = nullptr;   // [nc][n_bins] mid shift of each bin, km, float pair (0 where the
+                                  // air segment has zero length)
+    const float* hw = nullptr;    // [nc][n_bins] bin width, km (0 likewise)
+    int nb = 0, type = 0;
+};
+
+// Mixed atmospheric bins with production-height averaging.
+cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int ne,
+                                   const int* seg_off, const float2* seg_len, const int* seg_cls,
+                                   int n_cosines, const AvgMixed& av, float* out, cudaStream_t s,
+                                   RowRange rr = RowRange{});
+
 // Atmospheric bins whose segments each carry their own electron density (quadratic model):
 // per-segment eigen-solve.  seg_len: double[] (FP64) or float2[] hi/lo (mixed).
 cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,

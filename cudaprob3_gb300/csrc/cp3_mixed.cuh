@@ -223,6 +223,42 @@ CP3_HD WParams wparams(const OscParams& p) {
 
 // One atmospheric bin over M+1 segments, generic in where each segment's layer comes from:
 // seg(l, F) fills F for segment l (0 = air, then shells inwards).
+// The bin's amplitude before the air layer, for M >= 1: G = B^T S_M B (M >= 2) or S_1 (M = 1),
+// with B = S_{M-1}..S_1; seg(l, F) fills layer l.
+template <class SegFn>
+__device__ __forceinline__ void chain_mixed(SegFn seg, int M, cg9& G) {
+    Layer F;
+    seg(1, F);
+    layer_to_gen(F, G);  // B = S_1
+    if (M > 1) {
+        cg9& B = G;
+        for (int l = 2; l < M; l++) {
+            seg(l, F);
+            apply_left(F, B);
+        }
+        seg(M, F);
+        cg9 X = B;
+        apply_left(F, X);  // X = S_M B
+        cs6 Q;             // Q = B^T X (symmetric)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = i; j < 3; j++) {
+                cf acc = cmulf(B.a[0][i], X.a[0][j]);
+#pragma unroll
+                for (int k = 1; k < 3; k++) {
+                    const cf b = B.a[k][i], x = X.a[k][j];
+                    acc.re = fmaf(b.re, x.re, fmaf(-b.im, x.im, acc.re));
+                    acc.im = fmaf(b.re, x.im, fmaf(b.im, x.re, acc.im));
+                }
+                Q.a[sidx(i, j)] = acc;
+            }
+        sym_to_gen(Q, G);
+    }
+}
+
+// One atmospheric bin over M+1 segments, generic in where each segment's layer comes from:
+// seg(l, F) fills F for segment l (0 = air, then shells inwards).
 template <class SegFn>
 __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WParams& w,
                                                      float* __restrict__ out, size_t plane) {
@@ -232,33 +268,7 @@ __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WPa
         seg(0, F);
         layer_to_gen(F, A2);
     } else {
-        seg(1, F);
-        layer_to_gen(F, A2);  // B = S_1
-        if (M > 1) {
-            cg9& B = A2;
-            for (int l = 2; l < M; l++) {
-                seg(l, F);
-                apply_left(F, B);
-            }
-            seg(M, F);
-            cg9 X = B;
-            apply_left(F, X);  // X = S_M B
-            cs6 Q;             // Q = B^T X (symmetric)
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = i; j < 3; j++) {
-                    cf acc = cmulf(B.a[0][i], X.a[0][j]);
-#pragma unroll
-                    for (int k = 1; k < 3; k++) {
-                        const cf b = B.a[k][i], x = X.a[k][j];
-                        acc.re = fmaf(b.re, x.re, fmaf(-b.im, x.im, acc.re));
-                        acc.im = fmaf(b.re, x.im, fmaf(b.im, x.re, acc.im));
-                    }
-                    Q.a[sidx(i, j)] = acc;
-                }
-            sym_to_gen(Q, A2);
-        }
+        chain_mixed(seg, M, A2);
         seg(0, F);
         apply_right(F, A2);  // ... S_0
     }

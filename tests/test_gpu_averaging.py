@@ -1,6 +1,6 @@
-"""Production-height averaging on the FP64 kernels (physics.hpp:997-1067, switched on
-explicitly: the reference's own switch never enables it) against the fixture made by the
-reference's calculate_atmos and against the oracle."""
+"""Production-height averaging (physics.hpp:997-1067, switched on explicitly: the
+reference's own switch never enables it) on the FP64 and mixed kernels, against the fixture
+made by the reference's calculate_atmos and against the oracle."""
 import os
 
 import numpy as np
@@ -62,13 +62,43 @@ def test_averaging_against_oracle(oracle, poly):
         assert np.abs(got - ref).max() <= 1e-12
 
 
-def test_averaging_on_mixed_handle_is_refused():
+def test_mixed_averaging_matches_reference_fixture():
+    d = np.load(os.path.join(GOLDEN, "atmos_avg.npz"))
+    for t, knu in ((0, 1), (1, -1)):
+        got = run_avg("mixed", d["mix"], knu, t == 1, d["cosines"], d["energies"], d["radii"],
+                      d["rho"], d["ye"], float(d["h_km"]), int(d["avg_bins"]), d["avg_prob"],
+                      d["avg_edges"])
+        assert np.abs(got - d["out"][t]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("shells", [4, 59])
+def test_mixed_averaging_against_oracle(oracle, shells):
+    """Wide production-height bins (the shift phases reach hundreds of rad at low energy) on
+    4 and 59 shells, both neutrino types, all nine channels."""
+    from oracle.oracle import Mixing as OMix
+    rng = np.random.default_rng(3)
+    cz, en = np.linspace(-1, 1, 41), earth.log_energy_grid(37)
+    nb = 8
+    w = rng.uniform(0.1, 1.0, (2, 3, len(en), len(cz), nb))
+    w /= w.sum(axis=-1, keepdims=True)
+    edges = np.linspace(2.0, 60.0, nb + 1)
+    m = earth.gaussian_sets(1, seed=41)[0]
+    mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+    r, rho, ye = earth.PREM_4LAYER if shells == 4 else earth.synthetic_shells(59)
+    for anti, knu in ((False, 1), (True, -1)):
+        ref = oracle.atmos(OMix(*mix6[:4], mix6[4], mix6[5], knu), anti, cz, en, r, rho, ye, 20.0,
+                           avg=(nb, w.ravel(), edges))
+        got = run_avg("mixed", mix6, knu, anti, cz, en, r, rho, ye, 20.0, nb, w.ravel(), edges)
+        assert np.abs(got - ref).max() <= 1e-5
+
+
+def test_mixed_averaging_with_quadratic_density_is_refused():
     p = AtmosCudaPropagatorSingle(0, 3, 2, precision="mixed")
     p.setEnergyList([1.0, 2.0])
     p.setCosineList([-0.5, 0.0, 0.5])
     p.setMNSMatrix(0.5, 0.1, 0.7, 0.0, 1)
     p.setNeutrinoMasses(7.5e-5, 2.5e-3)
-    p.setDensity(*earth.PREM_4LAYER)
+    p.setDensity(*earth.PREM_4LAYER_QUAD_V2)
     p.setProductionHeight(20.0)
     p.SetNumberOfProductionHeightBinsForAveraging(1)
     p.setProductionHeightList(np.ones(2 * 3 * 2 * 3), [15.0, 25.0])

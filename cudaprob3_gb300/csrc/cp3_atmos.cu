@@ -41,20 +41,26 @@ struct Layer64 {
     cd z[2];         // e^{i (arg_k - arg_0)} - 1, k = 1, 2
 };
 
-// The phases of one layer from dmMatVac[k][0], as getArg and multiply_phase_matrix
-// (math.hpp:59-75) evaluate them; arg[] receives arg_k.
+// The phases of one layer from dmMatVac[k][0], as getArg (physics.hpp:439-450) evaluates
+// them; arg[] receives arg_k.  The relative phase arg_k - arg_0 is taken exactly, as a
+// TwoSum pair dh + dl (a rounded difference could be off by 1e-13 rad at ~800 rad, which
+// ~120 layers would accumulate), and e^{i(dh + dl)} = e^{i dh} (1 + i dl) to second order in
+// |dl| <= 1e-13: two sincos per layer instead of the three of multiply_phase_matrix
+// (math.hpp:59-75), with the reference's relative phases to ~1e-16.
 __device__ __forceinline__ void layer64_phases(const double dmv[3], double L, double E,
                                                Layer64& f, double arg[3]) {
-    double s[3], c[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        arg[k] = -kLoEFac * dmv[k] * L / E;
-        sincos(arg[k], &s[k], &c[k]);
-    }
+    for (int k = 0; k < 3; k++) arg[k] = -kLoEFac * dmv[k] * L / E;
 #pragma unroll
     for (int kk = 0; kk < 2; kk++) {
         const int k = kk + 1;
-        f.z[kk] = cd{c[k] * c[0] + s[k] * s[0] - 1.0, s[k] * c[0] - c[k] * s[0]};
+        const double dh = __dadd_rn(arg[k], -arg[0]);  // TwoSum (Knuth)
+        const double bb = __dadd_rn(dh, -arg[k]);
+        const double dl = __dadd_rn(__dadd_rn(arg[k], -__dadd_rn(dh, -bb)), __dadd_rn(-arg[0], -bb));
+        double s, c;
+        sincos(dh, &s, &c);
+        // e^{i dh} (1 + i dl) - 1
+        f.z[kk] = cd{(c - 1.0) - s * dl, s + c * dl};
     }
 }
 

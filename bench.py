@@ -45,8 +45,10 @@ NCU_TRAFFIC = {
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
     ("batch_atmos", "mixed"): (31.19872e6 + 897.908224e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
-    ("batch_beam", "mixed"): (105.65504e6 + 915.776512e6, 921.6e6,
+    ("batch_beam", "mixed"): (105.383168e6 + 904.410624e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
+    ("atmos59", "fp64"): (10.150656e6 + 244.74496e6, 288.0e6,
+                          "profiles/atmos_f64_kernel_59shells_2000x2000.md"),
 }
 
 

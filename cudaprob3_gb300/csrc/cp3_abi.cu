@@ -97,9 +97,19 @@ struct cp3_propagator {
     bool timed_table = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
+    // Energy lists go up asynchronously on `stream` from a pinned staging buffer; a compute
+    // on another stream waits for ev_upload.  ev_done marks the end of the last compute (on
+    // last_stream): uploads and computes that overwrite what it reads or writes wait for it.
+    cudaEvent_t ev_done = nullptr, ev_upload = nullptr;
+    bool upload_pending = false;
+    void* h_stage = nullptr;
+
     ~cp3_propagator() {
         for (cudaEvent_t& e : ev)
             if (e) cudaEventDestroy(e);
+        if (ev_done) cudaEventDestroy(ev_done);
+        if (ev_upload) cudaEventDestroy(ev_upload);
+        if (h_stage) cudaFreeHost(h_stage);
         if (h_result) cudaFreeHost(h_result);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -112,12 +122,15 @@ namespace {
 constexpr int kDefaultCopyChunks = 4;
 
 // x[i] as float pairs (hi, lo), hi + lo = x[i] to ~48 bits (the device's df_from, done once).
-std::vector<float2> split_pairs(const double* x, size_t n) {
-    std::vector<float2> out(n);
+void split_pairs(const double* x, size_t n, float2* out) {
     for (size_t i = 0; i < n; i++) {
         const float h = (float)x[i];
         out[i] = make_float2(h, (float)(x[i] - (double)h));
     }
+}
+std::vector<float2> split_pairs(const double* x, size_t n) {
+    std::vector<float2> out(n);
+    split_pairs(x, n, out.data());
     return out;
 }
 
@@ -174,6 +187,10 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
     h->result_bytes = elems * (precision == CP3_FP64 ? sizeof(double) : sizeof(float));
     if ((e = cudaSetDevice(device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_upload, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaMallocHost(&h->h_stage, (size_t)ne * (sizeof(double) + sizeof(float2)))) !=
+            cudaSuccess ||
         (e = h->d_energies.reserve(ne)) != cudaSuccess ||
         (precision == CP3_MIXED && (e = h->d_energies_df.reserve(ne)) != cudaSuccess) ||
         (e = h->d_result.reserve(h->result_bytes)) != cudaSuccess) {
@@ -186,9 +203,17 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
     return CP3_OK;
 }
 
+// The host-synchronous uploads and reallocations below overwrite what the last compute
+// reads: they start once it has ended.
+int wait_last_compute(cp3_propagator* h) {
+    if (h->last_stream) CP3_CUDA(h, cudaEventSynchronize(h->ev_done), "wait for the last compute");
+    return CP3_OK;
+}
+
 // Uploads the trajectory table and density classes if any of their inputs changed.
 int prepare_atmos(cp3_propagator* h) {
     if (!h->traj_dirty) return CP3_OK;
+    if (int rc = wait_last_compute(h)) return rc;
     std::string msg;
     int rc = build_trajectories(h->model, h->cosines.data(), h->nc, h->height_cm, &h->traj, &msg);
     if (rc) return fail(h, rc, msg);
@@ -243,6 +268,8 @@ int prepare_atmos(cp3_propagator* h) {
 // bin edges and the air segment in cm (the reference's `dist` of layer 0).
 int prepare_averaging(cp3_propagator* h, AvgArrays* av, AvgMixed* avm) {
     if (h->avg_bins == 0) return CP3_OK;
+    if (h->avg_dirty)
+        if (int rc = wait_last_compute(h)) return rc;
     if (h->avg_dirty && h->precision == CP3_MIXED) {
         // float probabilities; per (cosine, bin) the mid shift as a float pair and the width,
         // both in km (the phase rates are per km); zero where the air segment is zero, as the
@@ -316,6 +343,11 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
     OscParams p;
     build_osc_params(h->mix, type == CP3_ANTINEUTRINO, &p);
     cudaError_t e = cudaSuccess;
+    // the energies' upload, and the last compute (one result buffer per handle), come first
+    if (h->upload_pending && s != h->stream) e = cudaStreamWaitEvent(s, h->ev_upload, 0);
+    if (e == cudaSuccess && h->last_stream && h->last_stream != s)
+        e = cudaStreamWaitEvent(s, h->ev_done, 0);
+    if (e != cudaSuccess) return cuda_fail(h, e, "order compute");
     h->timed = false;
     const bool profile = h->profiling && !host_dst;  // kernel times only without copies
     auto mark = [&](int i) {
@@ -403,6 +435,7 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
             e = cudaMemcpyAsync(host_dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost, s);
         h->timed_table = false;
     }
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev_done, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     h->result_on_host = false;
     h->computed = true;
@@ -479,13 +512,24 @@ int cp3_set_energies(cp3_propagator* h, const double* energies, int n) {
                     "Propagator::setEnergyList. Propagator was not created for this number of energy nodes");
     h->energies.assign(energies, energies + n);
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    CP3_CUDA(h, cudaMemcpy(h->d_energies.ptr, energies, sizeof(double) * n, cudaMemcpyHostToDevice),
-             "upload energies");
+    // The staging buffer is reused: the previous upload must have read it.
+    if (h->upload_pending) CP3_CUDA(h, cudaEventSynchronize(h->ev_upload), "energy upload");
+    h->upload_pending = false;
+    double* stage = static_cast<double*>(h->h_stage);
+    std::memcpy(stage, energies, sizeof(double) * n);
+    // The upload overwrites what the last compute reads: it waits for it on the device.
+    if (h->last_stream && h->last_stream != h->stream)
+        CP3_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_done, 0), "order upload");
+    CP3_CUDA(h, cudaMemcpyAsync(h->d_energies.ptr, stage, sizeof(double) * n,
+                                cudaMemcpyHostToDevice, h->stream), "upload energies");
     if (h->precision == CP3_MIXED) {
-        const std::vector<float2> pairs = split_pairs(energies, (size_t)n);
-        CP3_CUDA(h, cudaMemcpy(h->d_energies_df.ptr, pairs.data(), sizeof(float2) * n,
-                               cudaMemcpyHostToDevice), "upload energies");
+        float2* pairs = reinterpret_cast<float2*>(stage + n);
+        split_pairs(energies, (size_t)n, pairs);
+        CP3_CUDA(h, cudaMemcpyAsync(h->d_energies_df.ptr, pairs, sizeof(float2) * n,
+                                    cudaMemcpyHostToDevice, h->stream), "upload energies");
     }
+    CP3_CUDA(h, cudaEventRecord(h->ev_upload, h->stream), "record upload");
+    h->upload_pending = true;
     h->energies_set = true;
     return CP3_OK;
 }
@@ -496,17 +540,18 @@ int cp3_set_cosines(cp3_propagator* h, const double* cosines, int n) {
     if (n != h->nc || !cosines)
         return fail(h, CP3_ERR_BAD_SIZE,
                     "Propagator::setCosineList. Propagator was not created for this number of cosine nodes");
+    // An unchanged list keeps the trajectories and its layer check, which passed when it was
+    // set (a new model is checked against it in set_model); the reference re-derives both
+    // every time, with the same result.
+    if (h->cosines_set && std::memcmp(h->cosines.data(), cosines, sizeof(double) * n) == 0)
+        return CP3_OK;
     if (h->model_set) {  // setMaxlayers runs on every cosine change (atmoscpupropagator.hpp:378)
         for (int i = 0; i < n; i++)
             if (count_shells(h->model, cosines[i]) > kMaxShells)
                 return fail(h, CP3_ERR_LAYER_LIMIT, "setMaxlayers : invalid number of maxLayer");
     }
-    // An unchanged list keeps the trajectories (the reference re-derives them every time; the
-    // result is the same).
-    if (!h->cosines_set || std::memcmp(h->cosines.data(), cosines, sizeof(double) * n) != 0) {
-        h->cosines.assign(cosines, cosines + n);
-        h->traj_dirty = true;
-    }
+    h->cosines.assign(cosines, cosines + n);
+    h->traj_dirty = true;
     h->cosines_set = true;
     return CP3_OK;
 }

@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(kBlock)
 
     // shift factors of the pairs (1,0), (2,0), (2,1): the reference's d = d0[k] - d0[q] is
     // -(omega_k - omega_q) per km of path-length shift (omega_0 = 0)
-    const df om1{__ldg(t0 + 6), __ldg(t0 + 7)}, om2{__ldg(t0 + 8), __ldg(t0 + 9)};
+    const df om1{__ldg(t0 + 6), __ldg(t0 + 8)}, om2{__ldg(t0 + 7), __ldg(t0 + 9)};
     const df dom[3] = {om1, om2, df_sub(om2, om1)};
     cf sf[3][3];
 #pragma unroll

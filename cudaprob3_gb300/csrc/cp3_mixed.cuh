@@ -41,12 +41,79 @@ __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Paired FP32.  sm_100+ executes FFMA2 / FMUL2 / FADD2: one instruction, two independent
+// FP32 lanes, each rounded exactly as fmaf / __fmul_rn / __fadd_rn.  On GB300 the FMA pipe
+// retires paired and scalar FMAs at the same FLOP rate, so pairing does not add arithmetic
+// throughput; it halves the issue slots of the paired work, and issue is what binds these
+// kernels.  Pairs: the real and imaginary parts of a complex entry, or the two phases
+// (k = 1, 2) of one layer.
+
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 f2(cf c) { return make_float2(c.re, c.im); }
+__device__ __forceinline__ cf fc(float2 v) { return cf{v.x, v.y}; }
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// reduced_phase for the two phase rates (ah + al).x and (ah + al).y of one layer times the
+// same path length bh + bl; lane for lane the same operations and roundings.
+__device__ __forceinline__ float2 reduced_phase2(float2 ah, float2 al, float bh, float bl,
+                                                 float2& lo) {
+    const float2 B = bc2(bh);
+    const float2 p = __fmul2_rn(ah, B);
+    float2 e = __ffma2_rn(ah, B, neg2(p));
+    e = __ffma2_rn(ah, bc2(bl), e);
+    e = __ffma2_rn(al, B, e);
+    const float2 q = __fmul2_rn(p, bc2(kInvTwoPi));
+    const float2 mn = make_float2(-rintf(q.x), -rintf(q.y));
+    float2 r = __ffma2_rn(mn, bc2(kTwoPiA), p);
+    r = __ffma2_rn(mn, bc2(kTwoPiB), r);
+    r = __ffma2_rn(mn, bc2(kTwoPiC), r);
+    const float2 s = __fadd2_rn(r, e);
+    lo = __fadd2_rn(__fadd2_rn(r, neg2(s)), e);
+    return s;
+}
+
+// poly_sincos of two arguments, lane for lane.
+__device__ __forceinline__ void poly_sincos2(float2 x, float2& s, float2& c) {
+    const float2 x2 = __fmul2_rn(x, x);
+    float2 ps = __ffma2_rn(bc2(kSin11), x2, bc2(kSin9));
+    ps = __ffma2_rn(ps, x2, bc2(kSin7));
+    ps = __ffma2_rn(ps, x2, bc2(kSin5));
+    ps = __ffma2_rn(ps, x2, bc2(kSin3));
+    s = __ffma2_rn(__fmul2_rn(ps, x2), x, x);
+    float2 pc = __ffma2_rn(bc2(kCos10), x2, bc2(kCos8));
+    pc = __ffma2_rn(pc, x2, bc2(kCos6));
+    pc = __ffma2_rn(pc, x2, bc2(kCos4));
+    pc = __ffma2_rn(pc, x2, bc2(kCos2));
+    c = __ffma2_rn(pc, x2, bc2(1.0f));
+}
+
+// unit_phase_minus_one of two phases, lane for lane: z_k = zre.k + i zim.k.
+__device__ __forceinline__ void unit_phase_minus_one2(float2 r, float2 lo, float2& zre,
+                                                      float2& zim) {
+    const float2 a = make_float2(fabsf(r.x), fabsf(r.y));
+    const bool rx = a.x > 1.57079637f, ry = a.y > 1.57079637f;
+    const float2 t = __fadd2_rn(__fadd2_rn(bc2(3.14159274f), neg2(a)), bc2(-8.74227766e-8f));
+    float2 sx, cx;
+    poly_sincos2(make_float2(rx ? t.x : a.x, ry ? t.y : a.y), sx, cx);
+    const float2 nn = __ffma2_rn(sx, sx, __fmul2_rn(cx, cx));
+    const float2 inv = make_float2(rsqrtf(nn.x), rsqrtf(nn.y));
+    const float2 si = __fmul2_rn(sx, inv);
+    const float2 sn = make_float2(copysignf(si.x, r.x), copysignf(si.y, r.y));
+    const float2 cs = __fmul2_rn(make_float2(rx ? -cx.x : cx.x, ry ? -cx.y : cx.y), inv);
+    const float2 ml = neg2(lo);
+    zre = __ffma2_rn(ml, sn, __fadd2_rn(cs, bc2(-1.0f)));
+    zim = __ffma2_rn(ml, cs, neg2(sn));
+}
+
 // How a kernel reads the eigen table: the read-only path (__ldg) for tables an earlier
 // launch wrote, L2 only (__ldcg) for tables written earlier in the same launch.
 enum TableLoad { kLoadReadOnly = 0, kLoadL2 = 1 };
 
-// t points at this bin's 48-byte table entry: u1 (3), u2 (3), omega_1 (hi, lo), omega_2
-// (hi, lo), 2 unused.
+// t points at this bin's 48-byte table entry: u1 (3), u2 (3), then the phase rates
+// omega_1, omega_2 as double-floats with the two high parts side by side and the two low
+// parts side by side (so that each pair is one aligned 8-byte register pair of the float4
+// loads), 2 unused: [u1 | u2 | om1.hi om2.hi | om1.lo om2.lo | 0 0].
 template <int kLoad = kLoadReadOnly>
 __device__ __forceinline__ void layer_from_table(const float* __restrict__ t, float2 L, Layer& f) {
     const float4* t4 = reinterpret_cast<const float4*>(t);
@@ -66,11 +133,13 @@ __device__ __forceinline__ void layer_from_table(const float* __restrict__ t, fl
     f.u[1][0] = a.w;
     f.u[1][1] = b.x;
     f.u[1][2] = b.y;
-    float lo;
-    float r = reduced_phase(b.z, b.w, L.x, L.y, lo);
-    unit_phase_minus_one(r, lo, f.z[0][0], f.z[0][1]);
-    r = reduced_phase(c.x, c.y, L.x, L.y, lo);
-    unit_phase_minus_one(r, lo, f.z[1][0], f.z[1][1]);
+    float2 lo, zr, zi;
+    const float2 r = reduced_phase2(make_float2(b.z, b.w), make_float2(c.x, c.y), L.x, L.y, lo);
+    unit_phase_minus_one2(r, lo, zr, zi);
+    f.z[0][0] = zr.x;
+    f.z[0][1] = zi.x;
+    f.z[1][0] = zr.y;
+    f.z[1][1] = zi.y;
 }
 
 // The table entry of one (class, energy): eigenvectors and phase rates, three float4.
@@ -78,11 +147,11 @@ __device__ __forceinline__ void store_table_entry(float* __restrict__ t, const f
                                                   const float om[2][2]) {
     float4* d = reinterpret_cast<float4*>(t);
     d[0] = make_float4(u[0][0], u[0][1], u[0][2], u[1][0]);
-    d[1] = make_float4(u[1][1], u[1][2], om[0][0], om[0][1]);
-    d[2] = make_float4(om[1][0], om[1][1], 0.f, 0.f);
+    d[1] = make_float4(u[1][1], u[1][2], om[0][0], om[1][0]);
+    d[2] = make_float4(om[0][1], om[1][1], 0.f, 0.f);
 }
 
-// G <- S G
+// G <- S G.  Per column: w = u^T G (paired over re/im), y = z w, G += u y (paired).
 __device__ __forceinline__ void apply_left(const Layer& f, cg9& G) {
 #pragma unroll
     for (int k = 0; k < 2; k++) {
@@ -90,22 +159,17 @@ __device__ __forceinline__ void apply_left(const Layer& f, cg9& G) {
         const float zr = f.z[k][0], zi = f.z[k][1];
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            float wr = u[0] * G.a[0][j].re, wi = u[0] * G.a[0][j].im;
-            wr = fmaf(u[1], G.a[1][j].re, wr);
-            wi = fmaf(u[1], G.a[1][j].im, wi);
-            wr = fmaf(u[2], G.a[2][j].re, wr);
-            wi = fmaf(u[2], G.a[2][j].im, wi);
-            const float yr = fmaf(zr, wr, -zi * wi), yi = fmaf(zr, wi, zi * wr);
+            float2 w = __fmul2_rn(bc2(u[0]), f2(G.a[0][j]));
+            w = __ffma2_rn(bc2(u[1]), f2(G.a[1][j]), w);
+            w = __ffma2_rn(bc2(u[2]), f2(G.a[2][j]), w);
+            const float2 y = make_float2(fmaf(zr, w.x, -zi * w.y), fmaf(zr, w.y, zi * w.x));
 #pragma unroll
-            for (int i = 0; i < 3; i++) {
-                G.a[i][j].re = fmaf(u[i], yr, G.a[i][j].re);
-                G.a[i][j].im = fmaf(u[i], yi, G.a[i][j].im);
-            }
+            for (int i = 0; i < 3; i++) G.a[i][j] = fc(__ffma2_rn(bc2(u[i]), y, f2(G.a[i][j])));
         }
     }
 }
 
-// G <- G S
+// G <- G S.  Per row: w = G u, y = w z, G += y u^T.
 __device__ __forceinline__ void apply_right(const Layer& f, cg9& G) {
 #pragma unroll
     for (int k = 0; k < 2; k++) {
@@ -113,67 +177,78 @@ __device__ __forceinline__ void apply_right(const Layer& f, cg9& G) {
         const float zr = f.z[k][0], zi = f.z[k][1];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            float wr = G.a[i][0].re * u[0], wi = G.a[i][0].im * u[0];
-            wr = fmaf(G.a[i][1].re, u[1], wr);
-            wi = fmaf(G.a[i][1].im, u[1], wi);
-            wr = fmaf(G.a[i][2].re, u[2], wr);
-            wi = fmaf(G.a[i][2].im, u[2], wi);
-            const float yr = fmaf(zr, wr, -zi * wi), yi = fmaf(zr, wi, zi * wr);
+            float2 w = __fmul2_rn(f2(G.a[i][0]), bc2(u[0]));
+            w = __ffma2_rn(f2(G.a[i][1]), bc2(u[1]), w);
+            w = __ffma2_rn(f2(G.a[i][2]), bc2(u[2]), w);
+            const float2 y = make_float2(fmaf(zr, w.x, -zi * w.y), fmaf(zr, w.y, zi * w.x));
 #pragma unroll
-            for (int j = 0; j < 3; j++) {
-                G.a[i][j].re = fmaf(yr, u[j], G.a[i][j].re);
-                G.a[i][j].im = fmaf(yi, u[j], G.a[i][j].im);
-            }
+            for (int j = 0; j < 3; j++) G.a[i][j] = fc(__ffma2_rn(y, bc2(u[j]), f2(G.a[i][j])));
         }
     }
 }
 
 // G = S = 1 + z1 u1 u1^T + z2 u2 u2^T
 __device__ __forceinline__ void layer_to_gen(const Layer& f, cg9& G) {
+    const float2 z0 = make_float2(f.z[0][0], f.z[0][1]), z1 = make_float2(f.z[1][0], f.z[1][1]);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = i; j < 3; j++) {
-            const float p0 = f.u[0][i] * f.u[0][j], p1 = f.u[1][i] * f.u[1][j];
-            const cf v{fmaf(f.z[1][0], p1, fmaf(f.z[0][0], p0, i == j ? 1.0f : 0.0f)),
-                       fmaf(f.z[1][1], p1, f.z[0][1] * p0)};
-            G.a[i][j] = v;
-            G.a[j][i] = v;
+            const float2 p0 = bc2(f.u[0][i] * f.u[0][j]), p1 = bc2(f.u[1][i] * f.u[1][j]);
+            const float2 v =
+                __ffma2_rn(z1, p1, __ffma2_rn(z0, p0, make_float2(i == j ? 1.0f : 0.0f, 0.0f)));
+            G.a[i][j] = fc(v);
+            G.a[j][i] = fc(v);
         }
+}
+
+// Complex dot products over k of 3 with paired FMAs: the products of x's real parts and of
+// its imaginary parts with the (re, im) pairs of y accumulate separately, so no lane swap is
+// needed; sum_k x_k y_k = (r.x - i.y, r.y + i.x) and sum_k conj(x_k) y_k = (r.x + i.y,
+// r.y - i.x) with r = sum re(x_k) y_k, i = sum im(x_k) y_k.
+struct cacc {
+    float2 r, i;
+};
+__device__ __forceinline__ cacc cdot3(cf x0, cf y0, cf x1, cf y1, cf x2, cf y2) {
+    cacc a;
+    a.r = __fmul2_rn(bc2(x0.re), f2(y0));
+    a.i = __fmul2_rn(bc2(x0.im), f2(y0));
+    a.r = __ffma2_rn(bc2(x1.re), f2(y1), a.r);
+    a.i = __ffma2_rn(bc2(x1.im), f2(y1), a.i);
+    a.r = __ffma2_rn(bc2(x2.re), f2(y2), a.r);
+    a.i = __ffma2_rn(bc2(x2.im), f2(y2), a.i);
+    return a;
 }
 
 // One Newton-Schulz step toward the nearest unitary matrix, A <- A (3 - A^+ A) / 2.  The
 // rounding of FP32 layer matrices leaves each slightly non-unitary and that part of the
 // error accumulates over the ~2M products of a deep trajectory; one step at the end removes
 // it to second order (measured: max error on the 59-shell, 2000 x 2000 grid drops by ~2x).
+// A^+ A is Hermitian: its upper triangle is formed and mirrored.
 __device__ __forceinline__ void newton_schulz(cg9& A) {
     cg9 G;
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+    for (int i = 0; i < 3; i++) {
+        // diagonal: sum_k |A_ki|^2
+        float2 q = __fmul2_rn(f2(A.a[0][i]), f2(A.a[0][i]));
+        q = __ffma2_rn(f2(A.a[1][i]), f2(A.a[1][i]), q);
+        q = __ffma2_rn(f2(A.a[2][i]), f2(A.a[2][i]), q);
+        G.a[i][i] = cf{1.5f - 0.5f * (q.x + q.y), 0.0f};
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-            float re = 0.f, im = 0.f;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const cf a = A.a[k][i], b = A.a[k][j];  // conj(a) b
-                re = fmaf(a.re, b.re, fmaf(a.im, b.im, re));
-                im = fmaf(a.re, b.im, fmaf(-a.im, b.re, im));
-            }
-            G.a[i][j] = cf{(i == j ? 1.5f : 0.f) - 0.5f * re, -0.5f * im};
+        for (int j = i + 1; j < 3; j++) {
+            const cacc h = cdot3(A.a[0][i], A.a[0][j], A.a[1][i], A.a[1][j], A.a[2][i], A.a[2][j]);
+            const float re = h.r.x + h.i.y, im = h.r.y - h.i.x;  // (A^+ A)_ij
+            G.a[i][j] = cf{-0.5f * re, -0.5f * im};
+            G.a[j][i] = cf{-0.5f * re, 0.5f * im};
         }
+    }
     cg9 R;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            cf acc = cmulf(A.a[i][0], G.a[0][j]);
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                const cf a = A.a[i][k], g = G.a[k][j];
-                acc.re = fmaf(a.re, g.re, fmaf(-a.im, g.im, acc.re));
-                acc.im = fmaf(a.re, g.im, fmaf(a.im, g.re, acc.im));
-            }
-            R.a[i][j] = acc;
+            const cacc h = cdot3(A.a[i][0], G.a[0][j], A.a[i][1], G.a[1][j], A.a[i][2], G.a[2][j]);
+            R.a[i][j] = cf{h.r.x - h.i.y, h.r.y + h.i.x};
         }
     A = R;
 }
@@ -237,23 +312,21 @@ __device__ __forceinline__ void chain_mixed(SegFn seg, int M, cg9& G) {
             apply_left(F, B);
         }
         seg(M, F);
-        cg9 X = B;
+        cg9 X = B, Q;
         apply_left(F, X);  // X = S_M B
-        cs6 Q;             // Q = B^T X (symmetric)
+        // G = B^T X (complex symmetric: the upper triangle is formed and mirrored)
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
             for (int j = i; j < 3; j++) {
-                cf acc = cmulf(B.a[0][i], X.a[0][j]);
-#pragma unroll
-                for (int k = 1; k < 3; k++) {
-                    const cf b = B.a[k][i], x = X.a[k][j];
-                    acc.re = fmaf(b.re, x.re, fmaf(-b.im, x.im, acc.re));
-                    acc.im = fmaf(b.re, x.im, fmaf(b.im, x.re, acc.im));
-                }
-                Q.a[sidx(i, j)] = acc;
+                const cacc h = cdot3(B.a[0][i], X.a[0][j], B.a[1][i], X.a[1][j], B.a[2][i], X.a[2][j]);
+                Q.a[i][j] = cf{h.r.x - h.i.y, h.r.y + h.i.x};
             }
-        sym_to_gen(Q, G);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < i; j++) Q.a[i][j] = Q.a[j][i];
+        G = Q;
     }
 }
 
@@ -297,12 +370,14 @@ __device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict
                                                      double rho_e, float2 L, Layer& f) {
     float om[2][2];
     rotated_eigen_vectors(p, df_from(E), df_from(rho_e), f.u, om);
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        float lo;
-        const float r = reduced_phase(om[k][0], om[k][1], L.x, L.y, lo);
-        unit_phase_minus_one(r, lo, f.z[k][0], f.z[k][1]);
-    }
+    float2 lo, zr, zi;
+    const float2 r = reduced_phase2(make_float2(om[0][0], om[1][0]),
+                                    make_float2(om[0][1], om[1][1]), L.x, L.y, lo);
+    unit_phase_minus_one2(r, lo, zr, zi);
+    f.z[0][0] = zr.x;
+    f.z[0][1] = zi.x;
+    f.z[1][0] = zr.y;
+    f.z[1][1] = zi.y;
 }
 
 // One beam energy (E, rho_e as double or float pair): eigen-decomposition (double-float
@@ -316,13 +391,11 @@ __device__ __forceinline__ void beam_bin_mixed(const OscParams* __restrict__ p, 
     float P[2][6], om[2][2];
     rotated_eigen_mixed(p, E, rho_e, P, om);
     for (int j = 0; j < nL; j++) {
-        float z[2][2];
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            float lo;
-            const float r = reduced_phase(om[k][0], om[k][1], L[j].x, L[j].y, lo);
-            unit_phase_minus_one(r, lo, z[k][0], z[k][1]);
-        }
+        float2 lo, zr, zi;
+        const float2 r = reduced_phase2(make_float2(om[0][0], om[1][0]),
+                                        make_float2(om[0][1], om[1][1]), L[j].x, L[j].y, lo);
+        unit_phase_minus_one2(r, lo, zr, zi);
+        const float z[2][2] = {{zr.x, zi.x}, {zr.y, zi.y}};
         cs6 S;
         layer_matrix(z, P[0], P[1], S);
         cg9 A2;

@@ -157,6 +157,36 @@ def test_calculate_to_host_matches_device_result(prec, model):
             assert np.array_equal(host.numpy().reshape(want.shape), want), chunks
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_energy_uploads_and_computes_ordered_across_streams(prec):
+    """setEnergyList uploads asynchronously; computes on other streams wait for the upload,
+    and an upload or compute that follows a compute on another stream waits for it."""
+    import torch
+    nc, ne = 48, 160
+    en_a = earth.log_energy_grid(ne)
+    en_b = en_a[::-1] * 0.7
+    want = []
+    for en in (en_a, en_b):
+        q = configured(nc=nc, ne=ne, prec=prec)
+        q.setEnergyList(en)
+        q.calculateProbabilities(NeutrinoType.Neutrino)
+        want.append(q.result().copy())
+    assert not np.array_equal(want[0], want[1])
+    dtype = torch.float64 if prec == "fp64" else torch.float32
+    p = configured(nc=nc, ne=ne, prec=prec)
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    for rep in range(3):
+        hosts = [torch.full((9 * nc * ne,), -1.0, dtype=dtype, pin_memory=True) for _ in range(2)]
+        for k, en in enumerate((en_a, en_b)):
+            p.setEnergyList(en)
+            p.calculate_to_host_async(NeutrinoType.Neutrino, hosts[k].data_ptr(), 3,
+                                      streams[k].cuda_stream)
+        for st in streams:
+            st.synchronize()
+        for k in range(2):
+            assert np.array_equal(hosts[k].numpy().reshape(want[k].shape), want[k]), (rep, k)
+
+
 def test_calculate_to_host_beam():
     import torch
     ne = 101

@@ -361,6 +361,62 @@ CP3_HD df df_sqrt(df x) {
     return df_fast2sum(r, d * (0.5f / r));
 }
 
+#ifdef __CUDACC__
+// ---------------------------------------------------------------------------------------
+// Paired FP32.  sm_100+ executes FFMA2 / FMUL2 / FADD2: one instruction, two independent
+// FP32 lanes, each rounded exactly as fmaf / __fmul_rn / __fadd_rn.  On GB300 the FMA pipe
+// retires paired and scalar FMAs at the same FLOP rate, so pairing does not add arithmetic
+// throughput; it halves the issue slots of the paired work, and issue is what binds the
+// mixed kernels.  Lanes pair independent computations: the real and imaginary parts of a
+// complex entry, the two phases of a layer, the two refined roots, the two projectors.
+
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// Two double-floats side by side (lane x, lane y); the operations are df_add / df_mul /
+// df_fast2sum lane for lane.
+struct df2 {
+    float2 hi, lo;
+};
+__device__ __forceinline__ df2 df2_bc(df x) { return df2{bc2(x.hi), bc2(x.lo)}; }
+__device__ __forceinline__ df2 df2_of(df x, df y) {
+    return df2{make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)};
+}
+__device__ __forceinline__ df df2_x(const df2& v) { return df{v.hi.x, v.lo.x}; }
+__device__ __forceinline__ df df2_y(const df2& v) { return df{v.hi.y, v.lo.y}; }
+__device__ __forceinline__ df2 df2_fast2sum(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    return df2{s, __fadd2_rn(b, neg2(__fadd2_rn(s, neg2(a))))};
+}
+__device__ __forceinline__ df2 df2_add(const df2& x, const df2& y) {
+    const float2 s = __fadd2_rn(x.hi, y.hi);
+    const float2 bb = __fadd2_rn(s, neg2(x.hi));
+    float2 e = __fadd2_rn(__fadd2_rn(x.hi, neg2(__fadd2_rn(s, neg2(bb)))),
+                          __fadd2_rn(y.hi, neg2(bb)));
+    e = __fadd2_rn(e, __fadd2_rn(x.lo, y.lo));
+    return df2_fast2sum(s, e);
+}
+__device__ __forceinline__ df2 df2_neg(const df2& x) { return df2{neg2(x.hi), neg2(x.lo)}; }
+__device__ __forceinline__ df2 df2_sub(const df2& x, const df2& y) { return df2_add(x, df2_neg(y)); }
+__device__ __forceinline__ df2 df2_mul(const df2& x, const df2& y) {
+    const float2 p = __fmul2_rn(x.hi, y.hi);
+    float2 e = __ffma2_rn(x.hi, y.hi, neg2(p));
+    e = __ffma2_rn(x.hi, y.lo, __ffma2_rn(x.lo, y.hi, e));
+    return df2_fast2sum(p, e);
+}
+__device__ __forceinline__ df2 df2_mulf(const df2& x, float2 y) {
+    const float2 p = __fmul2_rn(x.hi, y);
+    const float2 e = __ffma2_rn(x.hi, y, neg2(p));
+    return df2_fast2sum(p, __ffma2_rn(x.lo, y, e));
+}
+// df_recip lane for lane (the two float reciprocals stay scalar)
+__device__ __forceinline__ df2 df2_recip(const df2& x) {
+    const float2 r = make_float2(1.0f / x.hi.x, 1.0f / x.hi.y);
+    const df2 one_minus = df2_sub(df2{bc2(1.0f), bc2(0.0f)}, df2_mulf(x, r));
+    return df2_add(df2{r, bc2(0.0f)}, df2_mulf(one_minus, r));
+}
+#endif
+
 // Symmetric (Loewdin-style, first order) orthonormalisation of two nearly orthonormal
 // vectors: a -= (a.b)/2 b, b -= (a.b)/2 a, then both normalised.
 //
@@ -456,8 +512,8 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
 // P_k = u_k u_k^T (sign arbitrary), taken from the column j of P_k with the largest diagonal:
 // u_k = P_k e_j / sqrt(P_k[j][j]), in double-float before the final rounding.
 template <bool kVectors>
-CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rhod,
-                                  float P[2][6], float om[2][2]) {
+__device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed,
+                                                      df rhod, float P[2][6], float om[2][2]) {
     // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos
     const df tw = df{1.52588e-4f, -7.040322e-12f};  // kTwoRtTwoGf = hi + lo
     df V = df_mul(df_mul(tw, Ed), rhod);
@@ -481,18 +537,21 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
     sincosf(th, &sn, &cn);
     float l0 = fmaf(2.0f * rt, cn, s);
     float l1 = fmaf(2.0f * rt, fmaf(0.8660254f, sn, -0.5f * cn), s);
-    df r[3] = {df{l0, 0.0f}, df{l1, 0.0f}, df{0.0f, 0.0f}};
-    // Newton steps: the residual in double-float, the derivative in FP32 (its relative error,
-    // ~eps * spread / gap < 2e-5, only slows the quadratic convergence by that factor).
-#pragma unroll
-    for (int k = 0; k < 2; k++)
+    // Newton steps on both roots side by side: the residual in double-float, the derivative
+    // in FP32 (its relative error, ~eps * spread / gap < 2e-5, only slows the quadratic
+    // convergence by that factor).
+    df2 x{make_float2(l0, l1), bc2(0.0f)};
+    {
+        const df2 C2 = df2_bc(c2), C1 = df2_bc(c1), C0 = df2_bc(c0);
 #pragma unroll
         for (int it = 0; it < 2; it++) {
-            const df x = r[k];
-            const df f = df_sub(df_mul(df_add(df_mul(df_sub(x, c2), x), c1), x), c0);
-            const float d = fmaf(fmaf(3.0f, x.hi, -2.0f * c2.hi), x.hi, c1.hi);
-            r[k] = df_sub(x, df{f.hi / d, 0.0f});
+            const df2 f = df2_sub(df2_mul(df2_add(df2_mul(df2_sub(x, C2), x), C1), x), C0);
+            const float2 d = __ffma2_rn(__ffma2_rn(bc2(3.0f), x.hi, bc2(-2.0f * c2.hi)), x.hi,
+                                        bc2(c1.hi));
+            x = df2_sub(x, df2{make_float2(f.hi.x / d.x, f.hi.y / d.y), bc2(0.0f)});
         }
+    }
+    df r[3] = {df2_x(x), df2_y(x), df{0.0f, 0.0f}};
     r[2] = df_sub(df_sub(c2, r[0]), r[1]);
     const float spread = fmaxf(fabsf(r[0].hi - r[1].hi), fmaxf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     const float gap = fminf(fabsf(r[0].hi - r[1].hi), fminf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
@@ -513,83 +572,89 @@ CP3_HD void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed, df rho
     H2[2] = df_add(H2[2], df_mul(V, h[2]));
     h[0] = df_add(h[0], V);
     const df loe = df_mul(df{2.534f, 8.010864e-08f}, df_recip(Ed));  // kLoEFac (= hi + lo) / E
-#pragma unroll
-    for (int kk = 0; kk < 2; kk++) {
-        const int k = kk + 1, a = 0, b = k == 1 ? 2 : 1;
-        // (H - m_a)(H - m_b) = H^2 - (m_a + m_b) H + m_a m_b
-        const df sab = df_add(r[a], r[b]), pab = df_mul(r[a], r[b]);
-        if (!kVectors) {
-            // Projectors (the beam): FP32 accuracy of P is what a single layer needs, and the
-            // numerator's cancellation (terms ~spread^2, result ~gap x spread) needs ~30 bits,
-            // not 48.  Compensated FP32: the large terms meet in one FMA (a TwoSum first on the
-            // diagonal, where H^2 and m_a m_b are both large), rounded once after the
-            // cancellation; the low words add in FP32.  ~2 ulp of P.
-            const df dka = df_sub(r[k], r[a]), dkb = df_sub(r[k], r[b]);
-            const float inv = 1.0f / ((dka.hi + dka.lo) * (dkb.hi + dkb.lo));
-#pragma unroll
-            for (int q = 0; q < 6; q++) {
-                const bool diag = q == 0 || q == 3 || q == 5;
-                float sum = H2[q].hi, err = 0.0f;
-                if (diag) {  // TwoSum (Knuth): sum + err = H2.hi + pab.hi exactly
-                    sum = CP3_FADD(H2[q].hi, pab.hi);
-                    const float bb = CP3_FADD(sum, -H2[q].hi);
-                    err = CP3_FADD(CP3_FADD(H2[q].hi, -CP3_FADD(sum, -bb)), CP3_FADD(pab.hi, -bb));
-                }
-                const float lead = fmaf(-sab.hi, h[q].hi, sum);
-                float low = CP3_FADD(err, H2[q].lo);
-                if (diag) low = CP3_FADD(low, pab.lo);
-                low = fmaf(-sab.lo, h[q].hi, fmaf(-sab.hi, h[q].lo, low));
-                P[kk][q] = CP3_FADD(lead, low) * inv;
-            }
-            const df w = df_mul(dka, loe);  // a = 0: dka = m_k - m_0
-            om[kk][0] = w.hi;
-            om[kk][1] = w.lo;
-            continue;
-        }
-        const df inv = df_recip(df_mul(df_sub(r[k], r[a]), df_sub(r[k], r[b])));
-        df Pk[6];
+    // the two projectors side by side: lane x is k = 1 (a = 0, b = 2), lane y is k = 2
+    // (a = 0, b = 1); (H - m_a)(H - m_b) = H^2 - (m_a + m_b) H + m_a m_b
+    const df2 Rk = df2_of(r[1], r[2]), Ra = df2_bc(r[0]), Rb = df2_of(r[2], r[1]);
+    const df2 sab = df2_add(Ra, Rb), pab = df2_mul(Ra, Rb);
+    const df2 dka = df2_sub(Rk, Ra), dkb = df2_sub(Rk, Rb);
+    const df2 w = df2_mul(dka, df2_bc(loe));  // omega_k = 2.534 (m_k - m_0) / E
+    om[0][0] = w.hi.x;
+    om[0][1] = w.lo.x;
+    om[1][0] = w.hi.y;
+    om[1][1] = w.lo.y;
+    if (!kVectors) {
+        // Projectors (the beam): FP32 accuracy of P is what a single layer needs, and the
+        // numerator's cancellation (terms ~spread^2, result ~gap x spread) needs ~30 bits,
+        // not 48.  Compensated FP32: the large terms meet in one FMA (a TwoSum first on the
+        // diagonal, where H^2 and m_a m_b are both large), rounded once after the
+        // cancellation; the low words add in FP32.  ~2 ulp of P.
+        const float2 den = __fmul2_rn(__fadd2_rn(dka.hi, dka.lo), __fadd2_rn(dkb.hi, dkb.lo));
+        const float2 inv = make_float2(1.0f / den.x, 1.0f / den.y);
 #pragma unroll
         for (int q = 0; q < 6; q++) {
-            df n = df_sub(H2[q], df_mul(sab, h[q]));
-            if (q == 0 || q == 3 || q == 5) n = df_add(n, pab);
-            Pk[q] = df_mul(n, inv);
+            const bool diag = q == 0 || q == 3 || q == 5;
+            const float2 H2h = bc2(H2[q].hi);
+            float2 sum = H2h, err = bc2(0.0f);
+            if (diag) {  // TwoSum (Knuth): sum + err = H2.hi + pab.hi exactly
+                sum = __fadd2_rn(H2h, pab.hi);
+                const float2 bb = __fadd2_rn(sum, neg2(H2h));
+                err = __fadd2_rn(__fadd2_rn(H2h, neg2(__fadd2_rn(sum, neg2(bb)))),
+                                 __fadd2_rn(pab.hi, neg2(bb)));
+            }
+            const float2 lead = __ffma2_rn(neg2(sab.hi), bc2(h[q].hi), sum);
+            float2 low = __fadd2_rn(err, bc2(H2[q].lo));
+            if (diag) low = __fadd2_rn(low, pab.lo);
+            low = __ffma2_rn(neg2(sab.lo), bc2(h[q].hi), __ffma2_rn(neg2(sab.hi), bc2(h[q].lo), low));
+            const float2 v = __fmul2_rn(__fadd2_rn(lead, low), inv);
+            P[0][q] = v.x;
+            P[1][q] = v.y;
         }
-        {
-            // column j with the largest diagonal (>= 1/3), selected without indexing
-            const float d0 = Pk[0].hi, d1 = Pk[3].hi, d2 = Pk[5].hi;
-            const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
-            const df c0 = j == 0 ? Pk[0] : (j == 1 ? Pk[1] : Pk[2]);
-            const df c1 = j == 0 ? Pk[1] : (j == 1 ? Pk[3] : Pk[4]);
-            const df c2 = j == 0 ? Pk[2] : (j == 1 ? Pk[4] : Pk[5]);
-            const df t = df_sqrt(j == 0 ? c0 : (j == 1 ? c1 : c2));  // sqrt(P_jj)
-            const df it = df_recip(t);
-            const df u0 = j == 0 ? t : df_mul(c0, it);
-            const df u1 = j == 1 ? t : df_mul(c1, it);
-            const df u2 = j == 2 ? t : df_mul(c2, it);
-            P[kk][0] = u0.hi + u0.lo;
-            P[kk][1] = u1.hi + u1.lo;
-            P[kk][2] = u2.hi + u2.lo;
-        }
-        const df w = df_mul(df_sub(r[k], r[0]), loe);
-        om[kk][0] = w.hi;
-        om[kk][1] = w.lo;
+        return;
+    }
+    const df2 inv = df2_recip(df2_mul(dka, dkb));
+    df2 Pk[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        df2 n = df2_sub(df2_bc(H2[q]), df2_mul(sab, df2_bc(h[q])));
+        if (q == 0 || q == 3 || q == 5) n = df2_add(n, pab);
+        Pk[q] = df2_mul(n, inv);
+    }
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++) {
+        // column j with the largest diagonal (>= 1/3), selected without indexing
+        df c[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) c[q] = kk == 0 ? df2_x(Pk[q]) : df2_y(Pk[q]);
+        const float d0 = c[0].hi, d1 = c[3].hi, d2 = c[5].hi;
+        const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
+        const df c0 = j == 0 ? c[0] : (j == 1 ? c[1] : c[2]);
+        const df c1 = j == 0 ? c[1] : (j == 1 ? c[3] : c[4]);
+        const df c2 = j == 0 ? c[2] : (j == 1 ? c[4] : c[5]);
+        const df t = df_sqrt(j == 0 ? c0 : (j == 1 ? c1 : c2));  // sqrt(P_jj)
+        const df it = df_recip(t);
+        const df u0 = j == 0 ? t : df_mul(c0, it);
+        const df u1 = j == 1 ? t : df_mul(c1, it);
+        const df u2 = j == 2 ? t : df_mul(c2, it);
+        P[kk][0] = u0.hi + u0.lo;
+        P[kk][1] = u1.hi + u1.lo;
+        P[kk][2] = u2.hi + u2.lo;
     }
     // (No orthonormalisation here: with converged roots the double-float vectors are
     // orthogonal to rounding, and an FP32 correction step would only add a rounding.)
 }
 
 // Projectors P1, P2 (00,01,02,11,12,22) and phase rates.
-CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed, df rhod, float P[2][6],
-                                float om[2][2]) {
+__device__ __forceinline__ void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed,
+                                                    df rhod, float P[2][6], float om[2][2]) {
     rotated_eigen_mixed_t<false>(p, Ed, rhod, P, om);
 }
-CP3_HD void rotated_eigen_mixed(const OscParams* __restrict__ p, double E, double rho,
-                                float P[2][6], float om[2][2]) {
+__device__ __forceinline__ void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
+                                                    double rho, float P[2][6], float om[2][2]) {
     rotated_eigen_mixed_t<false>(p, df_from(E), df_from(rho), P, om);
 }
 // Unit eigenvectors u1, u2 (P_k = u_k u_k^T) and phase rates.
-CP3_HD void rotated_eigen_vectors(const OscParams* __restrict__ p, df Ed, df rhod,
-                                  float u[2][3], float om[2][2]) {
+__device__ __forceinline__ void rotated_eigen_vectors(const OscParams* __restrict__ p, df Ed,
+                                                      df rhod, float u[2][3], float om[2][2]) {
     float out[2][6];
     rotated_eigen_mixed_t<true>(p, Ed, rhod, out, om);
 #pragma unroll

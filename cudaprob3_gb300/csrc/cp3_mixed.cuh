@@ -42,17 +42,11 @@ __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1
 }
 
 // ------------------------------------------------------------------------------------
-// Paired FP32.  sm_100+ executes FFMA2 / FMUL2 / FADD2: one instruction, two independent
-// FP32 lanes, each rounded exactly as fmaf / __fmul_rn / __fadd_rn.  On GB300 the FMA pipe
-// retires paired and scalar FMAs at the same FLOP rate, so pairing does not add arithmetic
-// throughput; it halves the issue slots of the paired work, and issue is what binds these
-// kernels.  Pairs: the real and imaginary parts of a complex entry, or the two phases
-// (k = 1, 2) of one layer.
+// Paired FP32 forms (bc2, neg2 and df2 are in cp3_device.cuh): complex entries as (re, im)
+// lanes, and the two phases (k = 1, 2) of one layer side by side.
 
-__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
 __device__ __forceinline__ float2 f2(cf c) { return make_float2(c.re, c.im); }
 __device__ __forceinline__ cf fc(float2 v) { return cf{v.x, v.y}; }
-__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
 
 // reduced_phase for the two phase rates (ah + al).x and (ah + al).y of one layer times the
 // same path length bh + bl; lane for lane the same operations and roundings.

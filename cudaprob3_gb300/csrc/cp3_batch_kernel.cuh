@@ -103,10 +103,11 @@ CP3_HD int launch_kinds(bool has_atmos, bool has_beam) {
     return (has_atmos ? kAtmos : 0) | (has_beam ? kBeam : 0);
 }
 
-// 64 registers per thread (the budget of the standalone per-bin kernel): 8 blocks per SM.
+// 72 registers per thread, 7 blocks per SM: measured 1-2 % faster on the batched atmospheric
+// and beam workloads than 64 registers (8 blocks), which spill more; 6 blocks is slower.
 // Internal linkage: each translation unit that launches it (batches, the server) has its own.
 template <int kKinds>
-static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
+static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
     constexpr int kWarps = kBlock / 32;
     __shared__ float2 s_len[kWarps][kMaxSegments];  // one trajectory per warp
     __shared__ int s_cls[kWarps][kMaxSegments];
@@ -200,7 +201,7 @@ static __global__ void __launch_bounds__(kBlock, 8) batch_kernel(const Args a) {
                 }
                 __syncwarp();
                 if (e < P.ne)
-                    atmos_bin_mixed<kTableLoad>(a.tables + P.tab_off + (size_t)e * kMixFields,
+                    atmos_bin_mixed<kTableLoad, true>(a.tables + P.tab_off + (size_t)e * kMixFields,
                                           (size_t)kMixFields * P.ne_pad, s_len[wid], s_cls[wid],
                                           nseg - 1, w, a.out + P.out_off + (size_t)ic * P.ne + e,
                                           (size_t)P.nrows * P.ne);

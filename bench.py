@@ -41,11 +41,11 @@ BATCH_SETS = 0  # --batch-sets: fewer parameter sets for the batched workloads (
 # summary).  A launch of another size is scaled by its result bytes, since traffic is the
 # output stream plus a small table/descriptor read that grows with it.
 NCU_TRAFFIC = {
-    ("atmos59", "mixed"): (5.979904e6 + 85.276672e6, 144.0e6,
+    ("atmos59", "mixed"): (5.97504e6 + 85.72416e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
-    ("batch_atmos", "mixed"): (31.19872e6 + 897.908224e6, 912.332288e6,
+    ("batch_atmos", "mixed"): (30.310912e6 + 890.566144e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
-    ("batch_beam", "mixed"): (105.383168e6 + 904.410624e6, 921.6e6,
+    ("batch_beam", "mixed"): (104.909568e6 + 878.029568e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
     ("atmos59", "fp64"): (10.150656e6 + 244.74496e6, 288.0e6,
                           "profiles/atmos_f64_kernel_59shells_2000x2000.md"),

@@ -47,10 +47,22 @@ struct Layer64 {
 // ~120 layers would accumulate), and e^{i(dh + dl)} = e^{i dh} (1 + i dl) to second order in
 // |dl| <= 1e-13: two sincos per layer instead of the three of multiply_phase_matrix
 // (math.hpp:59-75), with the reference's relative phases to ~1e-16.
+// x / E, correctly rounded, from rE = 1/E correctly rounded: q = x rE, then one correction
+// with the exact residual x - q E (an FMA).  By Markstein's theorem (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34, 1990) the corrected quotient is the correctly rounded x / E; an exhaustive-style
+// check against IEEE division (4e8 random and edge-significand operand pairs) found no
+// difference.  Three FP64 instructions instead of a full division: the reference's phase
+// roundings at a fraction of the cost on GB300's narrow FP64 pipe.
+__device__ __forceinline__ double div_by(double x, double E, double rE) {
+    const double q = __dmul_rn(x, rE);
+    return fma(fma(-q, E, x), rE, q);
+}
+
 __device__ __forceinline__ void layer64_phases(const double dmv[3], double L, double E,
-                                               Layer64& f, double arg[3]) {
+                                               double rE, Layer64& f, double arg[3]) {
 #pragma unroll
-    for (int k = 0; k < 3; k++) arg[k] = -kLoEFac * dmv[k] * L / E;
+    for (int k = 0; k < 3; k++) arg[k] = div_by(__dmul_rn(__dmul_rn(-kLoEFac, dmv[k]), L), E, rE);
 #pragma unroll
     for (int kk = 0; kk < 2; kk++) {
         const int k = kk + 1;
@@ -66,7 +78,8 @@ __device__ __forceinline__ void layer64_phases(const double dmv[3], double L, do
 
 // Table entry (10 doubles, five 16-byte words): u1, u2, dmMatVac[0..2][0], 1 unused.
 __device__ __forceinline__ void layer64_from_table(const double* __restrict__ t, double L,
-                                                   double E, Layer64& f, double arg[3]) {
+                                                   double E, double rE, Layer64& f,
+                                                   double arg[3]) {
     const double2* t2 = reinterpret_cast<const double2*>(t);
     const double2 a = __ldg(t2), b = __ldg(t2 + 1), c = __ldg(t2 + 2), d = __ldg(t2 + 3),
                   e = __ldg(t2 + 4);
@@ -77,7 +90,7 @@ __device__ __forceinline__ void layer64_from_table(const double* __restrict__ t,
     f.u[1][1] = c.x;
     f.u[1][2] = c.y;
     const double dmv[3] = {d.x, d.y, e.x};
-    layer64_phases(dmv, L, E, f, arg);
+    layer64_phases(dmv, L, E, rE, f, arg);
 }
 
 // G <- S G
@@ -337,12 +350,12 @@ __global__ void __launch_bounds__(kBlock)
     __syncthreads();
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    const double E = energies[ie];
+    const double E = energies[ie], rE = 1.0 / E;
     atmos_bin_f64(
         [&](int l, Layer64& F, double arg[3]) {
             double dmv[3];
             rotated_layer_f64(&p, E, s_rho[l], F.u, dmv);
-            layer64_phases(dmv, s_len[l], E, F, arg);
+            layer64_phases(dmv, s_len[l], E, rE, F, arg);
         },
         nseg - 1, p.w, av, ic, nc, ie, ne, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
@@ -365,12 +378,12 @@ __global__ void __launch_bounds__(kBlock)
     __syncthreads();
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    const double E = energies[ie];
+    const double E = energies[ie], rE = 1.0 / E;
     const size_t cls_stride = (size_t)kF64Fields * ne_pad;
     const double* tab = table + (size_t)ie * kF64Fields;
     atmos_bin_f64(
         [&](int l, Layer64& F, double arg[3]) {
-            layer64_from_table(tab + s_cls[l] * cls_stride, s_len[l], E, F, arg);
+            layer64_from_table(tab + s_cls[l] * cls_stride, s_len[l], E, rE, F, arg);
         },
         nseg - 1, w.w, av, ic, nc, ie, ne, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }

@@ -118,7 +118,9 @@ _LIB = None
 
 
 def library_path() -> str:
-    return _build.LIB
+    """The in-tree library, or the one CP3GB300_LIB names (e.g. the debug build with device
+    bounds checks, `python -m cudaprob3_gb300.build --device-checks`)."""
+    return os.environ.get("CP3GB300_LIB") or _build.LIB
 
 
 def lib(build_if_missing: bool = False):

@@ -49,20 +49,31 @@ def _sources_mtime() -> float:
     return newest
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile (if stale) and return the path of the shared library."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
-        return LIB
+# The debug build: the same library with the persistent kernel's arena bounds checks
+# compiled in (-DCP3_DEVICE_CHECKS).  A tile whose accesses would leave an arena is skipped
+# and reported as a status; select it at run time with CP3GB300_LIB=<this path>.
+OUT_CHECKED = os.path.join(OUT, "checked")
+LIB_CHECKED = os.path.join(OUT_CHECKED, "libcp3gb300.so")
+
+
+def build(force: bool = False, verbose: bool = False, device_checks: bool = False) -> str:
+    """Compile (if stale) and return the path of the shared library (the debug build with
+    device bounds checks when device_checks is set)."""
+    out, lib = (OUT_CHECKED, LIB_CHECKED) if device_checks else (OUT, LIB)
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _sources_mtime():
+        return lib
     nvcc = _nvcc()
-    os.makedirs(OUT, exist_ok=True)
+    os.makedirs(out, exist_ok=True)
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC,
               "-I", os.path.join(os.path.dirname(HERE), "include")]
+    if device_checks:
+        common += ["-DCP3_DEVICE_CHECKS"]
     if verbose:
         common += ["-Xptxas", "-v"]
 
     def compile_one(unit):
         src, extra = unit
-        obj = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
+        obj = os.path.join(out, src.rsplit(".", 1)[0] + ".o")
         cmd = [nvcc] + ARCH + common + extra + ["-c", os.path.join(SRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         return obj, r, cmd
@@ -74,12 +85,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         logs.append(r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + [o for o, _, _ in results]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
+    if device_checks:
+        return lib
     # bench support: scalar FMA peaks (separate library, not part of the C ABI)
     cmd = [nvcc] + ARCH + common + ["-shared", os.path.join(SRC, "cp3_peaks.cu"), "-o", PEAKS_LIB]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -93,4 +106,5 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                device_checks="--device-checks" in sys.argv))

@@ -16,6 +16,7 @@
 #include "../../include/cudaprob3_gb300.h"
 #include "cp3_host.hpp"
 #include "cp3_kernels.hpp"
+#include "cp3_trace.hpp"
 
 using namespace cp3;
 
@@ -333,6 +334,7 @@ int prepare_averaging(cp3_propagator* h, AvgArrays* av, AvgMixed* avm) {
 // atmospheric rows in n_chunks pieces, each piece's copy queued right after its kernel, so
 // the copy of one piece overlaps the computation of the next.
 int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr, int n_chunks = 1) {
+    TraceRange trace(host_dst ? "calculate_to_host" : "calculate");
     if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
         return fail(h, CP3_ERR_BAD_ARGUMENT, "neutrino type must be Neutrino or Antineutrino");
     if (!h->energies_set) return fail(h, CP3_ERR_NOT_SET, "energy list was not set");
@@ -445,6 +447,7 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
 }
 
 int fetch_result(cp3_propagator* h) {
+    TraceRange trace("fetch_result");
     if (!h->computed) return fail(h, CP3_ERR_NOT_SET, "no probabilities computed yet");
     if (h->result_on_host) return CP3_OK;
     const size_t n = h->result_bytes / (h->precision == CP3_FP64 ? 8 : 4);
@@ -738,6 +741,7 @@ int cp3_get_probability_beam(cp3_propagator* h, int ie, int t, double* out) {
 }
 
 int cp3_get_probability_arr(cp3_propagator* h, int t, double* out) {
+    TraceRange trace("get_probability_arr");
     if (int rc = check_handle(h)) return rc;
     if (int rc = check_type(h, t)) return rc;
     if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");

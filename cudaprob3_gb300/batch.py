@@ -78,6 +78,11 @@ class Batch:
         self._check(self._lib.cp3_batch_get_shape(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    def debug_withhold_tables(self, on: bool = True):
+        """Testing aid: runs hand out no eigen-table tile, so the bin tiles' bounded waits run
+        out and synchronize() raises ("wait limit")."""
+        self._check(self._lib.cp3_batch_debug_withhold_tables(self._h, int(bool(on))))
+
     def tune(self, use_cache=True):
         self._check(self._lib.cp3_batch_tune(self._h, int(bool(use_cache))))
 

@@ -105,6 +105,7 @@ struct cp3_batch {
     bool params_dirty = true;
 
     int rows_per_tile = 2, blocks_per_sm = 0, beam_chunk = 4;
+    bool withhold_tables = false;  // testing aid: cp3_batch_debug_withhold_tables
     long long total_a = 0, total_b = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev_params = nullptr, ev0 = nullptr, ev1 = nullptr;
@@ -176,7 +177,9 @@ int configure(cp3_batch* b) {
     b->total_a = a[n];
     b->total_b = bb[n];
     const std::vector<int> ai(a.begin(), a.end()), bi(bb.begin(), bb.end());
-    Header h{n, b->rows_per_tile, b->beam_chunk, (int)a[n], (int)bb[n]};
+    // Withheld tables (a testing aid): no table tile is handed out, so every atmospheric bin
+    // tile's bounded wait runs out and the run reports it.
+    Header h{n, b->rows_per_tile, b->beam_chunk, b->withhold_tables ? 0 : (int)a[n], (int)bb[n]};
     B_CUDA(b, cudaMemcpyAsync(b->d_astart.ptr, ai.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
     B_CUDA(b, cudaMemcpyAsync(b->d_bstart.ptr, bi.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream), "upload tiles");
     B_CUDA(b, cudaMemcpyAsync(b->d_hdr.ptr, &h, sizeof(Header), cudaMemcpyHostToDevice, b->stream), "upload header");
@@ -471,6 +474,14 @@ int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int 
     b->rows_per_tile = rows_per_tile;
     b->blocks_per_sm = blocks_per_sm;
     b->beam_chunk = beam_chunk;
+    if (!b->committed) return CP3_OK;
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+    return configure(b);
+}
+
+int cp3_batch_debug_withhold_tables(cp3_batch* b, int on) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    b->withhold_tables = on != 0;
     if (!b->committed) return CP3_OK;
     B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
     return configure(b);

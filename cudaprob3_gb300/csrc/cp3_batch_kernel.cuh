@@ -22,7 +22,11 @@ constexpr int kTableLoad = kLoadL2;
 constexpr int kBlock = 128;                 // threads per block (4 independent warps)
 constexpr int kMaxRowsPerTile = 16;
 constexpr int kMaxBeamChunk = 64;
-constexpr long long kSpinLimit = 20000000;  // ~seconds with the nanosleep back-off
+// A bin tile's wait for its problem's eigen tables is bounded by time (the global timer) and,
+// as a backstop, by a poll count: after kWaitLimitNs the warp reports kStatusWaitLimit and
+// goes on, so a launch always ends and the context stays usable.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
+constexpr long long kSpinLimit = 20000000;
 // Tile indices are 32-bit: a launch holds fewer tiles than this (every warp also takes one
 // index past the end).  At 32 bins per tile that is far more output than device memory.
 constexpr long long kMaxTiles = (1LL << 31) - (1LL << 24);
@@ -73,6 +77,12 @@ struct Args {
 // not built for, and (CP3_DEVICE_CHECKS builds) a tile whose accesses would have left an
 // arena, which is then skipped.
 constexpr int kStatusWaitLimit = 1, kStatusKind = 2, kStatusBounds = 3;
+
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 #ifdef CP3_DEVICE_CHECKS
 // [off, off + len) inside an arena of n elements.
@@ -197,10 +207,11 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
                 if (lane == 0) {
                     const int need = __ldg(a.a_start + p + 1) - __ldg(a.a_start + p);
                     const volatile int* done = a.done_a + p;
+                    const unsigned long long t0 = global_timer_ns();
                     long long it = 0;
                     while (*done < need) {
                         __nanosleep(256);
-                        if (++it > kSpinLimit) {
+                        if (++it > kSpinLimit || global_timer_ns() - t0 > kWaitLimitNs) {
                             atomicExch(a.status, kStatusWaitLimit);  // tables never completed: report
                             break;
                         }

@@ -286,10 +286,12 @@ CP3_HD void poly_sincos(float x, float& s, float& c) {
     c = fmaf(pc, x2, 1.0f);
 }
 
-// z = e^{-i (r + lo)} - 1 for |r| <= pi.  |r| > pi/2 is reflected through pi (pi_f - |r| is
-// exact by Sterbenz, then the low part of pi), (sin, cos) are renormalised to unit modulus
-// so that every layer matrix built from z stays unitary to rounding, and the remainder lo
-// enters to first order: e^{-i lo} = 1 - i lo.
+// z = e^{-i (r + lo)} - 1 for |r| <= pi (+ a little: the reduction's rounding can leave
+// |r| just past pi).  |r| > pi/2 is reflected through pi (pi_f - |r| is exact by Sterbenz,
+// then the low part of pi); past pi the reflected argument is negative and so is its sine,
+// which is why the sign of r multiplies sin instead of replacing its sign.  (sin, cos) are
+// renormalised to unit modulus so that every layer matrix built from z stays unitary to
+// rounding, and the remainder lo enters to first order: e^{-i lo} = 1 - i lo.
 CP3_HD void unit_phase_minus_one(float r, float lo, float& zre, float& zim) {
     const float a = fabsf(r);
     const bool refl = a > 1.57079637f;
@@ -297,7 +299,7 @@ CP3_HD void unit_phase_minus_one(float r, float lo, float& zre, float& zim) {
     float sx, cx;
     poly_sincos(x, sx, cx);
     const float inv = rsqrtf(fmaf(sx, sx, cx * cx));
-    const float sn = copysignf(sx * inv, r);
+    const float sn = r < 0.0f ? -(sx * inv) : sx * inv;
     const float cs = (refl ? -cx : cx) * inv;
     zre = fmaf(-lo, sn, cs - 1.0f);
     zim = fmaf(-lo, cs, -sn);

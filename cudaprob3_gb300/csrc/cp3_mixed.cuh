@@ -93,7 +93,10 @@ __device__ __forceinline__ void unit_phase_minus_one2(float2 r, float2 lo, float
     const float2 nn = __ffma2_rn(sx, sx, __fmul2_rn(cx, cx));
     const float2 inv = make_float2(rsqrtf(nn.x), rsqrtf(nn.y));
     const float2 si = __fmul2_rn(sx, inv);
-    const float2 sn = make_float2(copysignf(si.x, r.x), copysignf(si.y, r.y));
+    // sin(r) = sign(r) sin(|r|): the sign bit of r flips that of si (one bit operation)
+    const float2 sn = make_float2(
+        __int_as_float(__float_as_int(si.x) ^ (__float_as_int(r.x) & 0x80000000)),
+        __int_as_float(__float_as_int(si.y) ^ (__float_as_int(r.y) & 0x80000000)));
     const float2 cs = __fmul2_rn(make_float2(rx ? -cx.x : cx.x, ry ? -cx.y : cx.y), inv);
     const float2 ml = neg2(lo);
     zre = __ffma2_rn(ml, sn, __fadd2_rn(cs, bc2(-1.0f)));

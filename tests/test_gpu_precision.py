@@ -29,3 +29,23 @@ def test_precision_study_59_shells_full_grid(oracle, anti):
     assert np.abs(f64[rows] - ref).max() <= 1e-12
     err = np.abs(mixed - f64).max(axis=(0, 1))  # per channel
     assert err.max() <= 1e-5, err
+
+
+def test_beam_mixed_within_1e5_over_baselines_densities_and_low_energies():
+    """Beam mixed kernel against the FP64 kernel where the phases are largest: baselines up to
+    the Earth's diameter, densities up to the core's, energies down to 0.05 GeV (phases past
+    1e3 rad, many of them reduced to within rounding of a half-turn)."""
+    from tests.gpu_helpers import run_beam
+    en = np.geomspace(0.05, 100.0, 20000)
+    worst = 0.0
+    for i, m in enumerate(earth.gaussian_sets(4, seed=7)):
+        for dm23 in (m.dm23sq, -abs(m.dm23sq)):
+            mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, dm23]
+            for L in (295.0, 1300.0, 5000.0, 12742.0):
+                for rho in (2.6, 4.5, 13.0):
+                    for anti in (False, True):
+                        knu = -1 if anti else 1
+                        f = run_beam("fp64", mix6, knu, anti, en, rho, L)
+                        g = run_beam("mixed", mix6, knu, anti, en, rho, L)
+                        worst = max(worst, float(np.abs(f - g).max()))
+    assert worst <= 1e-5, worst

@@ -49,3 +49,30 @@ def test_beam_mixed_within_1e5_over_baselines_densities_and_low_energies():
                         g = run_beam("mixed", mix6, knu, anti, en, rho, L)
                         worst = max(worst, float(np.abs(f - g).max()))
     assert worst <= 1e-5, worst
+
+
+def test_atmospheric_mixed_within_1e5_over_models_heights_and_low_energies():
+    """Atmospheric mixed kernels (table and quadratic-density) against the FP64 kernels over
+    Earth models (PREM 4 and 12 layers, 59 shells, the quadratic PREM), production heights,
+    both orderings, nu and nubar, and energies down to 0.05 GeV, below the configurations'
+    0.1 GeV (the 59-shell grid's largest errors, ~9e-6, sit there on core-crossing rows)."""
+    cz = earth.cosine_grid(200)
+    en = np.geomspace(0.05, 100.0, 300)
+    qr, qa, qb, qc, qy = earth.PREM_4LAYER_QUAD_V2
+    models = [earth.PREM_4LAYER, earth.PREM_12LAYER, earth.synthetic_shells(59), None]
+    worst = {}
+    for mi, model in enumerate(models):
+        for m in earth.gaussian_sets(2, seed=9):
+            for dm23 in (m.dm23sq, -abs(m.dm23sq)):
+                mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, dm23]
+                for h in (0.0, 22.0, 100.0):
+                    for anti in (False, True):
+                        knu = -1 if anti else 1
+                        if model is None:
+                            args = (cz, en, qr, None, qy, h, (qa, qb, qc))
+                        else:
+                            args = (cz, en, *model, h)
+                        f = run_atmos("fp64", mix6, knu, anti, *args)
+                        g = run_atmos("mixed", mix6, knu, anti, *args)
+                        worst[mi] = max(worst.get(mi, 0.0), float(np.abs(f - g).max()))
+    assert max(worst.values()) <= 1e-5, worst

@@ -542,16 +542,29 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
     // Newton steps on both roots side by side: the residual in double-float, the derivative
     // in FP32 (its relative error, ~eps * spread / gap < 2e-5, only slows the quadratic
     // convergence by that factor).
+    //   The FP32 trigonometric roots are off by ~eps * spread^2 / gap (acos near +-1), so one
+    // step leaves a relative error of ~eps^2 (spread / gap)^4 in the gap: below 1e-10 while
+    // gap > 0.05 spread.  The eigenvector tables of the deep atmospheric chains always take a
+    // second step; the beam's projectors take it only below that gap (near the solar
+    // resonance, a few per cent of a beam grid's energies).
     df2 x{make_float2(l0, l1), bc2(0.0f)};
     {
         const df2 C2 = df2_bc(c2), C1 = df2_bc(c1), C0 = df2_bc(c0);
-#pragma unroll
-        for (int it = 0; it < 2; it++) {
+        auto newton = [&]() {
             const df2 f = df2_sub(df2_mul(df2_add(df2_mul(df2_sub(x, C2), x), C1), x), C0);
             const float2 d = __ffma2_rn(__ffma2_rn(bc2(3.0f), x.hi, bc2(-2.0f * c2.hi)), x.hi,
                                         bc2(c1.hi));
             x = df2_sub(x, df2{make_float2(f.hi.x / d.x, f.hi.y / d.y), bc2(0.0f)});
+        };
+        newton();
+        bool again = kVectors;
+        if (!kVectors) {
+            const float m2 = c2.hi - x.hi.x - x.hi.y;
+            const float d01 = fabsf(x.hi.x - x.hi.y), d02 = fabsf(x.hi.x - m2),
+                        d12 = fabsf(x.hi.y - m2);
+            again = !(fminf(d01, fminf(d02, d12)) > 0.05f * fmaxf(d01, fmaxf(d02, d12)));
         }
+        if (again) newton();
     }
     df r[3] = {df2_x(x), df2_y(x), df{0.0f, 0.0f}};
     r[2] = df_sub(df_sub(c2, r[0]), r[1]);

@@ -572,7 +572,8 @@ __global__ void __launch_bounds__(kBlock)
     layer_from_table(t0, s_len[0], F0);
 
     // shift factors of the pairs (1,0), (2,0), (2,1): the reference's d = d0[k] - d0[q] is
-    // -(omega_k - omega_q) per km of path-length shift (omega_0 = 0)
+    // -(omega_k - omega_q) per km of path-length shift (omega_0 = 0); the table holds the
+    // rates in turns per km
     const df om1{__ldg(t0 + 6), __ldg(t0 + 8)}, om2{__ldg(t0 + 7), __ldg(t0 + 9)};
     const df dom[3] = {om1, om2, df_sub(om2, om1)};
     cf sf[3][3];
@@ -590,11 +591,11 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             float lo;
-            const float r = reduced_phase(dom[q].hi, dom[q].lo, -hm.x, -hm.y, lo);  // d hm
+            const float r = reduced_turn(dom[q].hi, dom[q].lo, -hm.x, -hm.y, lo);  // d hm
             float er, ei;
-            unit_phase_minus_one(-r, -lo, er, ei);  // e^{i d hm} - 1
+            unit_turn_minus_one(-r, -lo, er, ei);  // e^{i d hm} - 1
             er += 1.0f;
-            const float sc = sinc_reference_f(-0.5f * dom[q].hi * hw);
+            const float sc = sinc_reference_f(-kPiF * dom[q].hi * hw);  // d hw / 2 in rad
 #pragma unroll
             for (int f = 0; f < 3; f++) {
                 sf[q][f].re = fmaf(pr[f] * sc, er, sf[q][f].re);

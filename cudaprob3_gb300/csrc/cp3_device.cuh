@@ -168,7 +168,8 @@ __host__ __device__ constexpr int sidx(int i, int j) {
 // same spectrum); the projectors onto the eigenvalues k = 1, 2 are
 //   P_k = (H - m_a)(H - m_b) / ((m_k - m_a)(m_k - m_b)),  {a, b} = the other two,
 // (P_0 = 1 - P_1 - P_2), and the phase rates relative to eigenvalue 0 are
-//   omega_k = 2.534 (m_k - m_0) / E   [rad / km].
+//   omega_k = 2.534 (m_k - m_0) / E   [rad / km]
+// (the mixed kernels' fallback hands them on in turns per km, omega_k / (2 pi)).
 // Projectors P1, P2 (00,01,02,11,12,22) of the rotated H for the matter masses mm (in the
 // reference's mass order).
 CP3_HD void rotated_projectors_f64(const OscParams* __restrict__ p, double E, double rho,
@@ -235,74 +236,77 @@ CP3_HD void projector_vector(const T P[6], T u[3]) {
 // ---------------------------------------------------------------------------------------
 // Mixed-precision helpers.
 
-// 2*pi in three float parts: kTwoPiA has 8 significant bits so n*kTwoPiA is exact for
-// |n| < 2^16; the sum of the three equals 2*pi to ~1e-17.
-constexpr float kTwoPiA = 6.28125f;
-constexpr float kTwoPiB = 1.9353071693331003e-3f;   // float(2pi - A)
-constexpr float kTwoPiC = 1.0253376273028358e-11f;  // float(2pi - A - B)
-constexpr float kInvTwoPi = 0.15915494309189535f;
+// Phases in turns.  The mixed kernels carry every phase rate as omega / (2 pi) (turns per
+// km), so that a phase t = omega L is reduced by subtracting an integer: with t = p + e the
+// double-float product (p its float part), n = rint(p) and p - n are exact, and the reduced
+// phase (p - n) + e keeps the product's full accuracy (~1e-11 turns for |t| < 1e3).  A
+// reduction in radians, by a float 2 pi split in parts, rounds its remainder once more
+// (~1e-8 turns), and over the ~120 layers of a core-crossing trajectory that rounding was
+// the largest error term.
 
-// Double-float product x = (ah + al)(bh + bl) reduced to [-pi, pi], returned as r + lo with
-// |lo| <= ulp(r)/2 (error of the pair ~1e-9 rad for |x| < 1e4).  The exact product of the
-// leading parts comes from an FMA (Dekker/Ogita TwoProduct), the cross terms go to the error
-// word, then a three-part Cody-Waite reduction; the last addition's remainder is kept.
-CP3_HD float reduced_phase(float ah, float al, float bh, float bl, float& lo) {
+// Double-float product t = (ah + al)(bh + bl) reduced to [-1/2, 1/2] turns, returned as
+// r + lo with |lo| <= ulp(r)/2.  The exact product of the leading parts comes from an FMA
+// (Dekker/Ogita TwoProduct), the cross terms go to the error word, the integer part is
+// subtracted exactly, and the last addition's remainder is kept.
+CP3_HD float reduced_turn(float ah, float al, float bh, float bl, float& lo) {
     const float p = CP3_FMUL(ah, bh);
     float e = fmaf(ah, bh, -p);
     e = fmaf(ah, bl, e);
     e = fmaf(al, bh, e);
-    const float n = rintf(p * kInvTwoPi);
-    float r = fmaf(-n, kTwoPiA, p);
-    r = fmaf(-n, kTwoPiB, r);
-    r = fmaf(-n, kTwoPiC, r);
-    const float s = CP3_FADD(r, e);
-    lo = CP3_FADD(CP3_FADD(r, -s), e);  // Fast2Sum remainder (|r| >= |e| or r = 0)
+    const float f = CP3_FADD(p, -rintf(p));  // exact
+    const float s = CP3_FADD(f, e);
+    lo = CP3_FADD(CP3_FADD(f, -s), e);  // Fast2Sum remainder (second order where |f| < |e|)
     return s;
 }
 
-// sin and cos of 0 <= x <= pi/2: s = x + x^3 P(x^2), c = 1 + x^2 Q(x^2), P and Q of degree 4,
-// Horner form with FMA.  The coefficients are near-minimax fits on [0, pi/2] made for this
-// file (Lawson-reweighted least squares on Chebyshev nodes, fit_sincos.py beside it); with
-// the coefficients rounded to float the truncation error is below 3e-8 in sin, 5e-9 in cos
-// and 5e-9 in the angle of (s, c), under the FP32 rounding of the evaluation itself.
-constexpr float kSin3 = -1.666666716e-01f, kSin5 = 8.333330043e-03f,
-                kSin7 = -1.984080445e-04f, kSin9 = 2.752261935e-06f,
-                kSin11 = -2.384669529e-08f;
-constexpr float kCos2 = -5.000000000e-01f, kCos4 = 4.166664183e-02f,
-                kCos6 = -1.388840377e-03f, kCos8 = 2.476188638e-05f,
-                kCos10 = -2.607710883e-07f;
+// sin(2 pi x) and cos(2 pi x) for 0 <= x <= 1/4 (turns):
+//   s = x (S1 + x^2 P(x^2)),  c = 1 + x^2 (C2 + x^2 Q(x^2)),
+// S1 = 2 pi and C2 = -2 pi^2 as float pairs (hi + lo: a float 2 pi alone would put a
+// systematic 3e-8 into every angle), P and Q of degree 3, Horner form with FMA.  P and Q are
+// near-minimax fits on [0, 1/4] made for this file (Lawson-reweighted least squares on
+// Chebyshev nodes, fit_sincos.py beside it); with every coefficient rounded to float the
+// angle of (s, c) is off by at most 4e-9 rad, under the FP32 rounding of the evaluation.
+constexpr float kS1Hi = 6.283185482e+00f, kS1Lo = -1.748455531e-07f;
+constexpr float kC2Hi = -1.973920822e+01f, kC2Lo = -5.807431762e-07f;
+constexpr float kP3 = -4.134167862e+01f, kP5 = 8.160215759e+01f, kP7 = -7.657188416e+01f,
+                kP9 = 3.968270874e+01f;
+constexpr float kQ4 = 6.493937683e+01f, kQ6 = -8.545484924e+01f, kQ8 = 6.016622543e+01f,
+                kQ10 = -2.511871529e+01f;
+constexpr float kTwoPiF = 6.283185482e+00f;
+constexpr float kPiF = 3.141592741e+00f;
 
-CP3_HD void poly_sincos(float x, float& s, float& c) {
+CP3_HD void poly_sincos_turns(float x, float& s, float& c) {
     const float x2 = x * x;
-    float ps = fmaf(kSin11, x2, kSin9);
-    ps = fmaf(ps, x2, kSin7);
-    ps = fmaf(ps, x2, kSin5);
-    ps = fmaf(ps, x2, kSin3);
-    s = fmaf(ps * x2, x, x);
-    float pc = fmaf(kCos10, x2, kCos8);
-    pc = fmaf(pc, x2, kCos6);
-    pc = fmaf(pc, x2, kCos4);
-    pc = fmaf(pc, x2, kCos2);
-    c = fmaf(pc, x2, 1.0f);
+    float ps = fmaf(kP9, x2, kP7);
+    ps = fmaf(ps, x2, kP5);
+    ps = fmaf(ps, x2, kP3);
+    ps = fmaf(ps, x2, kS1Lo);  // S1lo + x^2 P
+    s = fmaf(x, kS1Hi, x * ps);
+    float pc = fmaf(kQ10, x2, kQ8);
+    pc = fmaf(pc, x2, kQ6);
+    pc = fmaf(pc, x2, kQ4);
+    pc = fmaf(pc, x2, kC2Lo);  // C2lo + x^2 Q
+    c = fmaf(x2, pc, fmaf(x2, kC2Hi, 1.0f));
 }
 
-// z = e^{-i (r + lo)} - 1 for |r| <= pi (+ a little: the reduction's rounding can leave
-// |r| just past pi).  |r| > pi/2 is reflected through pi (pi_f - |r| is exact by Sterbenz,
-// then the low part of pi); past pi the reflected argument is negative and so is its sine,
-// which is why the sign of r multiplies sin instead of replacing its sign.  (sin, cos) are
-// renormalised to unit modulus so that every layer matrix built from z stays unitary to
-// rounding, and the remainder lo enters to first order: e^{-i lo} = 1 - i lo.
-CP3_HD void unit_phase_minus_one(float r, float lo, float& zre, float& zim) {
+// z = e^{-2 pi i (r + lo)} - 1 for |r| <= 1/2 turn (+ a little: the Fast2Sum can leave |r|
+// just past 1/2).  |r| > 1/4 is reflected through 1/2 (1/2 - |r| is exact by Sterbenz);
+// past 1/2 the reflected argument is negative and so is its sine, which is why the sign of r
+// multiplies sin instead of replacing its sign.  (sin, cos) are renormalised to unit
+// modulus so that every layer matrix built from z stays unitary to rounding, and the
+// remainder lo enters to first order: e^{-2 pi i lo} = 1 - 2 pi i lo.
+CP3_HD void unit_turn_minus_one(float r, float lo, float& zre, float& zim) {
     const float a = fabsf(r);
-    const bool refl = a > 1.57079637f;
-    const float x = refl ? (3.14159274f - a) + -8.74227766e-8f : a;
+    const bool refl = a > 0.25f;
+    const float x = refl ? 0.5f - a : a;
     float sx, cx;
-    poly_sincos(x, sx, cx);
+    poly_sincos_turns(x, sx, cx);
     const float inv = rsqrtf(fmaf(sx, sx, cx * cx));
     const float sn = r < 0.0f ? -(sx * inv) : sx * inv;
     const float cs = (refl ? -cx : cx) * inv;
-    zre = fmaf(-lo, sn, cs - 1.0f);
-    zim = fmaf(-lo, cs, -sn);
+    const float ml = -kTwoPiF * lo;
+    zre = fmaf(ml, sn, cs - 1.0f);
+    zim = fmaf(ml, cs, -sn);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -481,8 +485,9 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
         } else {
             for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
         }
-        om[k][0] = (float)omd[k];
-        om[k][1] = (float)(omd[k] - (double)om[k][0]);
+        const double t = omd[k] * 0.15915494309189535;  // turns per km: omega / (2 pi)
+        om[k][0] = (float)t;
+        om[k][1] = (float)(t - (double)om[k][0]);
     }
     if (vectors) {
         orthonormalize_pair(Pd[0], Pd[1]);
@@ -497,7 +502,8 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
 //   3. two Newton steps per root on the df64 polynomial (the third root from the trace);
 //   4. P1, P2 = (H - m_a)(H - m_b)/((m_k - m_a)(m_k - m_b)) in df64, rounded to float, with
 //      the numerator as H^2 - (m_a + m_b) H + m_a m_b from H0^2 split on the host;
-//      omega_k = 2.534 (m_k - m_0) / E in df64 (hi, lo).
+//      the phase rates in turns per km, omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E),
+//      in df64 (hi, lo).
 // Where two refined roots lie closer than 5e-3 of the spread the FP64 reference cubic takes
 // over.  Below that the double-float Newton steps are not reliably in their quadratic regime
 // (FP32 starting roots near a double root are off by ~sqrt(eps) of the spread, and Newton
@@ -586,13 +592,14 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
     H2[1] = df_add(H2[1], df_mul(V, h[1]));
     H2[2] = df_add(H2[2], df_mul(V, h[2]));
     h[0] = df_add(h[0], V);
-    const df loe = df_mul(df{2.534f, 8.010864e-08f}, df_recip(Ed));  // kLoEFac (= hi + lo) / E
+    // kLoEFac / (2 pi E): phase rates in turns per km (kLoEFac / (2 pi) = hi + lo)
+    const df loe = df_mul(df{4.032986164e-01f, 9.385560773e-09f}, df_recip(Ed));
     // the two projectors side by side: lane x is k = 1 (a = 0, b = 2), lane y is k = 2
     // (a = 0, b = 1); (H - m_a)(H - m_b) = H^2 - (m_a + m_b) H + m_a m_b
     const df2 Rk = df2_of(r[1], r[2]), Ra = df2_bc(r[0]), Rb = df2_of(r[2], r[1]);
     const df2 sab = df2_add(Ra, Rb), pab = df2_mul(Ra, Rb);
     const df2 dka = df2_sub(Rk, Ra), dkb = df2_sub(Rk, Rb);
-    const df2 w = df2_mul(dka, df2_bc(loe));  // omega_k = 2.534 (m_k - m_0) / E
+    const df2 w = df2_mul(dka, df2_bc(loe));  // omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E)
     om[0][0] = w.hi.x;
     om[0][1] = w.lo.x;
     om[1][0] = w.hi.y;

@@ -11,9 +11,9 @@ namespace cp3 {
 // Fields of one (density class, energy) entry of the eigen tables.
 constexpr int kF64Fields = 10;  // u1 (3), u2 (3) rotated-basis unit eigenvectors,
                                 // dmMatVac[k][0] (3), 1 unused (one 80-byte entry)
-constexpr int kMixFields = 12;  // u1 (3), u2 (3) real unit eigenvectors; omega_1, omega_2
-                                // double-float as (hi1, hi2, lo1, lo2); 2 unused (one 48-byte
-                                // entry per (class, energy))
+constexpr int kMixFields = 12;  // u1 (3), u2 (3) real unit eigenvectors; omega_1, omega_2 in
+                                // turns per km, double-float as (hi1, hi2, lo1, lo2); 2 unused
+                                // (one 48-byte entry per (class, energy))
 
 inline int pad_energies(int ne) { return (ne + 31) / 32 * 32; }
 

@@ -9,7 +9,8 @@ namespace cp3 {
 
 // ------------------------------------------------------------------------------------
 // Mixed: the same physics, rearranged for FP32.
-//   T_l = W S_l W^+,  S_l = 1 + z1 u1 u1^T + z2 u2 u2^T,  z_k = e^{-i omega_k L_l} - 1,
+//   T_l = W S_l W^+,  S_l = 1 + z1 u1 u1^T + z2 u2 u2^T,  z_k = e^{-i omega_k L_l} - 1
+// (omega_k carried in turns, omega_k / 2 pi, so that the phase reduction is exact),
 // with u_k the real unit eigenvectors of H0 + V e0 e0^T (S_l is complex symmetric), and
 //   A   = W (S_1..S_{M-1}) S_M (S_{M-1}..S_1) S_0 W^+ = W (B^T S_M B) S_0 W^+,
 // with B = S_{M-1}..S_1, because S_l^T = S_l.  That is M+1 layer applications per bin
@@ -48,48 +49,44 @@ __device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1
 __device__ __forceinline__ float2 f2(cf c) { return make_float2(c.re, c.im); }
 __device__ __forceinline__ cf fc(float2 v) { return cf{v.x, v.y}; }
 
-// reduced_phase for the two phase rates (ah + al).x and (ah + al).y of one layer times the
-// same path length bh + bl; lane for lane the same operations and roundings.
-__device__ __forceinline__ float2 reduced_phase2(float2 ah, float2 al, float bh, float bl,
-                                                 float2& lo) {
+// reduced_turn for the two phase rates (ah + al).x and (ah + al).y of one layer (turns per
+// km) times the same path length bh + bl; lane for lane the same operations and roundings.
+__device__ __forceinline__ float2 reduced_turn2(float2 ah, float2 al, float bh, float bl,
+                                                float2& lo) {
     const float2 B = bc2(bh);
     const float2 p = __fmul2_rn(ah, B);
     float2 e = __ffma2_rn(ah, B, neg2(p));
     e = __ffma2_rn(ah, bc2(bl), e);
     e = __ffma2_rn(al, B, e);
-    const float2 q = __fmul2_rn(p, bc2(kInvTwoPi));
-    const float2 mn = make_float2(-rintf(q.x), -rintf(q.y));
-    float2 r = __ffma2_rn(mn, bc2(kTwoPiA), p);
-    r = __ffma2_rn(mn, bc2(kTwoPiB), r);
-    r = __ffma2_rn(mn, bc2(kTwoPiC), r);
-    const float2 s = __fadd2_rn(r, e);
-    lo = __fadd2_rn(__fadd2_rn(r, neg2(s)), e);
+    const float2 f = __fadd2_rn(p, make_float2(-rintf(p.x), -rintf(p.y)));  // exact
+    const float2 s = __fadd2_rn(f, e);
+    lo = __fadd2_rn(__fadd2_rn(f, neg2(s)), e);
     return s;
 }
 
-// poly_sincos of two arguments, lane for lane.
-__device__ __forceinline__ void poly_sincos2(float2 x, float2& s, float2& c) {
+// poly_sincos_turns of two arguments, lane for lane.
+__device__ __forceinline__ void poly_sincos_turns2(float2 x, float2& s, float2& c) {
     const float2 x2 = __fmul2_rn(x, x);
-    float2 ps = __ffma2_rn(bc2(kSin11), x2, bc2(kSin9));
-    ps = __ffma2_rn(ps, x2, bc2(kSin7));
-    ps = __ffma2_rn(ps, x2, bc2(kSin5));
-    ps = __ffma2_rn(ps, x2, bc2(kSin3));
-    s = __ffma2_rn(__fmul2_rn(ps, x2), x, x);
-    float2 pc = __ffma2_rn(bc2(kCos10), x2, bc2(kCos8));
-    pc = __ffma2_rn(pc, x2, bc2(kCos6));
-    pc = __ffma2_rn(pc, x2, bc2(kCos4));
-    pc = __ffma2_rn(pc, x2, bc2(kCos2));
-    c = __ffma2_rn(pc, x2, bc2(1.0f));
+    float2 ps = __ffma2_rn(bc2(kP9), x2, bc2(kP7));
+    ps = __ffma2_rn(ps, x2, bc2(kP5));
+    ps = __ffma2_rn(ps, x2, bc2(kP3));
+    ps = __ffma2_rn(ps, x2, bc2(kS1Lo));
+    s = __ffma2_rn(x, bc2(kS1Hi), __fmul2_rn(x, ps));
+    float2 pc = __ffma2_rn(bc2(kQ10), x2, bc2(kQ8));
+    pc = __ffma2_rn(pc, x2, bc2(kQ6));
+    pc = __ffma2_rn(pc, x2, bc2(kQ4));
+    pc = __ffma2_rn(pc, x2, bc2(kC2Lo));
+    c = __ffma2_rn(x2, pc, __ffma2_rn(x2, bc2(kC2Hi), bc2(1.0f)));
 }
 
-// unit_phase_minus_one of two phases, lane for lane: z_k = zre.k + i zim.k.
-__device__ __forceinline__ void unit_phase_minus_one2(float2 r, float2 lo, float2& zre,
-                                                      float2& zim) {
+// unit_turn_minus_one of two phases, lane for lane: z_k = zre.k + i zim.k.
+__device__ __forceinline__ void unit_turn_minus_one2(float2 r, float2 lo, float2& zre,
+                                                     float2& zim) {
     const float2 a = make_float2(fabsf(r.x), fabsf(r.y));
-    const bool rx = a.x > 1.57079637f, ry = a.y > 1.57079637f;
-    const float2 t = __fadd2_rn(__fadd2_rn(bc2(3.14159274f), neg2(a)), bc2(-8.74227766e-8f));
+    const bool rx = a.x > 0.25f, ry = a.y > 0.25f;
+    const float2 t = __fadd2_rn(bc2(0.5f), neg2(a));
     float2 sx, cx;
-    poly_sincos2(make_float2(rx ? t.x : a.x, ry ? t.y : a.y), sx, cx);
+    poly_sincos_turns2(make_float2(rx ? t.x : a.x, ry ? t.y : a.y), sx, cx);
     const float2 nn = __ffma2_rn(sx, sx, __fmul2_rn(cx, cx));
     const float2 inv = make_float2(rsqrtf(nn.x), rsqrtf(nn.y));
     const float2 si = __fmul2_rn(sx, inv);
@@ -98,7 +95,7 @@ __device__ __forceinline__ void unit_phase_minus_one2(float2 r, float2 lo, float
         __int_as_float(__float_as_int(si.x) ^ (__float_as_int(r.x) & 0x80000000)),
         __int_as_float(__float_as_int(si.y) ^ (__float_as_int(r.y) & 0x80000000)));
     const float2 cs = __fmul2_rn(make_float2(rx ? -cx.x : cx.x, ry ? -cx.y : cx.y), inv);
-    const float2 ml = neg2(lo);
+    const float2 ml = __fmul2_rn(lo, bc2(-kTwoPiF));
     zre = __ffma2_rn(ml, sn, __fadd2_rn(cs, bc2(-1.0f)));
     zim = __ffma2_rn(ml, cs, neg2(sn));
 }
@@ -108,7 +105,8 @@ __device__ __forceinline__ void unit_phase_minus_one2(float2 r, float2 lo, float
 enum TableLoad { kLoadReadOnly = 0, kLoadL2 = 1 };
 
 // t points at this bin's 48-byte table entry: u1 (3), u2 (3), then the phase rates
-// omega_1, omega_2 as double-floats with the two high parts side by side and the two low
+// omega_1, omega_2 in turns per km (omega / 2 pi) as double-floats with the two high parts
+// side by side and the two low
 // parts side by side (so that each pair is one aligned 8-byte register pair of the float4
 // loads), 2 unused: [u1 | u2 | om1.hi om2.hi | om1.lo om2.lo | 0 0].
 struct TableEntry {
@@ -131,8 +129,8 @@ __device__ __forceinline__ void layer_from_entry(const TableEntry& e, float2 L, 
     f.u[1][2] = e.b.y;
     float2 lo, zr, zi;
     const float2 r =
-        reduced_phase2(make_float2(e.b.z, e.b.w), make_float2(e.c.x, e.c.y), L.x, L.y, lo);
-    unit_phase_minus_one2(r, lo, zr, zi);
+        reduced_turn2(make_float2(e.b.z, e.b.w), make_float2(e.c.x, e.c.y), L.x, L.y, lo);
+    unit_turn_minus_one2(r, lo, zr, zi);
     f.z[0][0] = zr.x;
     f.z[0][1] = zi.x;
     f.z[1][0] = zr.y;
@@ -421,9 +419,9 @@ __device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict
     float om[2][2];
     rotated_eigen_vectors(p, df_from(E), df_from(rho_e), f.u, om);
     float2 lo, zr, zi;
-    const float2 r = reduced_phase2(make_float2(om[0][0], om[1][0]),
-                                    make_float2(om[0][1], om[1][1]), L.x, L.y, lo);
-    unit_phase_minus_one2(r, lo, zr, zi);
+    const float2 r = reduced_turn2(make_float2(om[0][0], om[1][0]),
+                                   make_float2(om[0][1], om[1][1]), L.x, L.y, lo);
+    unit_turn_minus_one2(r, lo, zr, zi);
     f.z[0][0] = zr.x;
     f.z[0][1] = zi.x;
     f.z[1][0] = zr.y;
@@ -442,9 +440,9 @@ __device__ __forceinline__ void beam_bin_mixed(const OscParams* __restrict__ p, 
     rotated_eigen_mixed(p, E, rho_e, P, om);
     for (int j = 0; j < nL; j++) {
         float2 lo, zr, zi;
-        const float2 r = reduced_phase2(make_float2(om[0][0], om[1][0]),
-                                        make_float2(om[0][1], om[1][1]), L[j].x, L[j].y, lo);
-        unit_phase_minus_one2(r, lo, zr, zi);
+        const float2 r = reduced_turn2(make_float2(om[0][0], om[1][0]),
+                                       make_float2(om[0][1], om[1][1]), L[j].x, L[j].y, lo);
+        unit_turn_minus_one2(r, lo, zr, zi);
         const float z[2][2] = {{zr.x, zi.x}, {zr.y, zi.y}};
         cs6 S;
         layer_matrix(z, P[0], P[1], S);

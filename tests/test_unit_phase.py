@@ -1,6 +1,7 @@
-"""The mixed kernels' unit phase factor e^{-i r} - 1 (unit_phase_minus_one) on the host,
-built with nvcc: accurate to 3e-7 over |r| <= pi plus the overshoot the FP32 range reduction
-can leave near a half-turn, where an earlier form took the sine's sign from r alone."""
+"""The mixed kernels' phase arithmetic in turns on the host, built with nvcc: the unit phase
+factor e^{-2 pi i r} - 1 (unit_turn_minus_one) to 3e-7 over |r| <= 1/2 turn plus the
+overshoot past a half-turn (where an earlier form took the sine's sign from r alone), and
+the exact range reduction of double-float products (reduced_turn) to 1e-10 turns."""
 import os
 import shutil
 import subprocess
@@ -11,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(os.path.dirname(HERE), "cudaprob3_gb300", "csrc")
 
 
-def test_unit_phase_factor_past_pi(tmp_path):
+def test_phase_factor_and_turn_reduction(tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not found")

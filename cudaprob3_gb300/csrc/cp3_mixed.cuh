@@ -289,13 +289,12 @@ __device__ __forceinline__ void store_probabilities(const cg9& A2, float c, floa
 }
 
 // Trajectories crossing at least this many shells get the Newton-Schulz step.  Measured max
-// |mixed - FP64| per number of shells M crossed (59-shell 2000 x 2000 grid, nu and nubar):
-// without the step it grows from ~1e-6 to 4.6e-6 at M = 12 and 9.5e-6 at M = 59; with it the
-// deep rows stay at 1.3e-6 (M = 16) to 6.7e-6 (M = 59).  From M = 16 on, the grid's max stays
-// 6.66e-6 and a PREM-12 grid's (M <= 12) is 4.2e-6, while the step's ~190 FMA-pipe operations
-// per bin are saved on every shallower trajectory (the batched PREM-12 workload: 10.0 ->
-// 9.3 ms).
-constexpr int kNewtonSchulzMinShells = 16;
+// |mixed - FP64| on the 59-shell 2000 x 2000 grid (nu and nubar) with the step from M >= 2 /
+// 6 / 16 / never: 2.2e-6 / 3.1e-6 / 6.3e-6 / 1.1e-5, the per-bin kernel 0.206 / 0.203 /
+// 0.201 / 0.197 ms; on a PREM-12 grid 1.1e-6 / 2.2e-6 / 4.6e-6 / 4.6e-6, the batched PREM-12
+// workload 9.95 / 9.66 / 9.27 / 9.27 ms.  Without the step the error grows with the number
+// of FP32 layer applications (unitarity drift, 1.7e-6 at M = 2, 5e-6 at M = 12).
+constexpr int kNewtonSchulzMinShells = 6;
 
 struct WParams {
     float c, s, er, ei;

@@ -15,8 +15,8 @@ namespace cp3 {
 //   A   = W (S_1..S_{M-1}) S_M (S_{M-1}..S_1) S_0 W^+ = W (B^T S_M B) S_0 W^+,
 // with B = S_{M-1}..S_1, because S_l^T = S_l.  That is M+1 layer applications per bin
 // instead of the reference's 2M-1 products; each applies S as two rank-1 updates,
-// G += z_k u_k (u_k^T G), 96 FMA-pipe instructions against 132 for forming S and a
-// symmetric-by-general product.
+// G += z_k u_k (u_k^T G): 96 FMAs (48 of them paired over re/im) against 132 for forming S
+// and a symmetric-by-general product.
 
 struct cs6 {  // complex symmetric 3x3
     cf a[6];
@@ -105,10 +105,9 @@ __device__ __forceinline__ void unit_turn_minus_one2(float2 r, float2 lo, float2
 enum TableLoad { kLoadReadOnly = 0, kLoadL2 = 1 };
 
 // t points at this bin's 48-byte table entry: u1 (3), u2 (3), then the phase rates
-// omega_1, omega_2 in turns per km (omega / 2 pi) as double-floats with the two high parts
-// side by side and the two low
-// parts side by side (so that each pair is one aligned 8-byte register pair of the float4
-// loads), 2 unused: [u1 | u2 | om1.hi om2.hi | om1.lo om2.lo | 0 0].
+// omega_1, omega_2 in turns per km (omega / 2 pi) as double-floats, the two high parts side
+// by side and the two low parts side by side (each pair one aligned 8-byte register pair of
+// the float4 loads), 2 unused: [u1 | u2 | om1.hi om2.hi | om1.lo om2.lo | 0 0].
 struct TableEntry {
     float4 a, b, c;
 };

@@ -76,7 +76,7 @@ struct cp3_propagator {
 
     DevBuf<double> d_energies;
     DevBuf<float2> d_energies_df, d_cls_rho_df;  // mixed kernels: (hi, lo) pairs split here
-    DevBuf<int> d_seg_off, d_seg_cls;
+    DevBuf<int> d_seg_off;
     DevBuf<double> d_seg_len, d_cls_rho, d_seg_rho;
     DevBuf<double> d_ph_prob, d_ph_shift, d_air_cm;  // production-height averaging (FP64)
     DevBuf<float> d_ph_prob_f, d_ph_hw;              // ... and its float form (mixed)
@@ -221,10 +221,7 @@ int prepare_atmos(cp3_propagator* h) {
     const TrajectoryTable& t = h->traj;
     const size_t nseg = t.len_km.size();
     CP3_CUDA(h, h->d_seg_off.reserve(t.offset.size()), "allocate trajectories");
-    CP3_CUDA(h, h->d_seg_cls.reserve(nseg), "allocate trajectories");
     CP3_CUDA(h, cudaMemcpy(h->d_seg_off.ptr, t.offset.data(), sizeof(int) * t.offset.size(),
-                           cudaMemcpyHostToDevice), "upload trajectories");
-    CP3_CUDA(h, cudaMemcpy(h->d_seg_cls.ptr, t.cls.data(), sizeof(int) * nseg,
                            cudaMemcpyHostToDevice), "upload trajectories");
     if (h->precision == CP3_FP64) {
         CP3_CUDA(h, h->d_seg_len.reserve(nseg), "allocate trajectories");
@@ -391,14 +388,14 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
                                            h->d_seg_rho.ptr, h->nc, av, h->d_result.ptr, s, rr);
             if (mixed && avm.nb > 0)
                 return launch_atmos_mixed_avg(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
-                                              h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc, avm,
+                                              h->d_seg_len_df.ptr, h->nc, avm,
                                               (float*)h->d_result.ptr, s, rr);
             if (mixed)
                 return launch_atmos_mixed(p, h->d_table32.ptr, h->ne, h->d_seg_off.ptr,
-                                          h->d_seg_len_df.ptr, h->d_seg_cls.ptr, h->nc,
+                                          h->d_seg_len_df.ptr, h->nc,
                                           (float*)h->d_result.ptr, s, rr);
             return launch_atmos_f64(p, h->d_energies.ptr, h->ne, h->d_table64.ptr,
-                                    h->d_seg_off.ptr, h->d_seg_len.ptr, h->d_seg_cls.ptr, h->nc,
+                                    h->d_seg_off.ptr, h->d_seg_len.ptr, h->nc,
                                     av, (double*)h->d_result.ptr, s, rr);
         };
         if (!host_dst) {

@@ -363,18 +363,13 @@ __global__ void __launch_bounds__(kBlock)
 __global__ void __launch_bounds__(kBlock)
     atmos_f64_kernel(const double* __restrict__ energies, int ne, int ne_pad,
                      const double* __restrict__ table, const int* __restrict__ seg_off,
-                     const double* __restrict__ seg_len, const int* __restrict__ seg_cls,
-                     int ic0, int nc, const __grid_constant__ WParams64 w, AvgInput av,
-                     double* __restrict__ out) {
+                     const double* __restrict__ seg_len, int ic0, int nc,
+                     const __grid_constant__ WParams64 w, AvgInput av, double* __restrict__ out) {
     __shared__ double s_len[kMaxSegments];
-    __shared__ int s_cls[kMaxSegments];
     const int ic = ic0 + blockIdx.y;
     const int s0 = seg_off[ic];
     const int nseg = seg_off[ic + 1] - s0;
-    for (int i = threadIdx.x; i < nseg; i += kBlock) {
-        s_len[i] = seg_len[s0 + i];
-        s_cls[i] = seg_cls[s0 + i];
-    }
+    for (int i = threadIdx.x; i < nseg; i += kBlock) s_len[i] = seg_len[s0 + i];
     __syncthreads();
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
@@ -383,7 +378,7 @@ __global__ void __launch_bounds__(kBlock)
     const double* tab = table + (size_t)ie * kF64Fields;
     atmos_bin_f64(
         [&](int l, Layer64& F, double arg[3]) {
-            layer64_from_table(tab + s_cls[l] * cls_stride, s_len[l], E, rE, F, arg);
+            layer64_from_table(tab + l * cls_stride, s_len[l], E, rE, F, arg);  // class l
         },
         nseg - 1, w.w, av, ic, nc, ie, ne, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
@@ -393,21 +388,17 @@ __global__ void __launch_bounds__(kBlock)
 __global__ void __launch_bounds__(kBlock)
     atmos_mixed_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
                        const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
-                       const int* __restrict__ seg_cls, int ic0, int nc, float* __restrict__ out) {
+                       int ic0, int nc, float* __restrict__ out) {
     __shared__ float2 s_len[kMaxSegments];
-    __shared__ int s_cls[kMaxSegments];
     const int ic = ic0 + blockIdx.y;
     const int s0 = seg_off[ic];
     const int nseg = seg_off[ic + 1] - s0;
-    for (int i = threadIdx.x; i < nseg; i += kBlock) {
-        s_len[i] = seg_len[s0 + i];
-        s_cls[i] = seg_cls[s0 + i];
-    }
+    for (int i = threadIdx.x; i < nseg; i += kBlock) s_len[i] = seg_len[s0 + i];
     __syncthreads();
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
-    atmos_bin_mixed(table + (size_t)ie * kMixFields, (size_t)kMixFields * ne_pad, s_len, s_cls,
-                    nseg - 1, w, out + (size_t)ic * ne + ie, (size_t)nc * ne);
+    atmos_bin_mixed(table + (size_t)ie * kMixFields, (size_t)kMixFields * ne_pad, s_len, nseg - 1,
+                    w, out + (size_t)ic * ne + ie, (size_t)nc * ne);
 }
 
 // Mixed atmospheric bins, quadratic density: every segment solves its own eigen-system.
@@ -449,7 +440,7 @@ __global__ void __launch_bounds__(kBlock)
 
 cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
                              const double* table, const int* seg_off, const double* seg_len,
-                             const int* seg_cls, int n_cosines, const AvgArrays& avg, double* out,
+                             int n_cosines, const AvgArrays& avg, double* out,
                              cudaStream_t s, RowRange rr) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
@@ -460,14 +451,14 @@ cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
         const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_f64_kernel<<<grid, kBlock, 0, s>>>(energies, ne, ne_pad, table, seg_off, seg_len,
-                                                 seg_cls, ic0, n_cosines, w, av, out);
+                                                 ic0, n_cosines, w, av, out);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
-                               const int* seg_off, const float2* seg_len, const int* seg_cls,
-                               int n_cosines, float* out, cudaStream_t s, RowRange rr) {
+                               const int* seg_off, const float2* seg_len, int n_cosines,
+                               float* out, cudaStream_t s, RowRange rr) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
     const WParams w = wparams(p);
@@ -476,7 +467,7 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
         const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_mixed_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
-                                                   seg_cls, ic0, n_cosines, out);
+                                                   ic0, n_cosines, out);
     }
     return cudaGetLastError();
 }
@@ -539,24 +530,19 @@ __device__ __forceinline__ void to_flavour_f32(const cg9& A2, const WParams& w, 
 __global__ void __launch_bounds__(kBlock)
     atmos_mixed_avg_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
                            const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
-                           const int* __restrict__ seg_cls, int ic0, int nc, AvgMixed av,
-                           float* __restrict__ out) {
+                           int ic0, int nc, AvgMixed av, float* __restrict__ out) {
     __shared__ float2 s_len[kMaxSegments];
-    __shared__ int s_cls[kMaxSegments];
     const int ic = ic0 + blockIdx.y;
     const int s0 = seg_off[ic];
     const int nseg = seg_off[ic + 1] - s0;
-    for (int i = threadIdx.x; i < nseg; i += kBlock) {
-        s_len[i] = seg_len[s0 + i];
-        s_cls[i] = seg_cls[s0 + i];
-    }
+    for (int i = threadIdx.x; i < nseg; i += kBlock) s_len[i] = seg_len[s0 + i];
     __syncthreads();
     const int ie = blockIdx.x * kBlock + threadIdx.x;
     if (ie >= ne) return;
     const float* tab = table + (size_t)ie * kMixFields;
     const size_t cls_stride = (size_t)kMixFields * ne_pad;
     const int M = nseg - 1;
-    auto seg = [&](int l, Layer& F) { layer_from_table(tab + s_cls[l] * cls_stride, s_len[l], F); };
+    auto seg = [&](int l, Layer& F) { layer_from_table(tab + l * cls_stride, s_len[l], F); };
     cg9 G;
     if (M == 0) {
 #pragma unroll
@@ -568,7 +554,7 @@ __global__ void __launch_bounds__(kBlock)
         if (M >= kNewtonSchulzMinShells) newton_schulz(G);
     }
     Layer F0;
-    const float* t0 = tab + s_cls[0] * cls_stride;
+    const float* t0 = tab;  // class 0: the air
     layer_from_table(t0, s_len[0], F0);
 
     // shift factors of the pairs (1,0), (2,0), (2,1): the reference's d = d0[k] - d0[q] is
@@ -652,8 +638,8 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int ne,
-                                   const int* seg_off, const float2* seg_len, const int* seg_cls,
-                                   int n_cosines, const AvgMixed& av, float* out, cudaStream_t s,
+                                   const int* seg_off, const float2* seg_len, int n_cosines,
+                                   const AvgMixed& av, float* out, cudaStream_t s,
                                    RowRange rr) {
     if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
     const int ne_pad = pad_energies(ne);
@@ -665,7 +651,7 @@ cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int n
         const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_mixed_avg_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
-                                                       seg_cls, ic0, n_cosines, a, out);
+                                                       ic0, n_cosines, a, out);
     }
     return cudaGetLastError();
 }

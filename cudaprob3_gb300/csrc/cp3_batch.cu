@@ -97,7 +97,7 @@ struct cp3_batch {
     Buf<int> d_astart, d_bstart;
     Buf<Header> d_hdr;
     Buf<OscParams> d_params;
-    Buf<int> d_row_off, d_seg_cls, d_done, d_status;
+    Buf<int> d_row_off, d_done, d_status;
     Buf<float2> d_energies, d_cls_rho, d_seg_len, d_baselines;
     Buf<float> d_tables, d_out;
     Buf<unsigned int> d_counter;
@@ -191,7 +191,7 @@ int configure(cp3_batch* b) {
     const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, occ) : occ;
     const int grid = std::max(1, b->sms * bps);
     Args args{b->d_hdr.ptr, b->d_probs.ptr, b->d_astart.ptr, b->d_bstart.ptr, b->d_params.ptr,
-              b->d_energies.ptr, b->d_row_off.ptr, b->d_seg_len.ptr, b->d_seg_cls.ptr,
+              b->d_energies.ptr, b->d_row_off.ptr, b->d_seg_len.ptr,
               b->d_cls_rho.ptr, b->d_baselines.ptr, b->d_tables.ptr, b->d_out.ptr,
               b->d_done.ptr, b->d_counter.ptr, b->d_status.ptr,
               (long long)b->d_tables.n, (long long)b->d_out.n, (long long)b->d_seg_len.n,
@@ -223,7 +223,7 @@ int configure(cp3_batch* b) {
 int commit(cp3_batch* b) {
     const int n = (int)b->hp.size();
     if (n == 0) return bfail(b, CP3_ERR_NOT_SET, "the batch has no problems");
-    std::vector<int> row_off, seg_cls;
+    std::vector<int> row_off;
     std::vector<float2> energies, cls_rho, seg_len, baselines;
     b->probs.assign(n, Problem{});
     b->out_off.assign(n, 0);
@@ -254,10 +254,8 @@ int commit(cp3_batch* b) {
             P.row_off = (long long)row_off.size();
             const int base = (int)seg_len.size();
             for (int v : t.offset) row_off.push_back(base + v);
-            for (size_t i = 0; i < t.len_km.size(); i++) {
-                seg_len.push_back(split(t.len_km[i]));
-                seg_cls.push_back(t.cls[i]);
-            }
+            // (segment l of a row is density class l: build_trajectories numbers them so)
+            for (size_t i = 0; i < t.len_km.size(); i++) seg_len.push_back(split(t.len_km[i]));
             P.cls_off = (long long)cls_rho.size();
             cls_rho.push_back(split(0.0));
             for (int c = 1; c < P.ncls; c++) cls_rho.push_back(split(b->model.rho[c - 1] * b->model.ye[c - 1]));
@@ -289,7 +287,6 @@ int commit(cp3_batch* b) {
     B_CUDA(b, b->d_energies.alloc(energies.size()), "allocate");
     B_CUDA(b, b->d_cls_rho.alloc(cls_rho.size()), "allocate");
     B_CUDA(b, b->d_row_off.alloc(row_off.size()), "allocate");
-    B_CUDA(b, b->d_seg_cls.alloc(seg_cls.size()), "allocate");
     B_CUDA(b, b->d_seg_len.alloc(seg_len.size()), "allocate");
     B_CUDA(b, b->d_baselines.alloc(baselines.size()), "allocate");
     B_CUDA(b, b->d_tables.alloc(tab), "allocate eigen tables");
@@ -301,7 +298,6 @@ int commit(cp3_batch* b) {
     B_CUDA(b, b->d_energies.upload(energies, b->stream), "upload");
     B_CUDA(b, b->d_cls_rho.upload(cls_rho, b->stream), "upload");
     B_CUDA(b, b->d_row_off.upload(row_off, b->stream), "upload");
-    B_CUDA(b, b->d_seg_cls.upload(seg_cls, b->stream), "upload");
     B_CUDA(b, b->d_seg_len.upload(seg_len, b->stream), "upload");
     B_CUDA(b, b->d_baselines.upload(baselines, b->stream), "upload");
     if (b->h_params) cudaFreeHost(b->h_params);

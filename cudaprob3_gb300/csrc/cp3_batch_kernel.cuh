@@ -60,8 +60,7 @@ struct Args {
     const OscParams* params;
     const float2* energies;    // float pairs (hi, lo) of the energies
     const int* row_off;
-    const float2* seg_len;
-    const int* seg_cls;
+    const float2* seg_len;     // segment l of a row is density class l (0 = air)
     const float2* cls_rho;     // float pairs of the class densities rho * Ye
     const float2* baselines;
     float* tables;
@@ -134,7 +133,6 @@ template <int kKinds>
 static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
     constexpr int kWarps = kBlock / 32;
     __shared__ float2 s_len[kWarps][kMaxSegments];  // one trajectory per warp
-    __shared__ int s_cls[kWarps][kMaxSegments];
     const unsigned lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const Header hdr = *a.hdr;
@@ -236,32 +234,23 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
                 const int s0 = __ldg(ro + ic);
                 const int nseg = __ldg(ro + ic + 1) - s0;
 #ifdef CP3_DEVICE_CHECKS
-                tile_ok = tile_ok && nseg >= 1 && nseg <= kMaxSegments && span_ok(s0, nseg, a.n_seg);
+                // segment l reads the table of class l: the row's M + 1 segments need M < ncls
+                tile_ok = tile_ok && nseg >= 1 && nseg <= kMaxSegments && nseg <= P.ncls &&
+                          span_ok(s0, nseg, a.n_seg);
                 if (!tile_ok) {
                     if (lane == 0) atomicExch(a.status, kStatusBounds);
                     break;
                 }
 #endif
                 __syncwarp();  // the previous row is done with the staging
-                for (int i = (int)lane; i < nseg; i += 32) {
-                    s_len[wid][i] = __ldg(a.seg_len + s0 + i);
-                    s_cls[wid][i] = __ldg(a.seg_cls + s0 + i);
-                }
+                for (int i = (int)lane; i < nseg; i += 32) s_len[wid][i] = __ldg(a.seg_len + s0 + i);
                 __syncwarp();
-#ifdef CP3_DEVICE_CHECKS
-                bool cls_ok = true;
-                for (int i = (int)lane; i < nseg; i += 32)
-                    cls_ok = cls_ok && s_cls[wid][i] >= 0 && s_cls[wid][i] < P.ncls;
-                if (!__all_sync(0xffffffffu, cls_ok)) {
-                    if (lane == 0) atomicExch(a.status, kStatusBounds);
-                    break;
-                }
-#endif
                 if (e < P.ne)
                     atmos_bin_mixed<kTableLoad, true>(a.tables + P.tab_off + (size_t)e * kMixFields,
-                                          (size_t)kMixFields * P.ne_pad, s_len[wid], s_cls[wid],
-                                          nseg - 1, w, a.out + P.out_off + (size_t)ic * P.ne + e,
-                                          (size_t)P.nrows * P.ne);
+                                                      (size_t)kMixFields * P.ne_pad, s_len[wid],
+                                                      nseg - 1, w,
+                                                      a.out + P.out_off + (size_t)ic * P.ne + e,
+                                                      (size_t)P.nrows * P.ne);
             }
         } else {
             if (!(kKinds & kBeam)) {

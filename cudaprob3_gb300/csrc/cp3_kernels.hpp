@@ -40,14 +40,17 @@ struct RowRange {
     int begin = 0, end = -1;
 };
 
-// Atmospheric bins of an n_cosines-row result ([9][n_cosines][ne]), rows rr only.
+// Atmospheric bins of an n_cosines-row result ([9][n_cosines][ne]), rows rr only.  The
+// trajectory of row i is segments seg_off[i]..seg_off[i+1]-1 (air, then shells inwards); the
+// table class of a row's segment l is l itself (class 0 the air, class l shell l-1, as
+// build_trajectories numbers them), so no class array is read.
 cudaError_t launch_atmos_f64(const OscParams& p, const double* energies, int ne,
                              const double* table, const int* seg_off, const double* seg_len,
-                             const int* seg_cls, int n_cosines, const AvgArrays& avg, double* out,
+                             int n_cosines, const AvgArrays& avg, double* out,
                              cudaStream_t s, RowRange rr = RowRange{});
 cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
-                               const int* seg_off, const float2* seg_len, const int* seg_cls,
-                               int n_cosines, float* out, cudaStream_t s,
+                               const int* seg_off, const float2* seg_len, int n_cosines,
+                               float* out, cudaStream_t s,
                                RowRange rr = RowRange{});
 
 // Production-height averaging inputs of the mixed kernels (float, from AvgArrays on the host).
@@ -61,8 +64,8 @@ struct AvgMixed {
 
 // Mixed atmospheric bins with production-height averaging.
 cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int ne,
-                                   const int* seg_off, const float2* seg_len, const int* seg_cls,
-                                   int n_cosines, const AvgMixed& av, float* out, cudaStream_t s,
+                                   const int* seg_off, const float2* seg_len, int n_cosines,
+                                   const AvgMixed& av, float* out, cudaStream_t s,
                                    RowRange rr = RowRange{});
 
 // Atmospheric bins whose segments each carry their own electron density (quadratic model):

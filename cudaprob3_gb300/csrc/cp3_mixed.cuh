@@ -363,9 +363,10 @@ __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WPa
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
 }
 
-// One atmospheric bin from the eigen table: the trajectory's segment lengths and classes are
-// in shared memory (s_len[0..M], s_cls[0..M]); tab points at this bin's energy column of the
-// table (entry of class c at tab + c * cls_stride); probabilities go to out[ch * plane].
+// One atmospheric bin from the eigen table: the trajectory's segment lengths are in shared
+// memory (s_len[0..M]); segment l's density class is l (0 the air, l shell l-1); tab points
+// at this bin's energy column of the table (entry of class c at tab + c * cls_stride);
+// probabilities go to out[ch * plane].
 //
 // kPrefetch: each segment's entry is loaded one layer ahead of its use, so that the L2
 // latency of the table overlaps the previous layer's arithmetic (the air segment's entry
@@ -373,10 +374,9 @@ __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WPa
 // same launch; 1 % slower in the single-grid kernel, which therefore loads on use.
 template <int kLoad = kLoadReadOnly, bool kPrefetch = false>
 __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, size_t cls_stride,
-                                                const float2* s_len, const int* s_cls, int M,
-                                                const WParams& w, float* __restrict__ out,
-                                                size_t plane) {
-    auto entry = [&](int l) { return load_table_entry<kLoad>(tab + s_cls[l] * cls_stride); };
+                                                const float2* s_len, int M, const WParams& w,
+                                                float* __restrict__ out, size_t plane) {
+    auto entry = [&](int l) { return load_table_entry<kLoad>(tab + l * cls_stride); };
     if (!kPrefetch) {
         atmos_bin_mixed_with(
             [&](int l, Layer& F) { layer_from_entry(entry(l), s_len[l], F); }, M, w, out, plane);

@@ -78,16 +78,22 @@ extern "C" int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int
                           "cosine row %lld has %lld segments (1..129 allowed)", ic, len);
     }
     const int n_seg = seg_offset[n_cosines];
-    for (int s = 0; s < n_seg; s++)
-        if (seg_class[s] < 0 || seg_class[s] >= n_classes)
-            return report(err, err_len, CP3_ERR_BAD_ARGUMENT,
-                          "segment %lld has class %lld outside [0, n_classes)", s, seg_class[s]);
+    // The kernels read the table of class l for a row's segment l (the numbering of
+    // cp3_trajectory_table): any other class array is refused rather than ignored.
+    for (int ic = 0; ic < n_cosines; ic++)
+        for (int s = seg_offset[ic]; s < seg_offset[ic + 1]; s++) {
+            const int l = s - seg_offset[ic];
+            if (seg_class[s] != l || l >= n_classes)
+                return report(err, err_len, CP3_ERR_BAD_ARGUMENT,
+                              "segment %lld has class %lld: segment l of a row must be class l "
+                              "< n_classes (cp3_trajectory_table's numbering)",
+                              s, seg_class[s]);
+        }
 
-    // ---- scratch plan: [offsets][classes][lengths f64][lengths f32 pair][class rho][table] --
+    // ---- scratch plan: [offsets][lengths f64][lengths f32 pair][class rho][table] ---------
     const size_t ne_pad = (size_t)pad_energies(n_energies);
     const size_t off_f = 0;
-    const size_t cls_f = off_f + section((size_t)n_cosines + 1);
-    const size_t lend_f = cls_f + section((size_t)n_seg);
+    const size_t lend_f = off_f + section((size_t)n_cosines + 1);
     const size_t lenf_f = lend_f + section(2 * (size_t)n_seg);
     const size_t rho_f = lenf_f + section(2 * (size_t)n_seg);
     const size_t tab_f = rho_f + section(2 * (size_t)n_classes);
@@ -130,7 +136,6 @@ extern "C" int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int
     cudaError_t e = cudaSetDevice(device);
     const cudaStream_t s = (cudaStream_t)stream;
     int* d_off = reinterpret_cast<int*>(base + off_f);
-    int* d_cls = reinterpret_cast<int*>(base + cls_f);
     double* d_len = reinterpret_cast<double*>(base + lend_f);
     float2* d_len2 = reinterpret_cast<float2*>(base + lenf_f);
     double* d_rho = reinterpret_cast<double*>(base + rho_f);
@@ -140,8 +145,6 @@ extern "C" int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int
     // the scratch needs clearing: each call writes every element it later reads.
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_off, seg_offset, sizeof(int) * (n_cosines + 1), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_cls, seg_class, sizeof(int) * n_seg, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_len, seg_len_km, sizeof(double) * n_seg, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
@@ -162,7 +165,7 @@ extern "C" int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int
     build_osc_params(m, neutrino_type == CP3_ANTINEUTRINO, &p);
     if (e == cudaSuccess) e = launch_table_mixed(p, d_energies, n_energies, d_rho, n_classes, d_tab, s);
     if (e == cudaSuccess)
-        e = launch_atmos_mixed(p, d_tab, n_energies, d_off, d_len2, d_cls, n_cosines, d_out, s);
+        e = launch_atmos_mixed(p, d_tab, n_energies, d_off, d_len2, n_cosines, d_out, s);
     if (prev >= 0) cudaSetDevice(prev);
     if (e != cudaSuccess) {
         cudaGetLastError();

@@ -162,9 +162,9 @@ struct cp3_server {
 
     // registration (host), then resident device arenas
     std::vector<Template> tmpls;
-    std::vector<int> h_row_off, h_seg_cls;
+    std::vector<int> h_row_off;
     std::vector<float2> h_energies, h_cls_rho, h_seg_len, h_baselines;
-    DBuf<int> d_row_off, d_seg_cls;
+    DBuf<int> d_row_off;
     DBuf<float2> d_energies, d_cls_rho, d_seg_len, d_baselines;
     DBuf<float> d_pool;
     Pool pool;
@@ -350,7 +350,7 @@ int capture_slot(cp3_server* s, Slot& sl) {
     S_CUDA(s, sl.h_params.alloc(cap), "pinned");
     S_CUDA(s, cudaMemset(sl.d_status.ptr, 0, sizeof(int)), "memset");
     Args args{sl.d_hdr.ptr, sl.d_probs.ptr, sl.d_a.ptr, sl.d_b.ptr, sl.d_params.ptr,
-              s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr, s->d_seg_cls.ptr,
+              s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr,
               s->d_cls_rho.ptr, s->d_baselines.ptr, s->d_pool.ptr, s->d_pool.ptr,
               sl.d_done.ptr, sl.d_counter.ptr, sl.d_status.ptr,
               (long long)s->d_pool.n, (long long)s->d_pool.n, (long long)s->d_seg_len.n,
@@ -474,10 +474,8 @@ int cp3_server_add_atmos_grid(cp3_server* s, const double* cosines, int nc, cons
     T.row_off = (long long)s->h_row_off.size();
     const int base = (int)s->h_seg_len.size();
     for (int v : t.offset) s->h_row_off.push_back(base + v);
-    for (size_t i = 0; i < t.len_km.size(); i++) {
-        s->h_seg_len.push_back(split_pair(t.len_km[i]));
-        s->h_seg_cls.push_back(t.cls[i]);
-    }
+    // (segment l of a row is density class l: build_trajectories numbers them so)
+    for (size_t i = 0; i < t.len_km.size(); i++) s->h_seg_len.push_back(split_pair(t.len_km[i]));
     T.cls_off = (long long)s->h_cls_rho.size();
     s->h_cls_rho.push_back(split_pair(0.0));
     for (int c = 1; c < T.ncls; c++)
@@ -523,7 +521,6 @@ int cp3_server_start(cp3_server* s) {
     S_CUDA(s, upload(s->d_energies, s->h_energies), "upload grids");
     S_CUDA(s, upload(s->d_cls_rho, s->h_cls_rho), "upload grids");
     S_CUDA(s, upload(s->d_row_off, s->h_row_off), "upload grids");
-    S_CUDA(s, upload(s->d_seg_cls, s->h_seg_cls), "upload grids");
     S_CUDA(s, upload(s->d_seg_len, s->h_seg_len), "upload grids");
     S_CUDA(s, upload(s->d_baselines, s->h_baselines), "upload grids");
     const size_t units = s->pool_bytes / (kUnit * sizeof(float));

@@ -192,7 +192,7 @@ int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream);
  * *n_segments and *n_classes, then with arrays of those sizes: seg_offset[n_cosines + 1],
  * seg_len_km / seg_rho_e / seg_class[*n_segments] (segments l = 0..M of each cosine: air,
  * then shells inwards), class_rho_e[*n_classes] (class 0 = air; class 1 + i = shell i of the
- * constant model; poly segments have class -1). */
+ * constant model, so segment l of every row has class l; poly segments have class -1). */
 int cp3_trajectory_table(const double* radii, const double* c1, const double* c2,
                          const double* c3, const double* ye, int n_radii, int poly,
                          const double* cosines, int n_cosines, double production_height_km,
@@ -328,8 +328,9 @@ int cp3_server_stats(cp3_server* s, long long* launches, long long* completed,
  *   d_energies   device, n_energies doubles (GeV)
  *   seg_offset, seg_len_km, seg_class, class_rho_e   host arrays, exactly as filled by
  *                cp3_trajectory_table for the caller's cosines, model and production height
- *                (validated here, then copied in; pageable arrays may be reused as soon as
- *                the call returns, page-locked ones once the stream has passed this call)
+ *                (validated here: segment l of each row must have class l < n_classes; then
+ *                copied in; pageable arrays may be reused as soon as the call returns,
+ *                page-locked ones once the stream has passed this call)
  *   d_out        device, 9 * n_cosines * n_energies floats, layout [9][n_cosines][n_energies]
  *   stream       cudaStream_t (NULL = the legacy default stream); the call is asynchronous
  *                with respect to the device

@@ -36,9 +36,11 @@ def regular_result(mix, knu, anti, cz, en, model, h):
     return p.result()
 
 
-def no_alloc_result(lib, mix, knu, anti, cz, en, model, h, out_pad=0):
+def no_alloc_result(lib, mix, knu, anti, cz, en, model, h, out_pad=0, edit=None):
     import torch
     t = _abi.trajectory_table(model[0], model[1], model[2], cz, h)
+    if edit is not None:
+        edit(t)
     d_en = torch.tensor(np.asarray(en, dtype=np.float64), device="cuda")
     n_out = 9 * len(cz) * len(en)
     d_out = torch.full((n_out + out_pad,), float("nan"), dtype=torch.float32, device="cuda")
@@ -77,3 +79,21 @@ def test_no_alloc_rejects_grids_beyond_its_scratch(lib):
     rc, msg, _ = no_alloc_result(lib, m, 1, False, cz, en, earth.synthetic_shells(59), 22.0)
     assert rc == 1  # CP3_ERR_BAD_SIZE
     assert "scratch" in msg and str(8 * 1024 * 1024) in msg
+
+
+def test_no_alloc_refuses_a_class_numbering_other_than_the_segment_index(lib):
+    """The kernels read class l for a row's segment l (cp3_trajectory_table's numbering); a
+    class array that says otherwise is refused, not silently ignored."""
+    m = earth.NOMINAL
+    cz, en = earth.cosine_grid(12), earth.log_energy_grid(16)
+
+    def swap(t):
+        cls = np.array(t["seg_class"])
+        off = np.array(t["seg_offset"])
+        row = int(np.argmax(np.diff(off) >= 3))  # a row crossing two shells or more
+        cls[off[row] + 1], cls[off[row] + 2] = cls[off[row] + 2], cls[off[row] + 1]
+        t["seg_class"] = cls
+
+    rc, msg, _ = no_alloc_result(lib, m, 1, False, cz, en, earth.PREM_4LAYER, 22.0, edit=swap)
+    assert rc == 6  # CP3_ERR_BAD_ARGUMENT
+    assert "class" in msg

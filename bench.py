@@ -41,7 +41,7 @@ BATCH_SETS = 0  # --batch-sets: fewer parameter sets for the batched workloads (
 # summary).  A launch of another size is scaled by its result bytes, since traffic is the
 # output stream plus a small table/descriptor read that grows with it.
 NCU_TRAFFIC = {
-    ("atmos59", "mixed"): (5.97504e6 + 85.72416e6, 144.0e6,
+    ("atmos59", "mixed"): (5.914112e6 + 85.716992e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
     ("batch_atmos", "mixed"): (30.310912e6 + 890.566144e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),

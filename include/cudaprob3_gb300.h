@@ -82,7 +82,10 @@ int cp3_get_info(const cp3_propagator* h, int* kind, int* precision, int* n_cosi
 /* ---- setters (Propagator / AtmosCpuPropagator / BeamCpuPropagator) ----------------------- */
 
 /* Propagator::setEnergyList (propagator.hpp:213-218) + device copy
- * (atmoscudapropagator.cu:181-186).  n must equal the handle's n_energies.  GeV. */
+ * (atmoscudapropagator.cu:181-186).  n must equal the handle's n_energies.  GeV.  The list is
+ * copied into the handle's pinned staging buffer before the call returns (the caller's array
+ * may be reused at once) and uploaded asynchronously on the handle's own stream, after the
+ * handle's last compute; a compute on another stream waits for the upload. */
 int cp3_set_energies(cp3_propagator* h, const double* energies, int n);
 
 /* AtmosCpuPropagator::setCosineList (atmoscpupropagator.hpp:368-381) + device copy

@@ -87,14 +87,11 @@ __device__ __forceinline__ void unit_turn_minus_one2(float2 r, float2 lo, float2
     const float2 t = __fadd2_rn(bc2(0.5f), neg2(a));
     float2 sx, cx;
     poly_sincos_turns2(make_float2(rx ? t.x : a.x, ry ? t.y : a.y), sx, cx);
-    const float2 nn = __ffma2_rn(sx, sx, __fmul2_rn(cx, cx));
-    const float2 inv = make_float2(rsqrtf(nn.x), rsqrtf(nn.y));
-    const float2 si = __fmul2_rn(sx, inv);
-    // sin(r) = sign(r) sin(|r|): the sign bit of r flips that of si (one bit operation)
+    // sin(r) = sign(r) sin(|r|): the sign bit of r flips that of sx (one bit operation)
     const float2 sn = make_float2(
-        __int_as_float(__float_as_int(si.x) ^ (__float_as_int(r.x) & 0x80000000)),
-        __int_as_float(__float_as_int(si.y) ^ (__float_as_int(r.y) & 0x80000000)));
-    const float2 cs = __fmul2_rn(make_float2(rx ? -cx.x : cx.x, ry ? -cx.y : cx.y), inv);
+        __int_as_float(__float_as_int(sx.x) ^ (__float_as_int(r.x) & 0x80000000)),
+        __int_as_float(__float_as_int(sx.y) ^ (__float_as_int(r.y) & 0x80000000)));
+    const float2 cs = make_float2(rx ? -cx.x : cx.x, ry ? -cx.y : cx.y);
     const float2 ml = __fmul2_rn(lo, bc2(-kTwoPiF));
     zre = __ffma2_rn(ml, sn, __fadd2_rn(cs, bc2(-1.0f)));
     zim = __ffma2_rn(ml, cs, neg2(sn));

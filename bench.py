@@ -43,9 +43,9 @@ BATCH_SETS = 0  # --batch-sets: fewer parameter sets for the batched workloads (
 NCU_TRAFFIC = {
     ("atmos59", "mixed"): (5.914112e6 + 85.716992e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
-    ("batch_atmos", "mixed"): (30.310912e6 + 890.566144e6, 912.332288e6,
+    ("batch_atmos", "mixed"): (29.306624e6 + 889.875968e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
-    ("batch_beam", "mixed"): (104.909568e6 + 878.029568e6, 921.6e6,
+    ("batch_beam", "mixed"): (102.544128e6 + 876.585984e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
     ("atmos59", "fp64"): (10.150656e6 + 244.74496e6, 288.0e6,
                           "profiles/atmos_f64_kernel_59shells_2000x2000.md"),

@@ -285,11 +285,12 @@ __device__ __forceinline__ void store_probabilities(const cg9& A2, float c, floa
 }
 
 // Trajectories crossing at least this many shells get the Newton-Schulz step.  Measured max
-// |mixed - FP64| on the 59-shell 2000 x 2000 grid (nu and nubar) with the step from M >= 2 /
-// 6 / 16 / never: 2.2e-6 / 3.1e-6 / 6.3e-6 / 1.1e-5, the per-bin kernel 0.206 / 0.203 /
-// 0.201 / 0.197 ms; on a PREM-12 grid 1.1e-6 / 2.2e-6 / 4.6e-6 / 4.6e-6, the batched PREM-12
-// workload 9.95 / 9.66 / 9.27 / 9.27 ms.  Without the step the error grows with the number
-// of FP32 layer applications (unitarity drift, 1.7e-6 at M = 2, 5e-6 at M = 12).
+// |mixed - FP64| on the 59-shell 2000 x 2000 grid (nu and nubar) with the step from M >= 6 /
+// 12 / 20 / never: 2.6e-6 / 5.2e-6 / 5.4e-6 / 9.5e-6, the per-bin kernel 0.186 / 0.184 /
+// 0.182 / 0.180 ms; on a PREM-12 grid 1.9e-6 / 3.8e-6 / 3.8e-6 / 3.8e-6, the batched PREM-12
+// workload 9.00 / 8.63 / 8.62 / 8.62 ms.  Without the step the error grows with the number
+// of FP32 layer applications (unitarity drift: 1.5e-6 at M = 2, 4.4e-6 at M = 12, 9.3e-6 at
+// M = 59).
 constexpr int kNewtonSchulzMinShells = 6;
 
 struct WParams {

@@ -52,6 +52,24 @@ NCU_TRAFFIC = {
 }
 
 
+# The dominant kernel's measured pipe utilisation in the same captures: the fraction of the
+# FMA (FP32) or FP64 pipe's peak the kernel keeps busy.  The canonical roofline fraction
+# counts the reference formulation's flops, more than these kernels execute (it can exceed
+# 1); this is the utilisation of what they do execute.
+NCU_PIPE = {
+    ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7233),
+    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.4992),
+    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6531),
+    ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8903),
+}
+
+
+def ncu_pipe(workload, prec):
+    """{metric: fraction} of the committed capture, or {} if there is none."""
+    t = NCU_PIPE.get((workload, prec))
+    return {"ncu_pipe_active": {t[0]: t[1], "source": NCU_TRAFFIC[(workload, prec)][2]}} if t else {}
+
+
 def ncu_traffic(workload, prec, result_bytes):
     """(traffic bytes of one launch of result_bytes, note) from the committed capture."""
     t = NCU_TRAFFIC.get((workload, prec))
@@ -240,7 +258,8 @@ def run_batch(args, w, rank, world):
                      "traffic_note": ncu_traffic(args.workload, "mixed", info["result_bytes"])[1],
                      "kernel": "batch_kernel (one persistent launch per step)",
                      "flops_per_launch": flops,
-                     "hbm_gbs_output": round(info["result_bytes"] / (t_ms * 1e-3) / 1e9, 1)},
+                     "hbm_gbs_output": round(info["result_bytes"] / (t_ms * 1e-3) / 1e9, 1),
+                     **ncu_pipe(args.workload, "mixed")},
         "peaks_tflops": peaks,
     }
     try:
@@ -686,6 +705,7 @@ def run_ours(args, rank, world):
         "frac": round(achieved / (peak32 if prec == "mixed" else peaks.get("fp64")), 4),
         "traffic": ncu_traffic(args.workload, prec, bytes_out_launch)[0],
         "traffic_note": ncu_traffic(args.workload, prec, bytes_out_launch)[1],
+        **ncu_pipe(args.workload, prec),
         "peak_source": "live FMA-chain microbenchmark in this run (cp3_peaks.cu); the pool's "
                        "measured HBM/bf16 peaks do not apply to scalar FP pipes",
         "kernel": "atmos_mixed_kernel" if (w["kind"] == "atmos" and prec == "mixed") else

@@ -23,7 +23,8 @@ EXPORTS = (
     "cp3_trajectory_table", "cp3_set_profiling", "cp3_kernel_times", "cp3_atmos_mixed_noalloc",
     "cp3_batch_create", "cp3_batch_destroy", "cp3_batch_last_error", "cp3_batch_set_earth",
     "cp3_batch_add_atmos", "cp3_batch_add_beam", "cp3_batch_set_params", "cp3_batch_commit",
-    "cp3_batch_set_shape", "cp3_batch_get_shape", "cp3_batch_debug_withhold_tables",
+    "cp3_batch_set_shape", "cp3_batch_get_shape", "cp3_batch_set_split_tables",
+    "cp3_batch_get_split_tables", "cp3_batch_debug_withhold_tables",
     "cp3_batch_tune", "cp3_batch_run",
     "cp3_batch_synchronize", "cp3_batch_result", "cp3_batch_copy_result", "cp3_batch_info",
     "cp3_batch_parameter_bytes",
@@ -83,6 +84,8 @@ _SIGS = {
     "cp3_batch_commit": ([_h], C.c_int),
     "cp3_batch_set_shape": ([_h, C.c_int, C.c_int, C.c_int], C.c_int),
     "cp3_batch_get_shape": ([_h, _ip, _ip, _ip], C.c_int),
+    "cp3_batch_set_split_tables": ([_h, C.c_int], C.c_int),
+    "cp3_batch_get_split_tables": ([_h, _ip], C.c_int),
     "cp3_batch_debug_withhold_tables": ([_h, C.c_int], C.c_int),
     "cp3_batch_tune": ([_h, C.c_int], C.c_int),
     "cp3_batch_run": ([_h, C.c_void_p], C.c_int),

@@ -78,6 +78,15 @@ class Batch:
         self._check(self._lib.cp3_batch_get_shape(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    def set_split_tables(self, on: bool = True):
+        """Tables and bins as two launches (True) or one launch with waits (False)."""
+        self._check(self._lib.cp3_batch_set_split_tables(self._h, int(bool(on))))
+
+    def split_tables(self) -> bool:
+        v = C.c_int()
+        self._check(self._lib.cp3_batch_get_split_tables(self._h, C.byref(v)))
+        return bool(v.value)
+
     def debug_withhold_tables(self, on: bool = True):
         """Testing aid: runs hand out no eigen-table tile, so the bin tiles' bounded waits run
         out and synchronize() raises ("wait limit")."""

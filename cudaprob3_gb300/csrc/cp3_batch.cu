@@ -3,20 +3,24 @@
 // A batch holds atmospheric problems (one Earth model and production height for the batch,
 // each problem with its own cosine and energy grid) and beam problems (own energies, density
 // and one or more baselines), each with its own oscillation parameters and neutrino type.
-// One run is one launch of a persistent kernel, captured once in a CUDA graph:
+// One run is one or two launches of a persistent kernel, captured once in a CUDA graph:
 //
-//   * the grid is (SMs x resident blocks); every warp pulls tiles from one atomic counter;
+//   * the grid is (SMs x resident blocks); every warp pulls tiles from an atomic counter;
 //   * tiles [0, A) build the per-(class, energy) eigen tables of the atmospheric problems,
 //     tiles [A, A+B) compute bins: atmospheric tiles are rows_per_tile cosine rows x 32
 //     energies, beam tiles are 32 x beam_chunk energies with every baseline of the problem;
-//   * an atmospheric bin tile first waits until its own problem's table tiles are done.
-//     Those tiles were handed out before it by the same counter, so the warps holding them
-//     are running and the wait ends; it is bounded all the same (status flag on time-out);
+//   * split (the default where there are tables): a launch of the table tiles, then a
+//     launch of the bin tiles, which reads the finished tables through the read-only path;
+//   * single launch: an atmospheric bin tile first waits until its own problem's table
+//     tiles are done.  Those tiles were handed out before it by the same counter, so the
+//     warps holding them are running and the wait ends; it is bounded all the same (status
+//     flag on time-out).  The serving loop uses this form;
 //   * everything a run needs -- descriptors, tile prefix sums, parameters -- is in device
 //     memory, so the captured graph replays unchanged while parameters change between runs.
 //
-// The tile shape (rows_per_tile, blocks per SM, beam_chunk) does not change any bin's arithmetic:
-// results are bit-identical across shapes, which lets an autotuner pick it by timing alone.
+// The tile shape (rows_per_tile, blocks per SM, beam_chunk) and the split do not change any
+// bin's arithmetic: results are bit-identical across them, which lets an autotuner pick by
+// timing alone.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,6 +29,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -105,6 +110,7 @@ struct cp3_batch {
     bool params_dirty = true;
 
     int rows_per_tile = 2, blocks_per_sm = 0, beam_chunk = 4;
+    bool split_tables = true;      // tables and bins as two launches (cp3_batch_set_split_tables)
     bool withhold_tables = false;  // testing aid: cp3_batch_debug_withhold_tables
     long long total_a = 0, total_b = 0;
     cudaGraphExec_t graph = nullptr;
@@ -148,12 +154,24 @@ int bcuda(cp3_batch* b, cudaError_t e, const char* where) {
 
 using KernelFn = void (*)(Args);
 
-KernelFn kernel_for(int kinds) {
-    return kinds == kAtmos ? batch_kernel<kAtmos> : kinds == kBeam ? batch_kernel<kBeam> : batch_kernel<kBoth>;
+template <int kPhases>
+KernelFn kernel_for_phases(int kinds) {
+    return kinds == kAtmos  ? batch_kernel<kAtmos, kPhases>
+           : kinds == kBeam ? batch_kernel<kBeam, kPhases>
+                            : batch_kernel<kBoth, kPhases>;
 }
 
-int occupancy(int kinds, int* blocks) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kernel_for(kinds), kBlock, 0) == cudaSuccess ? 0 : 1;
+KernelFn kernel_for(int kinds, int phases = kPhaseAll) {
+    return phases == kPhaseTables ? kernel_for_phases<kPhaseTables>(kinds)
+           : phases == kPhaseBins ? kernel_for_phases<kPhaseBins>(kinds)
+                                  : kernel_for_phases<kPhaseAll>(kinds);
+}
+
+int occupancy(int kinds, int* blocks, int phases = kPhaseAll) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, kernel_for(kinds, phases), kBlock, 0) ==
+                   cudaSuccess
+               ? 0
+               : 1;
 }
 
 int batch_kinds(const std::vector<Problem>& probs) {
@@ -185,11 +203,19 @@ int configure(cp3_batch* b) {
     B_CUDA(b, cudaMemcpyAsync(b->d_hdr.ptr, &h, sizeof(Header), cudaMemcpyHostToDevice, b->stream), "upload header");
     B_CUDA(b, cudaStreamSynchronize(b->stream), "configure");
 
-    int occ = 0;
+    // Split launches only where there are tables to build; the withheld-tables testing aid
+    // exercises the single launch's bounded wait, so it keeps the single launch.
+    const bool split = b->split_tables && a[n] > 0 && !b->withhold_tables;
     const int kinds = batch_kinds(b->probs);
-    if (occupancy(kinds, &occ) || occ < 1) return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
+    int occ = 0, occ_tab = 0;
+    if (occupancy(kinds, &occ, split ? kPhaseBins : kPhaseAll) || occ < 1 ||
+        (split && (occupancy(kinds, &occ_tab, kPhaseTables) || occ_tab < 1)))
+        return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
     const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, occ) : occ;
     const int grid = std::max(1, b->sms * bps);
+    // The table launch needs no more warps than it has tiles.
+    const long long tab_blocks = (a[n] + kBlock / 32 - 1) / (kBlock / 32);
+    const int grid_tab = (int)std::max(1LL, std::min<long long>((long long)b->sms * occ_tab, tab_blocks));
     Args args{b->d_hdr.ptr, b->d_probs.ptr, b->d_astart.ptr, b->d_bstart.ptr, b->d_params.ptr,
               b->d_energies.ptr, b->d_row_off.ptr, b->d_seg_len.ptr,
               b->d_cls_rho.ptr, b->d_baselines.ptr, b->d_tables.ptr, b->d_out.ptr,
@@ -204,10 +230,17 @@ int configure(cp3_batch* b) {
     B_CUDA(b, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
     cudaGraph_t g;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter.ptr, 0, sizeof(unsigned int), cs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter.ptr, 0, 2 * sizeof(unsigned int), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_done.ptr, 0, sizeof(int) * std::max(n, 1), cs);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_status.ptr, 0, sizeof(int), cs);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && split) {
+        kernel_for(kinds, kPhaseTables)<<<grid_tab, kBlock, 0, cs>>>(args);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            kernel_for(kinds, kPhaseBins)<<<grid, kBlock, 0, cs>>>(args);
+            e = cudaGetLastError();
+        }
+    } else if (e == cudaSuccess) {
         kernel_for(kinds)<<<grid, kBlock, 0, cs>>>(args);
         e = cudaGetLastError();
     }
@@ -293,7 +326,7 @@ int commit(cp3_batch* b) {
     B_CUDA(b, b->d_out.alloc(out), "allocate results");
     B_CUDA(b, b->d_done.alloc(n), "allocate");
     B_CUDA(b, b->d_status.alloc(1), "allocate");
-    B_CUDA(b, b->d_counter.alloc(1), "allocate");
+    B_CUDA(b, b->d_counter.alloc(2), "allocate");
     B_CUDA(b, b->d_probs.upload(b->probs, b->stream), "upload");
     B_CUDA(b, b->d_energies.upload(energies, b->stream), "upload");
     B_CUDA(b, b->d_cls_rho.upload(cls_rho, b->stream), "upload");
@@ -341,8 +374,9 @@ std::string tune_key(cp3_batch* b) {
     const int lg = (int)std::log2((double)std::max<long long>(1, b->total_bins));
     std::string name(prop.name);
     std::replace(name.begin(), name.end(), ' ', '_');
-    // "w32": shapes of the warp-tiled kernel (entries of other kernels are never matched)
-    return "w32:" + name + ":a" + std::to_string(na > 0) + "b" + std::to_string(nb > 0) + ":bins2^" + std::to_string(lg);
+    // "w32s": shapes of the warp-tiled kernel with the launch split (entries of other kernels
+    // are never matched)
+    return "w32s:" + name + ":a" + std::to_string(na > 0) + "b" + std::to_string(nb > 0) + ":bins2^" + std::to_string(lg);
 }
 
 }  // namespace
@@ -475,6 +509,20 @@ int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int 
     return configure(b);
 }
 
+int cp3_batch_set_split_tables(cp3_batch* b, int on) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    b->split_tables = on != 0;
+    if (!b->committed) return CP3_OK;
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+    return configure(b);
+}
+
+int cp3_batch_get_split_tables(const cp3_batch* b, int* on) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (on) *on = b->split_tables ? 1 : 0;
+    return CP3_OK;
+}
+
 int cp3_batch_debug_withhold_tables(cp3_batch* b, int on) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
     b->withhold_tables = on != 0;
@@ -526,31 +574,42 @@ int cp3_batch_tune(cp3_batch* b, int use_cache) {
     const std::string key = tune_key(b), path = tune_cache_path();
     if (use_cache) {
         std::ifstream f(path);
-        std::string k;
-        int R, bps, bc;
-        while (f >> k >> R >> bps >> bc)
-            if (k == key) return cp3_batch_set_shape(b, R, bps, bc);
+        std::string line;
+        while (std::getline(f, line)) {
+            std::istringstream in(line);
+            std::string k;
+            int R, bps, bc, sp;
+            if (in >> k >> R >> bps >> bc >> sp && k == key) {
+                if (int rc = cp3_batch_set_split_tables(b, sp)) return rc;
+                return cp3_batch_set_shape(b, R, bps, bc);
+            }
+        }
     }
-    int occ = 0;
-    occupancy(batch_kinds(b->probs), &occ);
+    const int kinds = batch_kinds(b->probs);
     bool has_a = false, has_b = false;
     for (const Problem& P : b->probs) (P.kind == 0 ? has_a : has_b) = true;
     struct Shape {
-        int rows, bps, bc;
+        int rows, bps, bc, split;
     };
     // Only the dimensions the batch's problem kinds use are swept.
     std::vector<int> rows = has_a ? std::vector<int>{1, 2, 4, 8, 16} : std::vector<int>{2};
     std::vector<int> chunks = has_b ? std::vector<int>{1, 4, 16} : std::vector<int>{4};
-    std::vector<int> bps = {0};
-    if (occ > 1) bps.push_back(std::max(1, occ / 2));
+    std::vector<int> splits = has_a ? std::vector<int>{0, 1} : std::vector<int>{0};
     std::vector<Shape> cand;
-    for (int r : rows)
-        for (int bc : chunks)
-            for (int k : bps) cand.push_back({r, k, bc});
+    for (int sp : splits) {
+        int occ = 0;
+        occupancy(kinds, &occ, sp ? kPhaseBins : kPhaseAll);
+        std::vector<int> bps = {0};
+        if (occ > 1) bps.push_back(std::max(1, occ / 2));
+        for (int r : rows)
+            for (int bc : chunks)
+                for (int k : bps) cand.push_back({r, k, bc, sp});
+    }
     double best = 1e30;
     Shape pick = cand[0];
     for (const Shape& s : cand) {
-        int rc = cp3_batch_set_shape(b, s.rows, s.bps, s.bc);
+        int rc = cp3_batch_set_split_tables(b, s.split);
+        if (!rc) rc = cp3_batch_set_shape(b, s.rows, s.bps, s.bc);
         if (rc) return rc;
         double total = 0;
         for (int it = 0; it < 4; it++) {
@@ -565,11 +624,12 @@ int cp3_batch_tune(cp3_batch* b, int use_cache) {
             pick = s;
         }
     }
-    int rc = cp3_batch_set_shape(b, pick.rows, pick.bps, pick.bc);
+    int rc = cp3_batch_set_split_tables(b, pick.split);
+    if (!rc) rc = cp3_batch_set_shape(b, pick.rows, pick.bps, pick.bc);
     if (rc) return rc;
     if (use_cache) {
         std::ofstream f(path, std::ios::app);
-        if (f) f << key << " " << pick.rows << " " << pick.bps << " " << pick.bc << "\n";
+        if (f) f << key << " " << pick.rows << " " << pick.bps << " " << pick.bc << " " << pick.split << "\n";
     }
     return CP3_OK;
 }

@@ -1,7 +1,7 @@
 // cp3_batch_kernel.cuh -- the persistent many-problem kernel, shared by batches
 // (cp3_batch.cu) and the serving loop (cp3_serve.cu).  See cp3_batch.cu for the design.
 //
-// Scheduling is per warp, not per block: every warp pulls its own tiles from the shared
+// Scheduling is per warp, not per block: every warp pulls its own tiles from a shared
 // counter (the next tile's index is fetched while the current one runs) and never waits at a
 // block barrier.  A tile is 32 energies, one per lane:
 //   * table tile:        one density class of one atmospheric problem;
@@ -17,8 +17,6 @@ namespace cp3 {
 namespace batchk {
 
 constexpr int kTileE = 32;                  // energies per tile (one per lane)
-// Bin tiles read their problem's table, written by this launch's table tiles, from L2.
-constexpr int kTableLoad = kLoadL2;
 constexpr int kBlock = 128;                 // threads per block (4 independent warps)
 constexpr int kMaxRowsPerTile = 16;
 constexpr int kMaxBeamChunk = 64;
@@ -126,17 +124,30 @@ CP3_HD int launch_kinds(bool has_atmos, bool has_beam) {
     return (has_atmos ? kAtmos : 0) | (has_beam ? kBeam : 0);
 }
 
+// Which tiles a launch runs.  kPhaseAll: table and bin tiles in one launch, each atmospheric
+// bin tile waiting (bounded) for its problem's tables, which it then reads from L2 (__ldcg:
+// they were written during this launch).  Split: a kPhaseTables launch, then a kPhaseBins
+// launch in stream order, which needs no wait and reads tables an earlier launch wrote
+// through the read-only path (__ldg).  Counter 0 serves kPhaseAll and kPhaseTables launches,
+// counter 1 kPhaseBins launches.
+constexpr int kPhaseTables = 1, kPhaseBins = 2, kPhaseAll = 3;
+
 // 72 registers per thread, 7 blocks per SM: measured 1-2 % faster on the batched atmospheric
-// and beam workloads than 64 registers (8 blocks), which spill more; 6 blocks is slower.
+// and beam workloads than 64 registers (8 blocks), which spill more; 6 blocks is slower.  The
+// kPhaseBins instance fits 72 registers without spills; 64 or 56 (8 or 9 blocks) measured
+// no faster on the batched atmospheric workload.
 // Internal linkage: each translation unit that launches it (batches, the server) has its own.
-template <int kKinds>
+template <int kKinds, int kPhases = kPhaseAll>
 static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
     constexpr int kWarps = kBlock / 32;
+    constexpr int kTableLoad = kPhases == kPhaseBins ? kLoadReadOnly : kLoadL2;
     __shared__ float2 s_len[kWarps][kMaxSegments];  // one trajectory per warp
     const unsigned lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const Header hdr = *a.hdr;
-    const int total = hdr.total_a + hdr.total_b;
+    const int first = kPhases == kPhaseBins ? hdr.total_a : 0;
+    const int total = kPhases == kPhaseTables ? hdr.total_a : hdr.total_a + hdr.total_b;
+    unsigned int* const counter = a.counter + (kPhases == kPhaseBins ? 1 : 0);
 
     // The warp's current problem: tiles arrive in increasing order, so a warp's problems do
     // too and the lookup resumes from the last one.  The descriptor itself is re-read per
@@ -144,13 +155,13 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
     int p = 0, phase = -1, ready = -1, p_lo = 0, p_hi = 0;
 
     int t = 0;
-    if (lane == 0) t = (int)atomicAdd(a.counter, 1u);
+    if (lane == 0) t = first + (int)atomicAdd(counter, 1u);
     t = __shfl_sync(0xffffffffu, t, 0);
     while (t < total) {
         int next = 0;
-        if (lane == 0) next = (int)atomicAdd(a.counter, 1u);  // in flight while this tile runs
+        if (lane == 0) next = first + (int)atomicAdd(counter, 1u);  // in flight while this tile runs
 
-        const int ph = t < hdr.total_a ? 0 : 1;
+        const int ph = kPhases == kPhaseTables ? 0 : kPhases == kPhaseBins ? 1 : t < hdr.total_a ? 0 : 1;
         const int tt = ph == 0 ? t : t - hdr.total_a;
         if (ph != phase || tt >= p_hi) {
             const int* pre = ph == 0 ? a.a_start : a.b_start;
@@ -199,7 +210,7 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
                 break;
             }
             // ---- atmospheric bin tile: rows_per_tile rows x 32 energies ------------------
-            if (ready != p) {
+            if (kPhases == kPhaseAll && ready != p) {
                 // This problem's table tiles were all handed out before this tile, to warps
                 // that are running them, so the wait ends; it is bounded all the same.
                 if (lane == 0) {

@@ -2,10 +2,11 @@
 //
 // Requests (a registered grid + one parameter set + a neutrino type) are submitted from any
 // thread and return at once.  A scheduler thread admits queued requests in arrival order
-// whenever device memory and a launch slot are free, packs them into one launch of the
-// persistent kernel, and keeps going: a request that arrives while others run joins the next
-// launch, which starts on the second slot (stream) while the first is still finishing, so
-// work from consecutive launches overlaps on the device.  Grids (trajectory tables, energies,
+// whenever device memory and a launch slot are free, packs them into one run of the
+// persistent kernel (a table launch and a bin launch where there are atmospheric requests),
+// and keeps going: a request that arrives while others run joins the next run, which starts
+// on the second slot (stream) while the first is still finishing, so work from consecutive
+// runs overlaps on the device.  Grids (trajectory tables, energies,
 // class densities) are registered once and stay resident; each request's eigen table and
 // result live in a device pool until the client releases the request.  A host callback on the
 // stream stamps the completion time of every request of a launch.
@@ -42,6 +43,9 @@ int64_t now_ns() {
 constexpr size_t kUnit = 64;  // pool granularity in floats (256 bytes)
 constexpr int kServeRows = 2;       // tile shape of the serving launches: cosine rows per tile
 constexpr int kServeBeamChunk = 2;  // and 32-energy groups per beam tile
+// Launches with atmospheric requests run as a table launch and a bin launch (see
+// capture_slot).
+constexpr bool kServeSplitTables = true;
 
 // x as a float pair (hi, lo), hi + lo = x to ~48 bits.
 float2 split_pair(double x) {
@@ -342,7 +346,7 @@ int capture_slot(cp3_server* s, Slot& sl) {
     S_CUDA(s, sl.d_params.alloc(cap), "allocate");
     S_CUDA(s, sl.d_done.alloc(cap), "allocate");
     S_CUDA(s, sl.d_status.alloc(1), "allocate");
-    S_CUDA(s, sl.d_counter.alloc(1), "allocate");
+    S_CUDA(s, sl.d_counter.alloc(2), "allocate");
     S_CUDA(s, sl.h_probs.alloc(cap), "pinned");
     S_CUDA(s, sl.h_a.alloc(cap + 1), "pinned");
     S_CUDA(s, sl.h_b.alloc(cap + 1), "pinned");
@@ -355,19 +359,33 @@ int capture_slot(cp3_server* s, Slot& sl) {
               sl.d_done.ptr, sl.d_counter.ptr, sl.d_status.ptr,
               (long long)s->d_pool.n, (long long)s->d_pool.n, (long long)s->d_seg_len.n,
               (long long)s->d_energies.n};
-    // one graph per kernel instance; a launch replays the one for the kinds it holds
+    // One graph per set of problem kinds; a launch replays the one for the kinds it holds.
+    // With atmospheric requests it is a table launch, then a bin launch that reads the
+    // finished tables (no wait); a beam-only launch is the single kernel.  The table launch
+    // has a full grid: the number of table tiles changes from launch to launch, and warps
+    // without a tile return at once.
     for (int kinds = 1; kinds <= 3; kinds++) {
-        void (*kern)(Args) = kinds == kAtmos ? batch_kernel<kAtmos>
-                             : kinds == kBeam ? batch_kernel<kBeam> : batch_kernel<kBoth>;
-        int occ = 0;
+        using Kern = void (*)(Args);
+        const bool split = kServeSplitTables && (kinds & kAtmos);
+        const Kern tab = kinds == kAtmos ? batch_kernel<kAtmos, kPhaseTables> : batch_kernel<kBoth, kPhaseTables>;
+        const Kern kern = !split ? (kinds == kBeam ? batch_kernel<kBeam> : kinds == kAtmos ? batch_kernel<kAtmos>
+                                                                                           : batch_kernel<kBoth>)
+                                 : (kinds == kAtmos ? batch_kernel<kAtmos, kPhaseBins> : batch_kernel<kBoth, kPhaseBins>);
+        int occ = 0, occ_tab = 0;
         S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlock, 0), "occupancy");
+        if (split) S_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_tab, tab, kBlock, 0), "occupancy");
         const int grid = std::max(1, s->sms * std::max(occ, 1));
+        const int grid_tab = std::max(1, s->sms * std::max(occ_tab, 1));
         cudaStream_t cs;
         S_CUDA(s, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
         cudaGraph_t g;
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, sizeof(unsigned int), cs);
+        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, 2 * sizeof(unsigned int), cs);
         if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_done.ptr, 0, sizeof(int) * cap, cs);
+        if (e == cudaSuccess && split) {
+            tab<<<grid_tab, kBlock, 0, cs>>>(args);
+            e = cudaGetLastError();
+        }
         if (e == cudaSuccess) {
             kern<<<grid, kBlock, 0, cs>>>(args);
             e = cudaGetLastError();

@@ -248,10 +248,17 @@ int cp3_batch_commit(cp3_batch* b);
 int cp3_batch_set_shape(cp3_batch* b, int rows_per_tile, int blocks_per_sm, int beam_chunk);
 int cp3_batch_get_shape(const cp3_batch* b, int* rows_per_tile, int* blocks_per_sm,
                         int* beam_chunk);
+/* How a run with atmospheric problems is launched (results do not depend on it): on = 0,
+ * one persistent launch in which each problem's bin tiles wait for its eigen-table tiles;
+ * on != 0 (the default), a table launch followed by a bin launch, with no wait.  The
+ * autotuner sets it. */
+int cp3_batch_set_split_tables(cp3_batch* b, int on);
+int cp3_batch_get_split_tables(const cp3_batch* b, int* on);
 /* Testing aid for failure detection (no reference counterpart): with on != 0 the following
- * runs hand out no eigen-table tile, so every atmospheric bin tile's bounded wait (2 s) runs
- * out; cp3_batch_synchronize then returns CP3_ERR_CUDA ("wait limit") and the results of
- * atmospheric problems are undefined.  on = 0 restores normal runs.  Faults nothing. */
+ * runs are single launches that hand out no eigen-table tile, so every atmospheric bin
+ * tile's bounded wait (2 s) runs out; cp3_batch_synchronize then returns CP3_ERR_CUDA
+ * ("wait limit") and the results of atmospheric problems are undefined.  on = 0 restores
+ * normal runs.  Faults nothing. */
 int cp3_batch_debug_withhold_tables(cp3_batch* b, int on);
 /* Autotuner: times every candidate shape on this batch and keeps the fastest; use_cache != 0
  * reads and appends the choice to $CP3_TUNE_CACHE (default ~/.cache/cp3gb300_tune.txt),

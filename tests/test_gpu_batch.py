@@ -81,19 +81,24 @@ def test_batch_matches_single_propagators_and_oracle(oracle):
 
 
 def test_batch_results_do_not_depend_on_tile_shape():
+    """Tile shapes and the launch split (one launch with waits, or a table launch then a bin
+    launch) leave every result bit-identical."""
     rng = np.random.default_rng(4)
     b, probs = build_batch(earth.gaussian_sets(3, seed=13), rng)
     ref = None
-    for shape in [(1, 0, 4), (2, 0, 1), (1, 2, 16), (4, 1, 4), (8, 0, 2), (16, 0, 64)]:
-        b.set_shape(*shape)
-        b.run()
-        b.synchronize()
-        res = [b.result(pid) for _, pid, *_ in probs]
-        if ref is None:
-            ref = res
-        else:
-            for a, c in zip(ref, res):
-                assert np.array_equal(a, c), shape
+    for split in (False, True):
+        b.set_split_tables(split)
+        assert b.split_tables() == split
+        for shape in [(1, 0, 4), (2, 0, 1), (1, 2, 16), (4, 1, 4), (8, 0, 2), (16, 0, 64)]:
+            b.set_shape(*shape)
+            b.run()
+            b.synchronize()
+            res = [b.result(pid) for _, pid, *_ in probs]
+            if ref is None:
+                ref = res
+            else:
+                for a, c in zip(ref, res):
+                    assert np.array_equal(a, c), (split, shape)
 
 
 def test_batch_parameter_update_between_runs():

@@ -784,18 +784,24 @@ def cpu_sample(w, seconds, orc=None, nthreads=1):
     if w["kind"] == "atmos":
         stride = max(1, len(w["cz"]) // 8)
         if orc is not None:
+            # a warm-up (library, thread pool), then a probe of four rows per thread
+            stride = max(1, len(w["cz"]) // (4 * nthreads))
             probe = dict(w, cz=w["cz"][::stride])
+            cpu_run(dict(probe, cz=probe["cz"][:nthreads]), orc, nthreads)
             t0 = time.perf_counter()
             cpu_run(probe, orc, nthreads)
-            per_row = (time.perf_counter() - t0) / len(probe["cz"])
+            rows_per_s = len(probe["cz"]) / max(time.perf_counter() - t0, 1e-9)
             # enough rows that the dynamic schedule keeps every thread busy
-            rows = max(8 * nthreads, min(len(w["cz"]), int(seconds / max(per_row, 1e-9))))
+            rows = max(8 * nthreads, min(len(w["cz"]), int(seconds * rows_per_s)))
             stride = max(1, len(w["cz"]) // rows)
         sub = w["cz"][::stride]
+        if stride == 1:
+            return dict(w, cz=sub), f"the whole grid ({len(sub)} x {len(w['en'])} bins), nu+nubar"
         return dict(w, cz=sub), f"every {stride}th cosine row ({len(sub)} x {len(w['en'])} bins), nu+nubar"
     n = len(w["en"])
     if orc is not None:
         probe = dict(w, en=w["en"][:20000])
+        cpu_run(probe, orc, nthreads)  # warm-up
         t0 = time.perf_counter()
         cpu_run(probe, orc, nthreads)
         n = max(20000, min(n, int(seconds / max((time.perf_counter() - t0) / 20000, 1e-12))))

@@ -416,9 +416,12 @@ __device__ __forceinline__ df2 df2_mulf(const df2& x, float2 y) {
     const float2 e = __ffma2_rn(x.hi, y, neg2(p));
     return df2_fast2sum(p, __ffma2_rn(x.lo, y, e));
 }
-// df_recip lane for lane (the two float reciprocals stay scalar)
+// df_recip lane for lane (the two float reciprocals stay scalar).  The starting reciprocal
+// is the fast one (2 ulp, relative error d < 2^-22): the double-float Newton step leaves d^2
+// < 2^-44, which is all its one caller (the projector normalisation of the eigenvector
+// tables, rounded to FP32 afterwards) can use.
 __device__ __forceinline__ df2 df2_recip(const df2& x) {
-    const float2 r = make_float2(1.0f / x.hi.x, 1.0f / x.hi.y);
+    const float2 r = make_float2(__fdividef(1.0f, x.hi.x), __fdividef(1.0f, x.hi.y));
     const df2 one_minus = df2_sub(df2{bc2(1.0f), bc2(0.0f)}, df2_mulf(x, r));
     return df2_add(df2{r, bc2(0.0f)}, df2_mulf(one_minus, r));
 }
@@ -541,9 +544,12 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
     // t = 2 sqrt(m) cos(a) solves t^3 + P t + Q = 0 when cos(3a) = -Q / (2 m^{3/2})
     const float carg = fminf(1.0f, fmaxf(-1.0f, (-0.5f * qq) / (mp3 * rt)));
     const float th = acosf(carg) * (1.0f / 3.0f);
-    // cos(th - 2 pi/3) = -cos(th)/2 + (sqrt(3)/2) sin(th): one sincos for both roots
+    // cos(th - 2 pi/3) = -cos(th)/2 + (sqrt(3)/2) sin(th): one sincos for both roots.  The
+    // hardware approximation (absolute error ~4e-7 on [0, pi/3]) puts the starting roots
+    // ~3e-7 of the spread off, no further than acos's own conditioning already does wherever
+    // the gap is below ~0.2 of the spread; the Newton steps below remove either.
     float sn, cn;
-    sincosf(th, &sn, &cn);
+    __sincosf(th, &sn, &cn);
     float l0 = fmaf(2.0f * rt, cn, s);
     float l1 = fmaf(2.0f * rt, fmaf(0.8660254f, sn, -0.5f * cn), s);
     // Newton steps on both roots side by side: the residual in double-float, the derivative
@@ -551,7 +557,8 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
     // convergence by that factor).
     //   The FP32 trigonometric roots are off by ~eps * spread^2 / gap (acos near +-1), so one
     // step leaves a relative error of ~eps^2 (spread / gap)^4 in the gap: below 1e-10 while
-    // gap > 0.05 spread.  The eigenvector tables of the deep atmospheric chains always take a
+    // gap > 0.05 spread.  The correction f / d itself needs only ~1e-6 relative accuracy
+    // (it scales the remaining error, not the root), so it takes the fast divide.  The eigenvector tables of the deep atmospheric chains always take a
     // second step; the beam's projectors take it only below that gap (near the solar
     // resonance, a few per cent of a beam grid's energies).
     df2 x{make_float2(l0, l1), bc2(0.0f)};
@@ -561,7 +568,7 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
             const df2 f = df2_sub(df2_mul(df2_add(df2_mul(df2_sub(x, C2), x), C1), x), C0);
             const float2 d = __ffma2_rn(__ffma2_rn(bc2(3.0f), x.hi, bc2(-2.0f * c2.hi)), x.hi,
                                         bc2(c1.hi));
-            x = df2_sub(x, df2{make_float2(f.hi.x / d.x, f.hi.y / d.y), bc2(0.0f)});
+            x = df2_sub(x, df2{make_float2(__fdividef(f.hi.x, d.x), __fdividef(f.hi.y, d.y)), bc2(0.0f)});
         };
         newton();
         bool again = kVectors;
@@ -589,7 +596,7 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
         h[q] = df{p->h0f[q][0], p->h0f[q][1]};
         H2[q] = df{p->h2f[q][0], p->h2f[q][1]};
     }
-    H2[0] = df_add(H2[0], df_mul(V, df_add(df_add(h[0], h[0]), V)));
+    H2[0] = df_add(H2[0], df_mul(V, df_add(df{2.0f * h[0].hi, 2.0f * h[0].lo}, V)));  // 2 h0 exact
     H2[1] = df_add(H2[1], df_mul(V, h[1]));
     H2[2] = df_add(H2[2], df_mul(V, h[2]));
     h[0] = df_add(h[0], V);
@@ -611,8 +618,10 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
         // not 48.  Compensated FP32: the large terms meet in one FMA (a TwoSum first on the
         // diagonal, where H^2 and m_a m_b are both large), rounded once after the
         // cancellation; the low words add in FP32.  ~2 ulp of P.
+        // (the fast reciprocal adds up to 2 ulp: P stays within a few ulp, far inside what a
+        // layer needs)
         const float2 den = __fmul2_rn(__fadd2_rn(dka.hi, dka.lo), __fadd2_rn(dkb.hi, dkb.lo));
-        const float2 inv = make_float2(1.0f / den.x, 1.0f / den.y);
+        const float2 inv = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
 #pragma unroll
         for (int q = 0; q < 6; q++) {
             const bool diag = q == 0 || q == 3 || q == 5;

@@ -211,14 +211,15 @@ int cp3_set_profiling(cp3_propagator* h, int enable);
  * per-bin kernel, milliseconds.  eigen_ms is 0 where no table kernel runs (beam). */
 int cp3_kernel_times(cp3_propagator* h, double* eigen_ms, double* bins_ms);
 
-/* ---- batches: many problems, one persistent launch --------------------------------------- */
+/* ---- batches: many problems, one run of a persistent kernel ------------------------------ */
 
 /* No reference counterpart (the reference propagates one grid per call; a fit evaluates many
- * parameter sets with uneven grids, here in one launch).  A batch holds atmospheric
+ * parameter sets with uneven grids, here in one run).  A batch holds atmospheric
  * problems (one Earth model and production height per batch, own cosine/energy grid each)
  * and beam problems (own energies, density and baselines), each with its own oscillation
  * parameters and neutrino type, computed in MIXED precision by one persistent kernel
- * replayed from a CUDA graph.  Results stay on the device:
+ * replayed from a CUDA graph (one launch, or a table launch and a bin launch: see
+ * cp3_batch_set_split_tables).  Results stay on the device:
  *   atmospheric problem  [9][n_cosines][n_energies] floats
  *   beam problem         [n_baselines][9][n_energies] floats */
 typedef struct cp3_batch cp3_batch;
@@ -285,7 +286,8 @@ int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins,
  * + a neutrino type; submit returns at once.  A scheduler thread admits queued requests in
  * arrival order as device memory (a pool of pool_bytes for their tables and results) and one
  * of two launch slots free up, packs up to max_batch requests / max_bins_per_launch bins
- * into one persistent launch, and overlaps consecutive launches on two streams.  Grids stay
+ * into one run of the persistent kernel (a table launch and a bin launch where there are
+ * atmospheric requests), and overlaps consecutive runs on two streams.  Grids stay
  * resident; a request's result stays on the device until cp3_server_release. */
 typedef struct cp3_server cp3_server;
 

@@ -207,7 +207,7 @@ public:
 
 // ---- additions with no reference counterpart: batches and the serving loop --------------
 
-// Many problems (own grids, own parameters) in one persistent launch (cp3_batch_*).
+// Many problems (own grids, own parameters) in one run of a persistent kernel (cp3_batch_*).
 class PropagatorBatch {
 public:
     explicit PropagatorBatch(int device = 0) { check(cp3_batch_create(device, &b_)); }

@@ -358,15 +358,6 @@ CP3_HD df df_recip(df x) {
     const df one_minus = df_sub(df{1.0f, 0.0f}, df_mulf(x, r));  // 1 - x r, small
     return df_add(df{r, 0.0f}, df_mulf(one_minus, r));
 }
-// sqrt(x) to df64 accuracy for x > 0: float square root r, then one Newton correction
-// (x - r^2) / (2 r) with r^2 exact through TwoProduct (Dekker/Karp-Markstein form).
-CP3_HD df df_sqrt(df x) {
-    const float r = sqrtf(x.hi);
-    const float p = CP3_FMUL(r, r);
-    const float pe = fmaf(r, r, -p);
-    const float d = CP3_FADD(CP3_FADD(CP3_FADD(x.hi, -p), -pe), x.lo);  // x.hi - p is exact
-    return df_fast2sum(r, d * (0.5f / r));
-}
 
 #ifdef __CUDACC__
 // ---------------------------------------------------------------------------------------
@@ -410,20 +401,6 @@ __device__ __forceinline__ df2 df2_mul(const df2& x, const df2& y) {
     float2 e = __ffma2_rn(x.hi, y.hi, neg2(p));
     e = __ffma2_rn(x.hi, y.lo, __ffma2_rn(x.lo, y.hi, e));
     return df2_fast2sum(p, e);
-}
-__device__ __forceinline__ df2 df2_mulf(const df2& x, float2 y) {
-    const float2 p = __fmul2_rn(x.hi, y);
-    const float2 e = __ffma2_rn(x.hi, y, neg2(p));
-    return df2_fast2sum(p, __ffma2_rn(x.lo, y, e));
-}
-// df_recip lane for lane (the two float reciprocals stay scalar).  The starting reciprocal
-// is the fast one (2 ulp, relative error d < 2^-22): the double-float Newton step leaves d^2
-// < 2^-44, which is all its one caller (the projector normalisation of the eigenvector
-// tables, rounded to FP32 afterwards) can use.
-__device__ __forceinline__ df2 df2_recip(const df2& x) {
-    const float2 r = make_float2(__fdividef(1.0f, x.hi.x), __fdividef(1.0f, x.hi.y));
-    const df2 one_minus = df2_sub(df2{bc2(1.0f), bc2(0.0f)}, df2_mulf(x, r));
-    return df2_add(df2{r, bc2(0.0f)}, df2_mulf(one_minus, r));
 }
 #endif
 
@@ -475,57 +452,68 @@ CP3_HD void rotated_layer_f64(const OscParams* __restrict__ p, double E, double 
 // The FP64 branch of the mixed eigen-solver (the reference cubic), kept out of line: inlined,
 // the compiler may hoist part of it (the double conversions of E and rho) above the branch,
 // and on GB300's narrow FP64 pipe even one such instruction per call costs more than the
-// whole double-float path.  vectors: P[k][0..2] = u_k (orthonormalised), else projectors.
+// whole double-float path.  vectors: P[k][0..2] = u_k, else the projectors u_k u_k^T; both
+// from eigenvectors orthonormalised in FP64.
+//   The fallback runs where two levels nearly meet.  There the Lagrange projectors have
+// entries ~spread / gap that cancel in S = 1 + z1 P1 + z2 P2 (z1 ~ z2), and rounded to FP32
+// separately they no longer do: the beam returned probabilities of 0.4-50 at the exact level
+// crossing of a state without electron component (theta12 = 0 or pi/2, E ~ 0.39 GeV at
+// 2.6 g/cm^3).  Orthonormal vectors give projectors of entries <= 1, exact to FP32
+// rounding, and leave only a rotation inside the near-degenerate plane, which S weighs by
+// the small z1 - z2.
 __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams* __restrict__ p,
                                                                 df Ed, df rhod, bool vectors,
                                                                 float P[2][6], float om[2][2]) {
-    double Pd[2][6], omd[2];
+    double Pd[2][6], omd[2], u[2][3];
     rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
     for (int k = 0; k < 2; k++) {
-        if (vectors) {
-            double u[3];
-            projector_vector(Pd[k], u);
-            for (int i = 0; i < 3; i++) Pd[k][i] = u[i];  // u_k in place (P is no longer needed)
-        } else {
-            for (int q = 0; q < 6; q++) P[k][q] = (float)Pd[k][q];
-        }
+        projector_vector(Pd[k], u[k]);
         const double t = omd[k] * 0.15915494309189535;  // turns per km: omega / (2 pi)
         om[k][0] = (float)t;
         om[k][1] = (float)(t - (double)om[k][0]);
     }
-    if (vectors) {
-        orthonormalize_pair(Pd[0], Pd[1]);
-        for (int k = 0; k < 2; k++)
-            for (int i = 0; i < 3; i++) P[k][i] = (float)Pd[k][i];
+    orthonormalize_pair(u[0], u[1]);
+    for (int k = 0; k < 2; k++) {
+        if (vectors) {
+            for (int i = 0; i < 3; i++) P[k][i] = (float)u[k][i];
+        } else {
+            const double* v = u[k];
+            const double q[6] = {v[0] * v[0], v[0] * v[1], v[0] * v[2], v[1] * v[1], v[1] * v[2], v[2] * v[2]};
+            for (int i = 0; i < 6; i++) P[k][i] = (float)q[i];
+        }
     }
 }
 
 // The mixed kernels' eigen-decomposition without FP64 on the common path:
 //   1. V = -fac (matter potential in 2E.H units, eV^2) and the cubic's coefficients in df64;
 //   2. the three roots from the trigonometric solution in FP32;
-//   3. two Newton steps per root on the df64 polynomial (the third root from the trace);
-//   4. P1, P2 = (H - m_a)(H - m_b)/((m_k - m_a)(m_k - m_b)) in df64, rounded to float, with
-//      the numerator as H^2 - (m_a + m_b) H + m_a m_b from H0^2 split on the host;
-//      the phase rates in turns per km, omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E),
-//      in df64 (hi, lo).
-// Where two refined roots lie closer than 5e-3 of the spread the FP64 reference cubic takes
-// over.  Below that the double-float Newton steps are not reliably in their quadratic regime
-// (FP32 starting roots near a double root are off by ~sqrt(eps) of the spread, and Newton
-// then converges only linearly), so neither the roots nor the gap test itself can be
-// trusted there.  Physical parameters stay well above it: a scan of 2.4e6 (E, rho)
+//   3. one or two Newton steps per root on the df64 polynomial (the third root from the
+//      trace);
+//   4. the phase rates in turns per km, omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E),
+//      in df64 (hi, lo);
+//   5. the eigenvectors of m_1, m_2 in FP32 from the vacuum eigen-system (the rank-one
+//      update below), and from them P1, P2.
+// Where two roots lie closer than 5e-3 of the spread -- tested on the FP32 starting roots
+// and again on the refined ones -- the FP64 reference cubic takes over.  Below that the
+// double-float Newton steps are not reliably in their quadratic regime (FP32 starting roots
+// near a double root are off by ~sqrt(eps) of the spread, and Newton then converges only
+// linearly, or diverges where the start sits between the pair), so neither the roots nor a
+// gap test on them can be trusted there.  Physical parameters stay well above it: a scan of 2.4e6 (E, rho)
 // points, 0.1-100 GeV, 0-6.6 g/cm^3 electron density, Gaussian parameter sets in both
 // orderings, nu and nubar, has min gap/spread = 0.022 (100 GeV through the core); exactly
-// degenerate vacuum masses (the reference's 5e-9 eV^2 degeneracy break) are the cases it
-// catches.
+// degenerate vacuum masses (the reference's 5e-9 eV^2 degeneracy break) and the exact level
+// crossings of a state without electron component (theta12 or theta13 at 0 or pi/2) are
+// the cases it catches.
 // E and rho arrive as float pairs (split once on the host), so the common path runs no FP64
 // instruction at all -- conversions included, which issue on the narrow FP64 pipe.
 //
 // kVectors: instead of the projectors, out[k][0..2] = u_k, the unit eigenvector with
-// P_k = u_k u_k^T (sign arbitrary), taken from the column j of P_k with the largest diagonal:
-// u_k = P_k e_j / sqrt(P_k[j][j]), in double-float before the final rounding.
+// P_k = u_k u_k^T (sign arbitrary).
+// The common path; false where the FP64 fallback has to take over (one call site for it,
+// below, so that no live range of the common path has to survive a call).
 template <bool kVectors>
-__device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed,
-                                                      df rhod, float P[2][6], float om[2][2]) {
+__device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restrict__ p, df Ed,
+                                                        df rhod, float P[2][6], float om[2][2]) {
     // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos
     const df tw = df{1.52588e-4f, -7.040322e-12f};  // kTwoRtTwoGf = hi + lo
     df V = df_mul(df_mul(tw, Ed), rhod);
@@ -552,6 +540,18 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
     __sincosf(th, &sn, &cn);
     float l0 = fmaf(2.0f * rt, cn, s);
     float l1 = fmaf(2.0f * rt, fmaf(0.8660254f, sn, -0.5f * cn), s);
+    // The fallback test, on the starting roots.  Near a double root the FP32 start is good
+    // only to ~sqrt(eps) of the spread and can sit where f' vanishes between the pair; the
+    // FP32 derivative is then rounding noise, the first Newton step throws the roots off by
+    // a quarter of the spread, and the test on the refined roots below passes on garbage
+    // (an exact level crossing of a state without electron component, theta12 = 0 or pi/2,
+    // put the beam 0.6 off).  With th in [0, pi/3] the starting roots are ordered l0 >= l1 >=
+    // l2, l0 - l1 = 2 sqrt3 rt sin(pi/3 - th), l1 - l2 = 2 sqrt3 rt sin(th) and the spread
+    // 2 sqrt3 rt sin(th + pi/3) >= 3 rt: gap < 5e-3 spread is th (or pi/3 - th) below
+    // 5e-3 sin(pi/3) = 4.33e-3.
+    if (!(th > 4.33e-3f && th < 1.0471976f - 4.33e-3f)) {
+        return false;
+    }
     // Newton steps on both roots side by side: the residual in double-float, the derivative
     // in FP32 (its relative error, ~eps * spread / gap < 2e-5, only slows the quadratic
     // convergence by that factor).
@@ -585,94 +585,108 @@ __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restric
     const float spread = fmaxf(fabsf(r[0].hi - r[1].hi), fmaxf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     const float gap = fminf(fabsf(r[0].hi - r[1].hi), fminf(fabsf(r[0].hi - r[2].hi), fabsf(r[1].hi - r[2].hi)));
     if (!(gap > 5e-3f * spread)) {
-        eigen_fallback_f64(p, Ed, rhod, kVectors, P, om);
-        return;
+        return false;
     }
-    // H = H0 + V e0 e0^T and H^2 = H0^2 + V (e0 a^T + a e0^T) + V^2 e0 e0^T (a = H0 e0): only
-    // the first row and column of H0^2 (from the host) change.
-    df h[6], H2[6];
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-        h[q] = df{p->h0f[q][0], p->h0f[q][1]};
-        H2[q] = df{p->h2f[q][0], p->h2f[q][1]};
-    }
-    H2[0] = df_add(H2[0], df_mul(V, df_add(df{2.0f * h[0].hi, 2.0f * h[0].lo}, V)));  // 2 h0 exact
-    H2[1] = df_add(H2[1], df_mul(V, h[1]));
-    H2[2] = df_add(H2[2], df_mul(V, h[2]));
-    h[0] = df_add(h[0], V);
     // kLoEFac / (2 pi E): phase rates in turns per km (kLoEFac / (2 pi) = hi + lo)
     const df loe = df_mul(df{4.032986164e-01f, 9.385560773e-09f}, df_recip(Ed));
-    // the two projectors side by side: lane x is k = 1 (a = 0, b = 2), lane y is k = 2
-    // (a = 0, b = 1); (H - m_a)(H - m_b) = H^2 - (m_a + m_b) H + m_a m_b
-    const df2 Rk = df2_of(r[1], r[2]), Ra = df2_bc(r[0]), Rb = df2_of(r[2], r[1]);
-    const df2 sab = df2_add(Ra, Rb), pab = df2_mul(Ra, Rb);
-    const df2 dka = df2_sub(Rk, Ra), dkb = df2_sub(Rk, Rb);
-    const df2 w = df2_mul(dka, df2_bc(loe));  // omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E)
+    // lane x is k = 1, lane y is k = 2; omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E)
+    const df2 lam = df2_of(r[1], r[2]);
+    const df2 w = df2_mul(df2_sub(lam, df2_bc(r[0])), df2_bc(loe));
     om[0][0] = w.hi.x;
     om[0][1] = w.lo.x;
     om[1][0] = w.hi.y;
     om[1][1] = w.lo.y;
-    if (!kVectors) {
-        // Projectors (the beam): FP32 accuracy of P is what a single layer needs, and the
-        // numerator's cancellation (terms ~spread^2, result ~gap x spread) needs ~30 bits,
-        // not 48.  Compensated FP32: the large terms meet in one FMA (a TwoSum first on the
-        // diagonal, where H^2 and m_a m_b are both large), rounded once after the
-        // cancellation; the low words add in FP32.  ~2 ulp of P.
-        // (the fast reciprocal adds up to 2 ulp: P stays within a few ulp, far inside what a
-        // layer needs)
-        const float2 den = __fmul2_rn(__fadd2_rn(dka.hi, dka.lo), __fadd2_rn(dkb.hi, dkb.lo));
-        const float2 inv = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+    // Eigenvectors by the rank-one update of the vacuum system (Golub 1973; Bunch, Nielsen
+    // and Sorensen 1978).  H0 = O diag(mu) O^T, so (H0 - l) u = -V (e0 . u) e0 gives
+    // u = O d with d_j = a_j / (mu_j - l), a = O^T e0 (the first row of O).  Multiplied
+    // through by prod_i (mu_i - l), d_j = a_j prod_{i != j} (mu_i - l): no division, and
+    // finite where l meets a vacuum mass (vacuum, or a state that decouples at low density).
+    // Each difference mu_i - l is formed from the double-float root before rounding to FP32
+    // (hi - hi is exact or correctly rounded, the low words add ~ulp), so d is good to a few
+    // ulp whatever the cancellation, and |u| = |d| (O orthogonal).
+    if constexpr (kVectors) {
+        // The eigenvector tables feed every layer of the deep atmospheric chains, where
+        // vector errors add up over the layers: on the 59-shell grid the FP32 form below
+        // gave 7.5e-6 max error, double-float without the final scaling 4.5e-6, and this
+        // form, rounded once after normalisation, 2.2e-6 (the same as the earlier projector
+        // columns).  So the tables run the formula in double-float.
+        df2 dd[3], e[3], uu[3];
 #pragma unroll
-        for (int q = 0; q < 6; q++) {
-            const bool diag = q == 0 || q == 3 || q == 5;
-            const float2 H2h = bc2(H2[q].hi);
-            float2 sum = H2h, err = bc2(0.0f);
-            if (diag) {  // TwoSum (Knuth): sum + err = H2.hi + pab.hi exactly
-                sum = __fadd2_rn(H2h, pab.hi);
-                const float2 bb = __fadd2_rn(sum, neg2(H2h));
-                err = __fadd2_rn(__fadd2_rn(H2h, neg2(__fadd2_rn(sum, neg2(bb)))),
-                                 __fadd2_rn(pab.hi, neg2(bb)));
-            }
-            const float2 lead = __ffma2_rn(neg2(sab.hi), bc2(h[q].hi), sum);
-            float2 low = __fadd2_rn(err, bc2(H2[q].lo));
-            if (diag) low = __fadd2_rn(low, pab.lo);
-            low = __ffma2_rn(neg2(sab.lo), bc2(h[q].hi), __ffma2_rn(neg2(sab.hi), bc2(h[q].lo), low));
-            const float2 v = __fmul2_rn(__fadd2_rn(lead, low), inv);
-            P[0][q] = v.x;
-            P[1][q] = v.y;
+        for (int i = 0; i < 3; i++) dd[i] = df2_sub(df2_bc(df{p->muf[i][0], p->muf[i][1]}), lam);
+        auto o = [&](int i, int j) { return df2_bc(df{p->of[i][j], p->oflo[i][j]}); };
+        e[0] = df2_mul(o(0, 0), df2_mul(dd[1], dd[2]));
+        e[1] = df2_mul(o(0, 1), df2_mul(dd[0], dd[2]));
+        e[2] = df2_mul(o(0, 2), df2_mul(dd[0], dd[1]));
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            uu[i] = df2_add(df2_add(df2_mul(o(i, 0), e[0]), df2_mul(o(i, 1), e[1])), df2_mul(o(i, 2), e[2]));
+        const df2 nn = df2_add(df2_add(df2_mul(e[0], e[0]), df2_mul(e[1], e[1])), df2_mul(e[2], e[2]));
+        const float s2 = spread * spread;
+        if (!(fminf(nn.hi.x, nn.hi.y) > 1e-16f * (s2 * s2))) {  // see the FP32 branch below
+            return false;
         }
-        return;
-    }
-    const df2 inv = df2_recip(df2_mul(dka, dkb));
-    df2 Pk[6];
+        // 1 / sqrt(n) in double-float: the float estimate r, then one Newton step on the
+        // exact residual 1 - n r^2 (r^2 and n.hi r^2 through TwoProduct); the vector is
+        // scaled in double-float and rounded once (1/2 ulp, as the tables were before)
+        const float2 r = make_float2(rsqrtf(nn.hi.x), rsqrtf(nn.hi.y));
+        const float2 r2 = __fmul2_rn(r, r), r2e = __ffma2_rn(r, r, neg2(r2));
+        const float2 q = __fmul2_rn(nn.hi, r2), qe = __ffma2_rn(nn.hi, r2, neg2(q));
+        float2 res = __fadd2_rn(bc2(1.0f), neg2(q));  // exact: q is within an ulp or two of 1
+        res = __fadd2_rn(res, neg2(__ffma2_rn(nn.lo, r2, __ffma2_rn(nn.hi, r2e, qe))));
+        const df2 rn = df2_fast2sum(r, __fmul2_rn(__fmul2_rn(r, bc2(0.5f)), res));
 #pragma unroll
-    for (int q = 0; q < 6; q++) {
-        df2 n = df2_sub(df2_bc(H2[q]), df2_mul(sab, df2_bc(h[q])));
-        if (q == 0 || q == 3 || q == 5) n = df2_add(n, pab);
-        Pk[q] = df2_mul(n, inv);
-    }
+        for (int i = 0; i < 3; i++) {
+            const df2 v = df2_mul(uu[i], rn);
+            const float2 f = __fadd2_rn(v.hi, v.lo);
+            P[0][i] = f.x;
+            P[1][i] = f.y;
+        }
+        return true;
+    } else {
+        float2 dl[3];
 #pragma unroll
-    for (int kk = 0; kk < 2; kk++) {
-        // column j with the largest diagonal (>= 1/3), selected without indexing
-        df c[6];
+        for (int i = 0; i < 3; i++)
+            dl[i] = __fadd2_rn(__fadd2_rn(bc2(p->muf[i][0]), neg2(lam.hi)),
+                               __fadd2_rn(bc2(p->muf[i][1]), neg2(lam.lo)));
+        float2 d[3];
+        d[0] = __fmul2_rn(bc2(p->of[0][0]), __fmul2_rn(dl[1], dl[2]));
+        d[1] = __fmul2_rn(bc2(p->of[0][1]), __fmul2_rn(dl[0], dl[2]));
+        d[2] = __fmul2_rn(bc2(p->of[0][2]), __fmul2_rn(dl[0], dl[1]));
+        float2 u[3];
 #pragma unroll
-        for (int q = 0; q < 6; q++) c[q] = kk == 0 ? df2_x(Pk[q]) : df2_y(Pk[q]);
-        const float d0 = c[0].hi, d1 = c[3].hi, d2 = c[5].hi;
-        const int j = (d0 >= d1 && d0 >= d2) ? 0 : (d1 >= d2 ? 1 : 2);
-        const df c0 = j == 0 ? c[0] : (j == 1 ? c[1] : c[2]);
-        const df c1 = j == 0 ? c[1] : (j == 1 ? c[3] : c[4]);
-        const df c2 = j == 0 ? c[2] : (j == 1 ? c[4] : c[5]);
-        const df t = df_sqrt(j == 0 ? c0 : (j == 1 ? c1 : c2));  // sqrt(P_jj)
-        const df it = df_recip(t);
-        const df u0 = j == 0 ? t : df_mul(c0, it);
-        const df u1 = j == 1 ? t : df_mul(c1, it);
-        const df u2 = j == 2 ? t : df_mul(c2, it);
-        P[kk][0] = u0.hi + u0.lo;
-        P[kk][1] = u1.hi + u1.lo;
-        P[kk][2] = u2.hi + u2.lo;
+        for (int i = 0; i < 3; i++)
+            u[i] = __ffma2_rn(bc2(p->of[i][2]), d[2],
+                              __ffma2_rn(bc2(p->of[i][1]), d[1], __fmul2_rn(bc2(p->of[i][0]), d[0])));
+        const float2 n = __ffma2_rn(d[2], d[2], __ffma2_rn(d[1], d[1], __fmul2_rn(d[0], d[0])));
+        // |d|^2 ~ spread^4 except where the formula has no content: a vacuum mass shared by two
+        // states (a degenerate splitting) or a state with no electron component (a_j = 0, e.g.
+        // theta13 = 0), where d vanishes with l - mu_j.  Those parameter sets take the FP64
+        // reference path; physical ones stay above 1e-12 spread^4.
+        const float s2 = spread * spread;
+        if (!(fminf(n.x, n.y) > 1e-16f * (s2 * s2))) {
+            return false;
+        }
+        // projectors P_k = u u^T / |d|^2 (00,01,02,11,12,22), good to a few ulp: the beam's one
+        // layer per baseline needs no more (C3 max error 1.9e-6, against 1.1e-6 with the
+        // double-float Lagrange projectors, for 15 % less time)
+        const float2 inv = make_float2(__fdividef(1.0f, n.x), __fdividef(1.0f, n.y));
+        const float2 v0 = __fmul2_rn(u[0], inv), v1 = __fmul2_rn(u[1], inv), v2 = __fmul2_rn(u[2], inv);
+        const float2 q[6] = {__fmul2_rn(v0, u[0]), __fmul2_rn(v0, u[1]), __fmul2_rn(v0, u[2]),
+                             __fmul2_rn(v1, u[1]), __fmul2_rn(v1, u[2]), __fmul2_rn(v2, u[2])};
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            P[0][k] = q[k].x;
+            P[1][k] = q[k].y;
+        }
+        return true;
     }
-    // (No orthonormalisation here: with converged roots the double-float vectors are
-    // orthogonal to rounding, and an FP32 correction step would only add a rounding.)
+}
+
+template <bool kVectors>
+__device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed,
+                                                      df rhod, float P[2][6], float om[2][2]) {
+    if (!rotated_eigen_mixed_try<kVectors>(p, Ed, rhod, P, om))
+        eigen_fallback_f64(p, Ed, rhod, kVectors, P, om);
 }
 
 // Projectors P1, P2 (00,01,02,11,12,22) and phase rates.

@@ -115,19 +115,15 @@ void build_osc_params(const MixingInput& m, int antineutrino, OscParams* o) {
         out[0] = (float)x;
         out[1] = (float)(x - (double)out[0]);
     };
-    for (int q = 0; q < 6; q++) split(o->h0[q], o->h0f[q]);
-    {
-        // H0^2 (symmetric), for the mixed eigen-solver's projector numerators
-        const int ix[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-        int q = 0;
-        for (int i = 0; i < 3; i++)
-            for (int j = i; j < 3; j++, q++) {
-                double acc = 0.0;
-                for (int m = 0; m < 3; m++) acc += o->h0[ix[i][m]] * o->h0[ix[m][j]];
-                split(acc, o->h2f[q]);
-            }
-    }
     for (int q = 0; q < 5; q++) split(o->cpoly[q], o->cpolyf[q]);
+    for (int k = 0; k < 3; k++) split(dk[k], o->muf[k]);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            float hl[2];
+            split(O[i][j], hl);
+            o->of[i][j] = hl[0];
+            o->oflo[i][j] = hl[1];
+        }
     o->w[0] = c23;
     o->w[1] = s23;
     o->w[2] = cd;

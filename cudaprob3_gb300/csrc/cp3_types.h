@@ -31,11 +31,12 @@ struct alignas(16) OscParams {
     // cpoly = {t = tr H0, c = sum of principal 2x2 minors, D = det H0,
     //          m = h11 + h22, n = h11 h22 - h12^2}
     double cpoly[5];
-    // The same numbers as float pairs (hi, lo), split on the host for the double-float
-    // eigen-solver of the mixed kernels.
-    float h0f[6][2];
+    // For the mixed kernels' eigen-solver: cpoly as float pairs (hi, lo), and the vacuum
+    // eigen-system H0 = O diag(mu) O^T, mu_k = DM(k,0) as float pairs, O in FP32.
     float cpolyf[5][2];
-    float h2f[6][2];     // H0^2 (00,01,02,11,12,22) as float pairs
+    float muf[3][2];
+    float of[3][3];      // O[i][j]; column j is the vacuum eigenvector of mu_j
+    float oflo[3][3];    // O - of, the low words (double-float O for the eigenvector tables)
     int order[3];        // root order from the vacuum cubic (prepare_getMfast)
     int anti;            // 1: antineutrino sign of the matter potential
     float wf[4];         // w rounded to float (the mixed kernels' W)

@@ -76,3 +76,35 @@ def test_atmospheric_mixed_within_1e5_over_models_heights_and_low_energies():
                         g = run_atmos("mixed", mix6, knu, anti, *args)
                         worst[mi] = max(worst.get(mi, 0.0), float(np.abs(f - g).max()))
     assert max(worst.values()) <= 1e-5, worst
+
+
+def test_mixed_on_degenerate_mixing_parameters():
+    """Parameter sets where a state has no electron component (theta13 = 0, theta12 = 0,
+    theta12 = pi/2) or a splitting nearly vanishes: the mixed eigen-solver's rank-one
+    eigenvector formula has no content for the decoupled state there and must hand it to the
+    FP64 reference path.  Mixed against FP64 (beam and atmospheric) within 1e-5, no NaN."""
+    from tests.gpu_helpers import run_beam
+    m = earth.NOMINAL
+    base = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+    cases = []
+    for name, idx, val in (("theta13=0", 1, 0.0), ("theta12=0", 0, 0.0),
+                           ("theta12=pi/2", 0, np.pi / 2), ("dm21=1e-9", 4, 1e-9)):
+        mix6 = list(base)
+        mix6[idx] = val
+        cases.append((name, mix6))
+    en = np.geomspace(0.1, 100.0, 2000)
+    cz, ena = earth.cosine_grid(100), earth.log_energy_grid(200)
+    worst = {}
+    for name, mix6 in cases:
+        for dm23 in (mix6[5], -abs(mix6[5])):
+            mx = mix6[:5] + [dm23]
+            for anti in (False, True):
+                knu = -1 if anti else 1
+                for L in (1300.0, 12742.0):
+                    f = run_beam("fp64", mx, knu, anti, en, 2.6, L)
+                    g = run_beam("mixed", mx, knu, anti, en, 2.6, L)
+                    worst[name] = max(worst.get(name, 0.0), float(np.abs(f - g).max()))
+                f = run_atmos("fp64", mx, knu, anti, cz, ena, *earth.PREM_4LAYER, 22.0)
+                g = run_atmos("mixed", mx, knu, anti, cz, ena, *earth.PREM_4LAYER, 22.0)
+                worst[name] = max(worst.get(name, 0.0), float(np.abs(f - g).max()))
+    assert all(v <= 1e-5 for v in worst.values()), worst

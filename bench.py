@@ -44,9 +44,9 @@ NCU_TRAFFIC = {
     ("atmos59", "mixed"): (5.914112e6 + 85.716992e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
     # the table launch and the bin launch of one run
-    ("batch_atmos", "mixed"): (0.436224e6 + 0.048640e6 + 85.522176e6 + 903.943680e6, 912.332288e6,
+    ("batch_atmos", "mixed"): (0.435456e6 + 0.033280e6 + 83.864320e6 + 902.968832e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
-    ("batch_beam", "mixed"): (105.446656e6 + 893.710080e6, 921.6e6,
+    ("batch_beam", "mixed"): (107.312384e6 + 912.375040e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
     ("atmos59", "fp64"): (9.935872e6 + 245.010688e6, 288.0e6,
                           "profiles/atmos_f64_kernel_59shells_2000x2000.md"),
@@ -59,8 +59,8 @@ NCU_TRAFFIC = {
 # 1); this is the utilisation of what they do execute.
 NCU_PIPE = {
     ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7233),
-    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6700),  # the bin launch
-    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.7136),
+    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6699),  # the bin launch
+    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6852),
     ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8926),
 }
 

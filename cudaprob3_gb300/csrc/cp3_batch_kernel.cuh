@@ -7,7 +7,7 @@
 //   * table tile:        one density class of one atmospheric problem;
 //   * atmospheric tile:  rows_per_tile cosine rows, walked one after the other;
 //   * beam tile:         beam_chunk consecutive groups of 32 energies, every baseline.
-// Each warp stages the trajectory it is walking (segment lengths and classes) in its own
+// Each warp stages the trajectory it is walking (its segment lengths) in its own
 // slice of shared memory; warps synchronise only with themselves (__syncwarp).
 #pragma once
 

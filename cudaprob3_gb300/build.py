@@ -56,18 +56,41 @@ OUT_CHECKED = os.path.join(OUT, "checked")
 LIB_CHECKED = os.path.join(OUT_CHECKED, "libcp3gb300.so")
 
 
+def _signature(nvcc, common, device_checks) -> str:
+    """Digest of everything besides the sources that decides the library's contents: the
+    compiler, the target, the common flags and every unit's own flags (cp3_tables.cu's
+    -fmad=false is what keeps the FP64 masses on the reference's roundings)."""
+    import hashlib
+    import json
+    text = json.dumps([os.path.realpath(nvcc), ARCH, [c for c in common if c != "-v"], UNITS,
+                       bool(device_checks)])
+    return hashlib.sha256(text.encode()).hexdigest()
+
+
 def build(force: bool = False, verbose: bool = False, device_checks: bool = False) -> str:
     """Compile (if stale) and return the path of the shared library (the debug build with
-    device bounds checks when device_checks is set)."""
+    device bounds checks when device_checks is set).  The library is stale when a source or
+    header is newer than it, or when the compile commands differ from the ones it was built
+    with (recorded beside it in build.sig)."""
     out, lib = (OUT_CHECKED, LIB_CHECKED) if device_checks else (OUT, LIB)
-    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _sources_mtime():
-        return lib
     nvcc = _nvcc()
-    os.makedirs(out, exist_ok=True)
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC,
               "-I", os.path.join(os.path.dirname(HERE), "include")]
     if device_checks:
         common += ["-DCP3_DEVICE_CHECKS"]
+    sig = _signature(nvcc, common, device_checks)
+    sig_path = os.path.join(out, "build.sig")
+    try:
+        with open(sig_path) as f:
+            same_commands = f.read().strip() == sig
+    except OSError:
+        same_commands = False
+    if (not force and same_commands and os.path.exists(lib)
+            and os.path.getmtime(lib) >= _sources_mtime()):
+        return lib
+    os.makedirs(out, exist_ok=True)
+    if os.path.exists(sig_path):
+        os.remove(sig_path)  # a build that fails half-way leaves no signature behind
     if verbose:
         common += ["-Xptxas", "-v"]
 
@@ -92,6 +115,8 @@ def build(force: bool = False, verbose: bool = False, device_checks: bool = Fals
         raise RuntimeError("link failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     os.replace(tmp, lib)
     if device_checks:
+        with open(sig_path, "w") as f:
+            f.write(sig)
         return lib
     # bench support: scalar FMA peaks (separate library, not part of the C ABI)
     cmd = [nvcc] + ARCH + common + ["-shared", os.path.join(SRC, "cp3_peaks.cu"), "-o", PEAKS_LIB]
@@ -100,6 +125,8 @@ def build(force: bool = False, verbose: bool = False, device_checks: bool = Fals
         raise RuntimeError("nvcc failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     with open(os.path.join(OUT, "build.log"), "w") as f:
         f.write("\n".join(logs))
+    with open(sig_path, "w") as f:
+        f.write(sig)
     if verbose:
         sys.stdout.write("\n".join(logs))
     return LIB

@@ -6,7 +6,10 @@ Two libraries can sit behind this module:
   machine by ``make -C oracle``); ``libcp3oracle_fast.so`` is the same source built with the
   compiler's default FMA contraction and is what bench.py times as the CPU baseline.
 * ``oracle/_ref/libcp3ref.so`` -- the reference's own CPU propagators compiled from the
-  reference tree (``make -C oracle ref``); only present where the reference sources are.
+  reference tree (``make -C oracle ref REF=<tree>``); only present where the reference
+  sources are.  ``libcp3ref_fast.so`` is the same with the compiler's default contraction
+  (the timed reference arm), and ``refgpu_bench`` runs the reference's own FP64 CUDA
+  propagators (``make -C oracle refgpu``).  ``reference_dir()`` says where the tree is.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this module.
 """
@@ -86,6 +89,34 @@ def build(quiet: bool = True) -> None:
 
 class OracleError(RuntimeError):
     pass
+
+
+def reference_dir():
+    """The reference source tree, or None: $CP3_REFERENCE_DIR if set, else the untracked copy
+    at <repo>/baseline/_ref (git-ignored; it travels with the working tree to a GPU host)."""
+    for cand in (os.environ.get("CP3_REFERENCE_DIR"),
+                 os.path.join(os.path.dirname(HERE), "baseline", "_ref")):
+        if cand and os.path.isfile(os.path.join(cand, "physics.hpp")):
+            return os.path.abspath(cand)
+    return None
+
+
+def build_reference(gpu: bool = True) -> dict:
+    """Compile the reference's CPU propagators (and, with ``gpu``, its CUDA timing driver)
+    from reference_dir() into oracle/_ref.  Returns {target: ok} ({} without a tree)."""
+    ref = reference_dir()
+    if ref is None:
+        return {}
+    done = {}
+    for target in (["ref", "refgpu"] if gpu else ["ref"]):
+        r = subprocess.run(["make", "-s", "-j3", "-C", HERE, target, f"REF={ref}"],
+                           capture_output=True, text=True)
+        done[target] = r.returncode == 0
+        if r.returncode != 0:
+            with open(os.path.join(REFDIR if os.path.isdir(REFDIR) else HERE,
+                                   f"build_{target}.log"), "w") as f:
+                f.write(r.stdout + r.stderr)
+    return done
 
 
 _ORC_MSG = {1: "bad size", 2: "radii order messed up", 3: "invalid number of maxLayer",
@@ -195,16 +226,19 @@ class Oracle:
 
 
 class Reference:
-    """The reference's own CPU propagators (only where oracle/_ref was built)."""
+    """The reference's own CPU propagators (only where oracle/_ref was built).  ``fast=True``
+    loads the build with the compiler's default contraction, the one the reference arm times."""
 
     PATH = os.path.join(REFDIR, "libcp3ref.so")
+    FAST_PATH = os.path.join(REFDIR, "libcp3ref_fast.so")
+    GPU_BENCH = os.path.join(REFDIR, "refgpu_bench")
 
     @classmethod
-    def available(cls) -> bool:
-        return os.path.exists(cls.PATH)
+    def available(cls, fast: bool = False) -> bool:
+        return os.path.exists(cls.FAST_PATH if fast else cls.PATH)
 
-    def __init__(self):
-        lib = C.CDLL(self.PATH)
+    def __init__(self, fast: bool = False):
+        lib = C.CDLL(self.FAST_PATH if fast else self.PATH)
         lib.ref_atmos.argtypes = ([C.c_double] * 4 + [C.c_int] + [C.c_double] * 2 + [C.c_int]
                                   + [_dp, C.c_int, _dp, C.c_int] + [_dp] * 5
                                   + [C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int,

@@ -55,3 +55,29 @@ def test_null_handle_is_an_error(lib):
     rc = lib.cp3_set_mns(None, 0.1, 0.1, 0.1, 0.0, 1)
     assert rc != 0
     assert b"null" in lib.cp3_last_error(None)
+
+
+def test_build_is_stale_when_unit_flags_change(monkeypatch):
+    """The library is rebuilt when a compile command changes, not only when a source does:
+    cp3_tables.cu's -fmad=false is what the FP64 parity rests on."""
+    from cudaprob3_gb300 import build
+    base = build._signature("nvcc", ["-O3"], False)
+    assert build._signature("nvcc", ["-O3"], False) == base
+    monkeypatch.setattr(build, "UNITS", [(u, [] if u == "cp3_tables.cu" else f)
+                                         for u, f in build.UNITS])
+    assert build._signature("nvcc", ["-O3"], False) != base
+    monkeypatch.undo()
+    monkeypatch.setattr(build, "ARCH", ["-gencode", "arch=compute_100a,code=sm_100a"])
+    assert build._signature("nvcc", ["-O3"], False) != base
+    monkeypatch.undo()
+    assert build._signature("nvcc", ["-O3"], True) != base
+
+
+def test_reference_tree_comes_from_the_environment(monkeypatch, tmp_path):
+    from oracle import oracle
+    (tmp_path / "physics.hpp").write_text("// stand-in\n")
+    monkeypatch.setenv("CP3_REFERENCE_DIR", str(tmp_path))
+    assert oracle.reference_dir() == str(tmp_path)
+    monkeypatch.setenv("CP3_REFERENCE_DIR", str(tmp_path / "absent"))
+    got = oracle.reference_dir()  # falls back to the untracked copy, if there is one
+    assert got is None or os.path.isfile(os.path.join(got, "physics.hpp"))

@@ -41,7 +41,7 @@ BATCH_SETS = 0  # --batch-sets: fewer parameter sets for the batched workloads (
 # summary).  A launch of another size is scaled by its result bytes, since traffic is the
 # output stream plus a small table/descriptor read that grows with it.
 NCU_TRAFFIC = {
-    ("atmos59", "mixed"): (5.914112e6 + 85.716992e6, 144.0e6,
+    ("atmos59", "mixed"): (5.910016e6 + 84.903680e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
     # the table launch and the bin launch of one run
     ("batch_atmos", "mixed"): (0.435456e6 + 0.033280e6 + 83.864320e6 + 902.968832e6, 912.332288e6,
@@ -58,7 +58,7 @@ NCU_TRAFFIC = {
 # counts the reference formulation's flops, more than these kernels execute (it can exceed
 # 1); this is the utilisation of what they do execute.
 NCU_PIPE = {
-    ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7233),
+    ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7099),
     ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6699),  # the bin launch
     ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6852),
     ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8926),
@@ -146,8 +146,9 @@ def workload(name, rank=0):
                          "1e5 E (0.1-10 GeV), rho=2.6, L=295 and 1300 km, nu+nubar "
                          "(8192 problems), one persistent launch")
     if name == "serve":
-        return dict(kind="serve", desc="serving: 64 closed-loop chains, requests of atm 200^2, "
-                                       "500^2, 2000^2 and beam 1e4, 1e5 bins (PREM 4-layer)")
+        return dict(kind="serve", desc="serving: open-loop Poisson arrivals from 64 chains, "
+                                       "requests of atm 200^2, 500^2, 2000^2 and beam 1e4, 1e5 "
+                                       "bins (PREM 4-layer)")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -480,123 +481,218 @@ def set_params(p, m, knu):
     p.setNeutrinoMasses(m.dm12sq, m.dm23sq)
 
 
-def run_serve(args, rank, world):
-    """Serving workload: 64 closed-loop chains (each waits for its result, then thinks for an
-    exponential time and submits again) over request sizes {atm 200^2, 500^2, 2000^2; beam
-    1e4, 1e5}; the think time is swept down to zero (saturation)."""
-    import threading
+SERVE_KINDS = (("atm200x200", "atmos", 200), ("atm500x500", "atmos", 500),
+               ("atm2000x2000", "atmos", 2000), ("beam10000", "beam", 10000),
+               ("beam100000", "beam", 100000))
+
+
+def make_server(dev):
+    """The serving configuration: PREM 4-layer at 22 km, the five request sizes registered,
+    a 16 GB pool, up to 256 requests / 8e6 bins per launch."""
     from cudaprob3_gb300 import earth
     from cudaprob3_gb300.serve import Server
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
     srv = Server(dev, pool_bytes=16 << 30, max_batch=256, max_bins_per_launch=8_000_000)
     srv.set_earth(*earth.PREM_4LAYER, 22.0)
     kinds = []
-    for n in (200, 500, 2000):
-        kinds.append((f"atm{n}x{n}", srv.add_atmos_grid(earth.cosine_grid(n), earth.log_energy_grid(n)), n * n))
-    for n in (10000, 100000):
-        kinds.append((f"beam{n}", srv.add_beam_grid(earth.lin_energy_grid(n), 2.6, [1300.0]), n))
+    for name, kind, n in SERVE_KINDS:
+        if kind == "atmos":
+            g = srv.add_atmos_grid(earth.cosine_grid(n), earth.log_energy_grid(n))
+            kinds.append((name, g, n * n))
+        else:
+            kinds.append((name, srv.add_beam_grid(earth.lin_energy_grid(n), 2.6, [1300.0]), n))
     srv.start()
+    return srv, kinds
+
+
+def serve_level(srv, kinds, sets, rate, seconds, n_chains=64, seed=0):
+    """One offered load, open loop: each of n_chains chains is a Poisson process of
+    rate/n_chains requests/s (together a Poisson process of `rate`).  Arrival times, request
+    sizes, parameter sets and nu/nubar are drawn in advance from `seed`; one host thread
+    submits each request at its arrival time, whatever is still outstanding, and collects
+    completions through the server's completion queue.  A request's latency is its arrival
+    time to the completion of its launch: the server's submit-to-completion time plus any
+    delay of the submit behind its scheduled arrival."""
+    rng = np.random.default_rng(seed)
+    per_chain = rate / n_chains
+    times = []
+    for _ in range(n_chains):
+        n = int(per_chain * seconds * 2) + 16
+        t = np.cumsum(rng.exponential(1.0 / per_chain, size=n))
+        times.append(t[t < seconds])
+    times = np.sort(np.concatenate(times))
+    n_req = len(times)
+    kind = rng.integers(len(kinds), size=n_req)
+    pset = rng.integers(len(sets), size=n_req)
+    anti = rng.integers(2, size=n_req).astype(bool)
+    srv.poll(0)  # start recording completions
+    outstanding = {}
+    lat = np.full(n_req, np.nan)
+    t_done = np.full(n_req, np.inf)
+    lag_max = 0.0
+    i = done = 0
+    st0 = srv.stats()
+    deadline = seconds * 4 + 30.0
+    t0 = time.perf_counter()
+    now = 0.0
+    while done < n_req and now < deadline:
+        now = time.perf_counter() - t0
+        while i < n_req and times[i] <= now:
+            rid = srv.submit(kinds[kind[i]][1], sets[pset[i]], bool(anti[i]))
+            lag = time.perf_counter() - t0 - times[i]
+            lag_max = max(lag_max, lag)
+            outstanding[rid] = (i, lag)
+            i += 1
+        wait = 0.05 if i >= n_req else max(0.0, min(times[i] - (time.perf_counter() - t0), 0.001))
+        for rid in srv.poll(4096, wait):
+            k, lag = outstanding.pop(rid)
+            lat[k] = srv.latency_ms(rid) + lag * 1e3
+            t_done[k] = time.perf_counter() - t0
+            srv.release(rid)
+            done += 1
+    wall = time.perf_counter() - t0
+    st1 = srv.stats()
+    ok = ~np.isnan(lat)
+    probs = 9.0 * sum(kinds[k][2] for k in kind[ok])
+    # achieved: completions inside the arrival window over the window (an overloaded server
+    # falls behind there; the backlog it clears afterwards does not count)
+    lv = {"offered_req_per_s": round(rate, 1), "requests": int(n_req), "completed": int(ok.sum()),
+          "achieved_req_per_s": round(float((t_done <= seconds).sum()) / seconds, 1),
+          "probabilities_per_s": probs / wall, "launches": st1["launches"] - st0["launches"],
+          "p50_ms": round(float(np.percentile(lat[ok], 50)), 3) if ok.any() else None,
+          "p99_ms": round(float(np.percentile(lat[ok], 99)), 3) if ok.any() else None,
+          "max_submit_lag_ms": round(lag_max * 1e3, 3), "seconds": round(wall, 3)}
+    for k, (name, _, _) in enumerate(kinds):
+        sel = lat[(kind == k) & ok]
+        if len(sel):
+            lv[name] = {"n": int(len(sel)), "p50_ms": round(float(np.percentile(sel, 50)), 3),
+                        "p99_ms": round(float(np.percentile(sel, 99)), 3)}
+    return lv
+
+
+def serve_capacity(srv, kinds, sets, n=4000, seed=99):
+    """Requests/s the server completes with a deep queue: n requests of the serving mix
+    submitted at once, timed to the last completion.  It is the scale of the offered loads
+    swept, not the knee: the sweep finds that."""
+    rng = np.random.default_rng(seed)
+    srv.poll(0)
+    t0 = time.perf_counter()
+    ids = [srv.submit(kinds[int(rng.integers(len(kinds)))][1], sets[int(rng.integers(len(sets)))],
+                      bool(rng.integers(2))) for _ in range(n)]
+    left = set(ids)
+    while left and time.perf_counter() - t0 < 60.0:
+        for rid in srv.poll(4096, 0.05):
+            left.discard(rid)
+            srv.release(rid)
+    return n / (time.perf_counter() - t0)
+
+
+def serve_sweep(dev, fractions, seconds, gpu_index):
+    """Latency against offered load: the server's capacity from a deep-queue burst, then one
+    open-loop level per fraction of it, each with its own clock record.  The knee is the
+    highest offered load the server sustains: every request completed, the completions
+    inside the arrival window at least 97 % of the arrivals, and the median latency within
+    twice that of the lightest load (waiting in the queue does not dominate)."""
+    from cudaprob3_gb300 import earth
+    srv, kinds = make_server(dev)
     sets = earth.gaussian_sets(512, seed=31)
-    n_chains = 64
-    # warm-up: every kind once
-    for _, g, _ in kinds:
+    for name, g, _ in kinds:  # warm-up: every size once
         rid = srv.submit(g, sets[0], False)
-        srv.wait(rid)
+        srv.wait(rid, 60.0)
         srv.release(rid)
+    serve_capacity(srv, kinds, sets, n=300)  # warm-up of the burst path
+    cap = serve_capacity(srv, kinds, sets)
     levels = []
-    for think_ms in (args.serve_think or [20.0, 5.0, 1.0, 0.0]):
-        records, lock = [], threading.Lock()
-        t_end = time.perf_counter() + args.serve_seconds
-
-        def chain(cid):
-            rng = np.random.default_rng(1000 * cid + int(think_ms * 10))
-            local = []
-            while time.perf_counter() < t_end:
-                if think_ms > 0:
-                    time.sleep(rng.exponential(think_ms * 1e-3))
-                k = int(rng.integers(len(kinds)))
-                rid = srv.submit(kinds[k][1], sets[int(rng.integers(len(sets)))], bool(rng.integers(2)))
-                srv.wait(rid, 60.0)
-                local.append((k, srv.latency_ms(rid)))
-                srv.release(rid)
-            with lock:
-                records.extend(local)
-
-        st0 = srv.stats()
-        t0 = time.perf_counter()
-        th = [threading.Thread(target=chain, args=(c,)) for c in range(n_chains)]
-        for t in th:
-            t.start()
-        for t in th:
-            t.join()
-        wall = time.perf_counter() - t0
-        st1 = srv.stats()
-        lat = np.array([x[1] for x in records])
-        kk = np.array([x[0] for x in records])
-        probs = 9.0 * sum(kinds[k][2] for k in kk)
-        lv = {"think_ms": think_ms, "requests": len(records),
-              "requests_per_s": round(len(records) / wall, 1),
-              "probabilities_per_s": probs / wall,
-              "launches": st1["launches"] - st0["launches"],
-              "p50_ms": round(float(np.percentile(lat, 50)), 3),
-              "p99_ms": round(float(np.percentile(lat, 99)), 3)}
-        for k, (name, _, _) in enumerate(kinds):
-            sel = lat[kk == k]
-            if len(sel):
-                lv[name] = {"n": int(len(sel)), "p50_ms": round(float(np.percentile(sel, 50)), 3),
-                            "p99_ms": round(float(np.percentile(sel, 99)), 3)}
+    for f in fractions:
+        with Clocks(gpu_index) as clk:
+            lv = serve_level(srv, kinds, sets, f * cap, seconds, seed=int(f * 1000))
+        lv["fraction_of_capacity"] = f
+        lv["clocks"] = clk.summary()
         levels.append(lv)
-    sat = levels[-1]
     srv.close()
+    return cap, levels, serve_knee(levels, seconds), kinds
+
+
+def serve_knee(levels, seconds):
+    """The highest offered load sustained (see serve_sweep), or None."""
+    p50s = [lv["p50_ms"] for lv in levels if lv["p50_ms"] is not None]
+    if not p50s:
+        return None
+    p50_light = min(p50s)
+    sustained = [lv for lv in levels
+                 if lv["completed"] == lv["requests"]
+                 and lv["achieved_req_per_s"] * seconds >= 0.97 * lv["requests"]
+                 and lv["p50_ms"] <= 2.0 * p50_light]
+    return max(sustained, key=lambda lv: lv["offered_req_per_s"]) if sustained else None
+
+
+def serve_summary(cap, knee, kinds, levels=()):
+    """The serving object of a bench line: the knee's offered load and latencies, and the
+    level of the highest throughput (past the knee the queue grows for as long as the
+    arrivals last, so latencies there measure the level's length as much as the server)."""
+    top = max(levels, key=lambda lv: lv["achieved_req_per_s"]) if levels else None
+    sat = None if top is None else {
+        "offered_req_per_s": top["offered_req_per_s"], "achieved_req_per_s": top["achieved_req_per_s"],
+        "probabilities_per_s": top["probabilities_per_s"], "p50_ms": top["p50_ms"],
+        "p99_ms": top["p99_ms"], "atm500x500": top.get("atm500x500")}
+    if knee is None:
+        return {"capacity_req_per_s": round(cap, 1), "sustained": None, "highest_throughput": sat}
+    out = {"capacity_req_per_s": round(cap, 1), "highest_throughput": sat,
+           "offered_req_per_s": knee["offered_req_per_s"],
+           "achieved_req_per_s": knee["achieved_req_per_s"],
+           "probabilities_per_s": knee["probabilities_per_s"],
+           "p50_ms": knee["p50_ms"], "p99_ms": knee["p99_ms"],
+           "atm500x500": knee.get("atm500x500"),
+           "clocks": knee.get("clocks")}
+    return out
+
+
+def run_serve(args, rank, world):
+    """Serving workload: open-loop Poisson arrivals from 64 chains over request sizes {atm
+    200^2, 500^2, 2000^2; beam 1e4, 1e5}, swept over offered loads up to past the server's
+    capacity; p50/p99 latency and probabilities/s per level."""
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    fractions = args.serve_loads or [0.2, 0.4, 0.6, 0.8, 1.0, 1.2, 1.4, 1.6, 1.8, 2.0]
+    cap, levels, knee, kinds = serve_sweep(dev, fractions, args.serve_seconds, dev)
+    top = knee or levels[0]
     line = {
-        "metric": "serving: probabilities/s at saturation (64 closed-loop chains), p50/p99 latency vs load",
-        "value": sat["probabilities_per_s"], "unit": "probabilities/s", "n_gpus": world,
+        "metric": "serving: probabilities/s at the highest sustained offered load (open-loop "
+                  "Poisson, 64 chains), p50/p99 latency vs offered load",
+        "value": world * top["probabilities_per_s"], "unit": "probabilities/s", "n_gpus": world,
         "steps": len(levels), "warmup": 1, "ms_per_step": args.serve_seconds * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic (seeded parameter sets; PREM 4-layer, h=22 km; beam rho=2.6, L=1300 km)",
-        "config": {"workload": "serve", "chains": n_chains,
+        "data": "synthetic (seeded parameter sets and arrivals; PREM 4-layer, h=22 km; beam "
+                "rho=2.6, L=1300 km)",
+        "config": {"workload": "serve", "chains": 64, "arrivals": "open-loop Poisson",
                    "request_sizes": [k[0] for k in kinds], "pool_bytes": 16 << 30,
-                   "max_bins_per_launch": 8_000_000, "scheduling": "smallest-first, 4 ms aging"},
-        "latency_p99_atm500_at_saturation_ms": sat.get("atm500x500", {}).get("p99_ms"),
+                   "max_bins_per_launch": 8_000_000, "scheduling": "smallest-first, 4 ms aging",
+                   "seconds_per_level": args.serve_seconds},
+        "serve": serve_summary(cap, knee, kinds, levels),
+        "latency_p99_atm500_at_knee_ms": (knee or {}).get("atm500x500", {}).get("p99_ms"),
         "levels": levels,
+        "clocks": top["clocks"],
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(workload("serve"), seconds=args.cpu_seconds)
     return line
 
 
-def run_ours(args, rank, world):
-    import torch
-    from cudaprob3_gb300 import earth
-
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    if args.workload == "serve":
-        return run_serve(args, rank, world)
-    w = workload(args.workload, rank)
-    if w["kind"] == "batch":
-        if args.precision == "fp64":
-            return run_batch_fp64(args, w, rank, world)
-        return run_batch(args, w, rank, world)
-    prec = args.precision
-    # weak scaling: each rank propagates its own parameter set over the full grid
-    m = rank_parameter_set(rank, world)
+def make_pair(w, prec, m):
+    """Neutrino and antineutrino handles of one workload and parameter set."""
     props = []
     for knu in (1, -1):
         p = make_propagator(w, prec)
         set_params(p, m, knu)
         props.append(p)
-    # A dedicated stream: kernels, events and the L2 flush are all ordered on it (the legacy
-    # default stream's handle is 0, which the C ABI reads as "the handle's own stream").
-    stream = torch.cuda.Stream()
-    sptr = stream.cuda_stream
-    assert sptr != 0
-    torch.cuda.set_stream(stream)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    return props
 
-    # Neutrino and antineutrino on two streams forked from and joined back into `stream`, as
-    # a caller with two handles would run them: one type's eigen-table kernel overlaps the
-    # other's per-bin kernel.
+
+def time_device_steps(props, stream, flush, steps, warmup, gpu, world):
+    """Device-resident steps: neutrino and antineutrino on two streams forked from and joined
+    back into `stream`, as a caller with two handles would run them (one type's eigen-table
+    kernel overlaps the other's per-bin kernel).  The host queues the steps back to back;
+    each is timed with CUDA events on `stream`, with the L2 flushed (untimed) before it.
+    Returns (per-step ms, clock record)."""
+    import torch
     type_streams = [torch.cuda.Stream() for _ in props]
 
     def step():
@@ -612,12 +708,192 @@ def run_ours(args, rank, world):
         for e in done:
             stream.wait_event(e)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    # numerical check of the timed configuration: nu and nubar against the CPU oracle on a
-    # slice of cosine rows (the full grid would take the oracle minutes)
-    max_err = check_against_oracle(w, props, m) if rank == 0 else None
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(gpu) as clk:
+        for k in range(steps):
+            flush.add_(1.0)
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    return [a.elapsed_time(b) for a, b in ev], clk.summary()
+
+
+def serial_kernel_times(props, sptr, flush, n):
+    """Per-launch kernel durations from the ABI's own CUDA events, the two types one after
+    the other on one stream with the L2 flushed before each: (table ms, per-bin ms) means."""
+    import torch
+    eig, bins = [], []
+    for p in props:
+        p.set_profiling(True)
+    for _ in range(n):
+        for t, p in enumerate(props):
+            flush.add_(1.0)
+            p.calculate_async(t, sptr)
+            a, b = p.kernel_times()
+            eig.append(a)
+            bins.append(b)
+    for p in props:
+        p.set_profiling(False)
+    torch.cuda.synchronize()
+    return float(np.mean(eig)), float(np.mean(bins))
+
+
+def oracle_full(w, m):
+    """The CPU oracle on the whole grid, neutrino and antineutrino (reference CPU layout)."""
+    from oracle.oracle import Mixing as OMix, Oracle
+    orc = Oracle()
+    nt = os.cpu_count() or 1
+    refs = []
+    for anti, knu in ((False, 1), (True, -1)):
+        mix = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
+        if w["kind"] == "atmos":
+            refs.append(orc.atmos(mix, anti, w["cz"], w["en"], *w["model"], w["h"], nthreads=nt))
+        else:
+            refs.append(orc.beam(mix, anti, w["en"], w["rho"], w["L"], nthreads=nt))
+    return refs
+
+
+def channel_errors(props, refs):
+    """Max |GPU - oracle| of each of the nine channels (index a*3+b = P(a->b)), per neutrino
+    type, over every bin of the grid."""
+    out = {}
+    for name, p, ref in zip(("nu", "nubar"), props, refs):
+        res = p.result()  # [9][nc][ne] (atmospheric) or [9][ne] (beam), device precision
+        errs = []
+        for c in range(9):
+            errs.append(float(np.abs(res[c].astype(np.float64) - ref[..., c]).max()))
+        out[name] = errs
+    return out
+
+
+def fp64_arm(w, m, stream, flush, steps, warmup, gpu, world, refs, peaks, flops_launch):
+    """The plain FP64 kernels on the same grid, parameters and step structure as the mixed
+    arm: device probabilities/s, kernel times, FP64 roofline and per-channel errors."""
+    props = make_pair(w, "fp64", m)
+    step_ms, clocks = time_device_steps(props, stream, flush, steps, warmup, gpu, world)
+    t_ms = max_over_ranks(float(np.mean(step_ms)), world, "cuda")
+    nbins = len(w["en"]) * (len(w["cz"]) if w["kind"] == "atmos" else 1)
+    probs_step = 9 * nbins * N_TYPES
+    eig_ms, kern_ms = serial_kernel_times(props, stream.cuda_stream, flush, 3)
+    out = {"value": world * probs_step / (t_ms * 1e-3), "unit": "probabilities/s",
+           "ms_per_step": t_ms, "steps": steps,
+           "kernel": "atmos_f64_kernel" if w["kind"] == "atmos" else "beam_f64_kernel",
+           "kernel_ms": round(kern_ms, 4), "eigen_table_ms": round(eig_ms, 4)}
+    if peaks.get("fp64"):
+        achieved = flops_launch / (kern_ms * 1e-3) / 1e12
+        out["roofline"] = {"bound": "fp64", "achieved": round(achieved, 3),
+                           "peak": round(peaks["fp64"], 3), "unit": "TFLOP/s",
+                           "frac": round(achieved / peaks["fp64"], 4),
+                           "frac_incl_table": round(flops_launch / ((kern_ms + eig_ms) * 1e-3)
+                                                    / 1e12 / peaks["fp64"], 4),
+                           **ncu_pipe(w.get("name", ""), "fp64")}
+    if refs is not None:
+        errs = channel_errors(props, refs)
+        out["max_abs_err_per_channel"] = errs
+        out["max_abs_err_vs_oracle"] = max(max(v) for v in errs.values())
+    out["clocks"] = clocks
+    for p in props:
+        p.close()
+    return out
+
+
+def reference_gpu(w, m, steps, refs, sample_every=40, timeout=600):
+    """The reference's own FP64 CUDA propagator (AtmosCudaPropagatorSingle, compiled from the
+    reference tree by `make -C oracle refgpu`) on the same grid and parameters, timed through
+    its public, synchronous calculateProbabilities in a child process; every
+    sample_every-th cosine row read back through getProbability and checked against the
+    oracle."""
+    from oracle.oracle import Reference
+    exe = Reference.GPU_BENCH
+    if not os.path.exists(exe):
+        return {"unavailable": "no reference source tree here (CP3_REFERENCE_DIR or "
+                               "baseline/_ref), so the reference's CUDA propagator was not built"}
+    with tempfile.TemporaryDirectory() as d:
+        inp, outb = os.path.join(d, "in.txt"), os.path.join(d, "sample.bin")
+        with open(inp, "w") as f:
+            f.write(f"kind {w['kind']}\nsteps {steps}\nwarmup 1\n")
+            f.write("params %r %r %r %r %r %r\n" % (m.theta12, m.theta13, m.theta23, m.dcp,
+                                                    m.dm12sq, m.dm23sq))
+            if w["kind"] == "atmos":
+                r, rho, ye = w["model"]
+                f.write(f"height_km {w['h']!r}\nsample_every {sample_every}\n")
+                f.write(f"cosines {len(w['cz'])} " + " ".join(repr(float(x)) for x in w["cz"]) + "\n")
+                f.write(f"model {len(r)}\n" + "".join(f"{a!r} {b!r} {c!r}\n" for a, b, c in
+                                                      zip(map(float, r), map(float, rho), map(float, ye))))
+            else:
+                f.write(f"rho {w['rho']!r}\nlength_km {w['L']!r}\n")
+            f.write(f"energies {len(w['en'])} " + " ".join(repr(float(x)) for x in w["en"]) + "\n")
+        try:
+            r = subprocess.run([exe, inp, outb], capture_output=True, text=True, timeout=timeout)
+        except subprocess.TimeoutExpired:
+            return {"unavailable": f"the reference's CUDA propagator did not finish in {timeout} s"}
+        try:
+            res = json.loads(r.stdout.strip().splitlines()[-1])
+        except (ValueError, IndexError):
+            res = {}
+        if r.returncode != 0 or "ms_per_call" not in res:
+            return {"unavailable": f"the reference's CUDA propagator exited {r.returncode}: "
+                                   + (res.get("error") or (r.stdout + r.stderr).strip()[-300:])}
+        ms = np.asarray(res["ms_per_call"], dtype=np.float64)  # [step][nu, nubar]
+        ne = len(w["en"])
+        rows = len(w["cz"][::sample_every]) if w["kind"] == "atmos" else 1
+        sample = np.fromfile(outb, dtype=np.float64)
+    step_ms = float(np.mean(ms.sum(axis=1)))
+    nbins = ne * (len(w["cz"]) if w["kind"] == "atmos" else 1)
+    out = {"value": 9 * nbins * N_TYPES / (step_ms * 1e-3), "unit": "probabilities/s",
+           "ms_per_step": step_ms, "ms_per_call": [round(float(x), 3) for x in ms.mean(axis=0)],
+           "steps": int(len(ms)), "device": res.get("device"),
+           "source": "the reference's AtmosCudaPropagatorSingle/BeamCudaPropagatorSingle "
+                     "(calculateAtmosKernel / calculateBeamKernel, FP64), compiled from its own "
+                     "sources for sm_103a with MaxNLayers raised to 64 through the constants "
+                     "header's include guard; wall time of its synchronous calculateProbabilities",
+           "timing": "one propagator per neutrino type, called one after the other"}
+    if refs is not None and sample.size == 2 * rows * ne * 9:
+        sample = sample.reshape(2, rows, ne, 9)
+        errs = []
+        for t in range(2):
+            ref = refs[t][::sample_every] if w["kind"] == "atmos" else refs[t][None]
+            errs.append(float(np.abs(sample[t] - ref).max()))
+        out["max_abs_err_vs_oracle"] = max(errs)
+        out["checked"] = (f"every {sample_every}th cosine row" if w["kind"] == "atmos"
+                          else "every energy")
+    return out
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if args.workload == "serve":
+        return run_serve(args, rank, world)
+    w = workload(args.workload, rank)
+    if w["kind"] == "batch":
+        if args.precision == "fp64":
+            return run_batch_fp64(args, w, rank, world)
+        return run_batch(args, w, rank, world)
+    w["name"] = args.workload
+    prec = args.precision
+    # weak scaling: each rank propagates its own parameter set over the full grid
+    m = rank_parameter_set(rank, world)
+    props = make_pair(w, prec, m)
+    # A dedicated stream: kernels, events and the L2 flush are all ordered on it (the legacy
+    # default stream's handle is 0, which the C ABI reads as "the handle's own stream").
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    assert sptr != 0
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     if w["kind"] == "atmos":
         nbins = len(w["cz"]) * len(w["en"])
@@ -630,41 +906,14 @@ def run_ours(args, rank, world):
     bytes_out_launch = 9 * nbins * (4 if prec == "mixed" else 8)
 
     # device-resident timed region: K steps, L2 flushed (untimed) between steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    bins_ms, eig_ms = [], []
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with Clocks(dev) as clk:
-        for k in range(args.steps):
-            flush.add_(1.0)
-            ev[k][0].record(stream)
-            step()
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+    step_ms, clocks = time_device_steps(props, stream, flush, args.steps, args.warmup, dev, world)
     t_ms = max_over_ranks(float(np.mean(step_ms)), world, "cuda")
-    if world > 1:
-        torch.distributed.barrier()
     value = world * probs_step / (t_ms * 1e-3)
 
     # The roofline's kernel durations come from a second, serial pass (the two types one
     # after the other on one stream, L2 flushed before each): in the timed steps the types
     # overlap, so each kernel's wall time there includes the other's.
-    for p in props:
-        p.set_profiling(True)
-    for k in range(max(3, args.steps)):
-        for t, p in enumerate(props):
-            flush.add_(1.0)
-            p.calculate_async(t, sptr)
-            a, b = p.kernel_times()
-            eig_ms.append(a)
-            bins_ms.append(b)
-    for p in props:
-        p.set_profiling(False)
-    torch.cuda.synchronize()
-    kernel_ms = float(np.mean(bins_ms))
+    eig_ms, kernel_ms = serial_kernel_times(props, sptr, flush, max(3, args.steps))
 
     # end to end through the public API: grid H2D from pinned memory, compute, full D2H
     is_float = prec == "mixed"
@@ -702,14 +951,17 @@ def run_ours(args, rank, world):
     d2h = bytes_out_launch * len(props)
 
     peaks = fma_peaks(dev)
+    peak = peaks.get("fp32") if prec == "mixed" else peaks.get("fp64")
     achieved = flops_launch / (kernel_ms * 1e-3) / 1e12
-    peak32 = peaks.get("fp32")
     roofline = {
         "bound": "fp32" if prec == "mixed" else "fp64",
         "achieved": round(achieved, 3),
-        "peak": round(peak32 if prec == "mixed" else peaks.get("fp64"), 3),
+        "peak": round(peak, 3),
         "unit": "TFLOP/s",
-        "frac": round(achieved / (peak32 if prec == "mixed" else peaks.get("fp64")), 4),
+        "frac": round(achieved / peak, 4),
+        # the canonical count includes the per-segment eigen-solve, which these kernels do
+        # once per (density class, energy) in the table kernel: charging its time as well
+        "frac_incl_table": round(flops_launch / ((kernel_ms + eig_ms) * 1e-3) / 1e12 / peak, 4),
         "traffic": ncu_traffic(args.workload, prec, bytes_out_launch)[0],
         "traffic_note": ncu_traffic(args.workload, prec, bytes_out_launch)[1],
         **ncu_pipe(args.workload, prec),
@@ -719,7 +971,7 @@ def run_ours(args, rank, world):
                   ("atmos_f64_kernel" if w["kind"] == "atmos" else
                    ("beam_mixed_kernel" if prec == "mixed" else "beam_f64_kernel")),
         "kernel_ms": round(kernel_ms, 4),
-        "eigen_table_ms": round(float(np.mean(eig_ms)), 4),
+        "eigen_table_ms": round(eig_ms, 4),
         "flops_per_launch": flops_launch,
         "hbm_gbs_output": round(bytes_out_launch / (kernel_ms * 1e-3) / 1e9, 1),
     }
@@ -749,50 +1001,108 @@ def run_ours(args, rank, world):
         "e2e": {"value": world * probs_step / (e2e_ms * 1e-3), "unit": "probabilities/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": args.steps * len(props) * (2 if w["kind"] == "atmos" else 1),
-        "max_abs_err_vs_oracle": max_err,
         "roofline": roofline,
         "peaks_tflops": peaks,
     }
+
+    # parity of this run: every bin of both types against the CPU oracle, per channel
+    refs = oracle_full(w, m) if rank == 0 else None
+    if refs is not None:
+        errs = channel_errors(props, refs)
+        line["max_abs_err_vs_oracle"] = max(max(v) for v in errs.values())
+        line["max_abs_err_per_channel"] = dict(errs, channels="a*3+b = P(a->b): e_e, e_m, e_t, "
+                                               "m_e, m_m, m_t, t_e, t_m, t_t",
+                                               bins="every bin of the grid")
+    line["clocks"] = clocks
+    for p in props:
+        p.close()
+    del host_out
+
+    if prec == "mixed" and not args.no_fp64:
+        fp = fp64_arm(w, m, stream, flush, args.steps, args.warmup, dev, world, refs, peaks,
+                      flops_launch)
+        line["fp64"] = fp
+        line["mixed_over_fp64"] = round(value / fp["value"], 2)
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        line["reference_fp64_gpu"] = reference_gpu(w, m, 3, refs)
+        if "value" in line["reference_fp64_gpu"]:
+            line["mixed_over_reference_fp64_gpu"] = round(value / line["reference_fp64_gpu"]["value"], 1)
+    if args.workload == "atmos59" and not args.no_serve:
+        cap, levels, knee, kinds = serve_sweep(dev, [0.5, 0.8, 1.0, 1.2, 1.4, 1.6, 1.8], 1.0, dev)
+        line["serve"] = dict(serve_summary(cap, knee, kinds, levels),
+                             workload="open-loop Poisson arrivals from 64 chains, sizes "
+                                      + ", ".join(k[0] for k in kinds) + "; PREM 4-layer",
+                             levels=[{k: lv[k] for k in ("fraction_of_capacity", "offered_req_per_s",
+                                                         "achieved_req_per_s", "p50_ms", "p99_ms")}
+                                     for lv in levels])
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
-    line["clocks"] = clk.summary()
     return line
 
 
-def check_against_oracle(w, props, m):
-    from oracle.oracle import Mixing as OMix, Oracle
-    orc = Oracle()
-    errs = []
-    for t, p in enumerate(props):
-        got = p.probabilities()
-        knu = 1 if t == 0 else -1
-        mix = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
-        if w["kind"] == "atmos":
-            rows = np.arange(0, len(w["cz"]), max(1, len(w["cz"]) // 50))
-            r, rho, ye = w["model"]
-            ref = orc.atmos(mix, t == 1, w["cz"][rows], w["en"], r, rho, ye, w["h"],
-                            nthreads=os.cpu_count() or 1)
-            errs.append(float(np.abs(got[rows] - ref).max()))
+class CpuPath:
+    """The CPU implementation timed beside the GPU: the reference's own CpuPropagator<double>
+    (AtmosCpuPropagator / BeamCpuPropagator built from its headers into
+    oracle/_ref/libcp3ref_fast.so, MaxNLayers raised to 64) where it was compiled, else the C
+    restatement (oracle/_build/libcp3oracle_fast.so).  Both use OpenMP over cosines."""
+
+    def __init__(self):
+        from oracle.oracle import Oracle, Reference
+        if Reference.available(fast=True):
+            self.impl, self.kind = Reference(fast=True), "reference"
+            self.what = ("the reference's own AtmosCpuPropagator<double>/BeamCpuPropagator<double> "
+                         "compiled from its headers (-O3 -fopenmp, MaxNLayers raised to 64 "
+                         "through the constants header's include guard); time of "
+                         "calculateProbabilities, all host threads")
         else:
-            ref = orc.beam(mix, t == 1, w["en"], w["rho"], w["L"], nthreads=os.cpu_count() or 1)
-            errs.append(float(np.abs(got - ref).max()))
-    return max(errs)
+            self.impl, self.kind = Oracle(fast=True), "port"
+            self.what = ("C restatement of the reference CpuPropagator<double> (oracle/"
+                         "cp3_oracle.c, OpenMP over cosines, -O3), all host threads; the "
+                         "reference's own build needs its source tree, absent on this host")
+
+    def seconds(self, w, m, nthreads):
+        """Compute seconds of one single-grid job, neutrino and antineutrino."""
+        from oracle.oracle import Mixing as OMix
+        total = 0.0
+        for anti, knu in ((False, 1), (True, -1)):
+            mix = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
+            if self.kind == "reference":
+                if w["kind"] == "atmos":
+                    total += self.impl.atmos(mix, anti, w["cz"], w["en"], *w["model"], w["h"],
+                                             nthreads=nthreads, reps=1)[1]
+                else:
+                    for L in np.atleast_1d(w["L"]):
+                        total += self.impl.beam(mix, anti, w["en"], w["rho"], float(L),
+                                                nthreads=nthreads, reps=1)[1]
+                continue
+            t0 = time.perf_counter()
+            if w["kind"] == "atmos":
+                self.impl.atmos(mix, anti, w["cz"], w["en"], *w["model"], w["h"], nthreads=nthreads)
+            else:
+                for L in np.atleast_1d(w["L"]):
+                    self.impl.beam(mix, anti, w["en"], w["rho"], float(L), nthreads=nthreads)
+            total += time.perf_counter() - t0
+        return total
 
 
-def cpu_sample(w, seconds, orc=None, nthreads=1):
+def cpu_run(w, cpu, nthreads, m=None):
+    """Probabilities/s of the CPU implementation on one single-grid job, nu and nubar."""
+    from cudaprob3_gb300 import earth
+    return job_probs(w) / max(cpu.seconds(w, m or earth.NOMINAL, nthreads), 1e-12)
+
+
+def cpu_sample(w, seconds, cpu=None, nthreads=1):
     """A bounded slice of the workload for the CPU, sized from a short probe run to take
-    about ``seconds`` of wall time: every k-th cosine row (keeps the distribution of shells
+    about ``seconds`` of compute: every k-th cosine row (keeps the distribution of shells
     crossed) or a contiguous block of beam energies."""
     if w["kind"] == "atmos":
         stride = max(1, len(w["cz"]) // 8)
-        if orc is not None:
+        if cpu is not None:
             # a warm-up (library, thread pool), then a probe of four rows per thread
             stride = max(1, len(w["cz"]) // (4 * nthreads))
             probe = dict(w, cz=w["cz"][::stride])
-            cpu_run(dict(probe, cz=probe["cz"][:nthreads]), orc, nthreads)
-            t0 = time.perf_counter()
-            cpu_run(probe, orc, nthreads)
-            rows_per_s = len(probe["cz"]) / max(time.perf_counter() - t0, 1e-9)
+            cpu_run(dict(probe, cz=probe["cz"][:nthreads]), cpu, nthreads)
+            rows_per_s = cpu_run(probe, cpu, nthreads) / (job_probs(probe) / len(probe["cz"]))
             # enough rows that the dynamic schedule keeps every thread busy
             rows = max(8 * nthreads, min(len(w["cz"]), int(seconds * rows_per_s)))
             stride = max(1, len(w["cz"]) // rows)
@@ -801,43 +1111,22 @@ def cpu_sample(w, seconds, orc=None, nthreads=1):
             return dict(w, cz=sub), f"the whole grid ({len(sub)} x {len(w['en'])} bins), nu+nubar"
         return dict(w, cz=sub), f"every {stride}th cosine row ({len(sub)} x {len(w['en'])} bins), nu+nubar"
     n = len(w["en"])
-    if orc is not None:
+    if cpu is not None:
         probe = dict(w, en=w["en"][:20000])
-        cpu_run(probe, orc, nthreads)  # warm-up
-        t0 = time.perf_counter()
-        cpu_run(probe, orc, nthreads)
-        n = max(20000, min(n, int(seconds / max((time.perf_counter() - t0) / 20000, 1e-12))))
+        cpu_run(probe, cpu, nthreads)  # warm-up
+        per_energy = 1.0 / (cpu_run(probe, cpu, nthreads) / (job_probs(probe) / 20000))
+        n = max(20000, min(n, int(seconds / max(per_energy, 1e-12))))
     return dict(w, en=w["en"][:n]), f"{n} energies, nu+nubar"
 
 
-def cpu_run(w, orc, nthreads, m=None):
-    """Probabilities/s of the C restatement on one single-grid workload, nu and nubar."""
-    from cudaprob3_gb300 import earth
-    from oracle.oracle import Mixing as OMix
-    m = m or earth.NOMINAL
-    t0 = time.perf_counter()
-    nbins = 0
-    for anti, knu in ((False, 1), (True, -1)):
-        mix = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
-        if w["kind"] == "atmos":
-            r, rho, ye = w["model"]
-            orc.atmos(mix, anti, w["cz"], w["en"], r, rho, ye, w["h"], nthreads=nthreads)
-            nbins += len(w["cz"]) * len(w["en"])
-        else:
-            for L in np.atleast_1d(w["L"]):
-                orc.beam(mix, anti, w["en"], w["rho"], float(L), nthreads=nthreads)
-                nbins += len(w["en"])
-    return 9 * nbins / (time.perf_counter() - t0)
-
-
-def cpu_jobs(w, seconds, orc, nthreads):
+def cpu_jobs(w, seconds, cpu, nthreads):
     """The CPU's share of a workload: (list of (single-grid workload, parameter set), text).
     Single grids are sliced by cpu_sample; batched workloads take their first parameter sets
     on their own grids, as many as fit about ``seconds``; serving takes 500 x 500 PREM-4
     requests (the size its latency target is quoted for)."""
     from cudaprob3_gb300 import earth
     if w["kind"] in ("atmos", "beam"):
-        sw, desc = cpu_sample(w, seconds, orc, nthreads)
+        sw, desc = cpu_sample(w, seconds, cpu, nthreads)
         return [(sw, None)], desc
     if w["kind"] == "serve":
         req = dict(kind="atmos", model=earth.PREM_4LAYER, cz=earth.cosine_grid(500),
@@ -856,7 +1145,7 @@ def cpu_jobs(w, seconds, orc, nthreads):
         what = "atmospheric problems on their own grids, one parameter set each"
     jobs, t0 = [], time.perf_counter()
     for job in cands:  # the probe is the sample itself: stop once the budget is spent
-        cpu_run(job[0], orc, nthreads, job[1])
+        cpu_run(job[0], cpu, nthreads, job[1])
         jobs.append(job)
         if time.perf_counter() - t0 >= seconds:
             break
@@ -870,35 +1159,35 @@ def job_probs(w):
     return 9 * N_TYPES * len(w["en"]) * len(np.atleast_1d(w["L"]))
 
 
-def run_jobs(jobs, orc, nthreads):
-    """Probabilities/s over a list of jobs (one pass)."""
-    t0 = time.perf_counter()
-    for w, m in jobs:
-        cpu_run(w, orc, nthreads, m)
-    return sum(job_probs(w) for w, _ in jobs) / (time.perf_counter() - t0)
+def run_jobs(jobs, cpu, nthreads):
+    """Probabilities/s over a list of jobs (one pass; compute time only)."""
+    from cudaprob3_gb300 import earth
+    secs = sum(cpu.seconds(w, m or earth.NOMINAL, nthreads) for w, m in jobs)
+    return sum(job_probs(w) for w, _ in jobs) / max(secs, 1e-12)
 
 
 def cpu_baseline(w, seconds=2.0):
-    from oracle.oracle import Oracle
-    orc = Oracle(fast=True)
+    cpu = CpuPath()
     cores = os.cpu_count() or 1
-    jobs, desc = cpu_jobs(w, seconds, orc, cores)  # the sizing run also warms up
-    rate = run_jobs(jobs, orc, cores)
-    return {"value": rate, "unit": "probabilities/s", "cores": cores, "kind": "port",
-            "sample": desc + "; C restatement of the reference CpuPropagator<double> "
-                             "(OpenMP over cosines, -O3), all host threads"}
+    jobs, desc = cpu_jobs(w, seconds, cpu, cores)  # the sizing run also warms up
+    rate = run_jobs(jobs, cpu, cores)
+    return {"value": rate, "unit": "probabilities/s", "cores": cores, "kind": cpu.kind,
+            "sample": desc + "; " + cpu.what}
 
 
 def run_reference(args):
-    """The reference arm: the reference's CPU algorithm (C restatement) on the host cores."""
-    from oracle.oracle import Oracle
+    """The reference arm: the reference's own CPU propagators (where its sources were found
+    and compiled; else the C restatement) on the host cores, on a bounded sample."""
+    from oracle import oracle
+    oracle.build()
+    oracle.build_reference(gpu=False)
     w = workload(args.workload)
-    orc = Oracle(fast=True)
+    cpu = CpuPath()
     cores = os.cpu_count() or 1
-    jobs, desc = cpu_jobs(w, args.cpu_seconds, orc, cores)
+    jobs, desc = cpu_jobs(w, args.cpu_seconds, cpu, cores)
     for _ in range(max(0, args.warmup - 1)):  # the sizing pass was the first warm-up
-        run_jobs(jobs, orc, cores)
-    rates = [run_jobs(jobs, orc, cores) for _ in range(args.steps)]
+        run_jobs(jobs, cpu, cores)
+    rates = [run_jobs(jobs, cpu, cores) for _ in range(args.steps)]
     value = float(np.median(rates))
     probs_step = sum(job_probs(j) for j, _ in jobs)
     return {
@@ -910,10 +1199,7 @@ def run_reference(args):
         "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"],
                                         "sample": desc},
         "cpu_baseline": {"value": value, "unit": "probabilities/s", "cores": cores,
-                         "kind": "port",
-                         "sample": desc + "; reference CPU algorithm restated in C "
-                                          "(oracle/cp3_oracle.c), the reference's own build "
-                                          "needs its source tree, absent on this host"},
+                         "kind": cpu.kind, "sample": desc + "; " + cpu.what},
         "e2e": {"value": value, "unit": "probabilities/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -927,12 +1213,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="atmos59",
                     choices=["atmos59", "prem4", "beam", "batch_atmos", "batch_beam", "serve"])
-    ap.add_argument("--serve-seconds", type=float, default=2.0)
-    ap.add_argument("--serve-think", type=float, nargs="*", default=None,
-                    help="mean think times (ms) of the chains, one load level each")
+    ap.add_argument("--serve-seconds", type=float, default=1.5,
+                    help="seconds of arrivals per offered-load level")
+    ap.add_argument("--serve-loads", type=float, nargs="*", default=None,
+                    help="offered loads as fractions of the measured capacity, one level each")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=2.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="leave out the plain FP64 arm of the single-grid workloads")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="leave out the serving sweep of the default workload")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="leave out the reference's own FP64 CUDA propagator")
     ap.add_argument("--batch-sets", type=int, default=0,
                     help="parameter sets of the batched workloads (default: the configuration's)")
     args = ap.parse_args()

@@ -32,7 +32,7 @@ EXPORTS = (
     "cp3_server_add_atmos_grid", "cp3_server_add_beam_grid", "cp3_server_start",
     "cp3_server_submit", "cp3_server_wait", "cp3_server_result", "cp3_server_copy_result",
     "cp3_server_release",
-    "cp3_server_stats",
+    "cp3_server_stats", "cp3_server_poll", "cp3_server_debug_fail_launches",
 )
 
 CP3_OK = 0
@@ -112,6 +112,8 @@ _SIGS = {
     "cp3_server_release": ([_h, C.c_ulonglong], C.c_int),
     "cp3_server_stats": ([_h, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                           C.POINTER(C.c_longlong)], C.c_int),
+    "cp3_server_poll": ([_h, C.POINTER(C.c_ulonglong), C.c_int, C.c_double, _ip], C.c_int),
+    "cp3_server_debug_fail_launches": ([_h, C.c_int], C.c_int),
     "cp3_atmos_mixed_noalloc": ([C.c_int, C.c_void_p, C.c_int, _ip, _dp, _ip, C.c_int, _dp, C.c_int]
                                 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double, C.c_int,
                                                       C.c_void_p, C.c_void_p, C.c_char_p,

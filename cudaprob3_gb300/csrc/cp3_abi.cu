@@ -358,9 +358,6 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
         if (!h->height_set)
             return fail(h, CP3_ERR_NOT_SET,
                         "CudaPropagatorSingle::calculateProbabilities. production height was not set");
-        if (h->avg_bins > 0 && h->precision != CP3_FP64 && h->model.poly)
-            return fail(h, CP3_ERR_UNSUPPORTED,
-                        "production-height averaging with a quadratic density model runs on the FP64 kernels (create the handle with CP3_FP64)");
         const bool traj_was_dirty = h->traj_dirty;
         int rc = prepare_atmos(h);
         if (rc) return rc;
@@ -381,6 +378,10 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
         }
         mark(1);
         auto bins = [&](RowRange rr) {
+            if (h->model.poly && mixed && avm.nb > 0)
+                return launch_atmos_mixed_inline_avg(p, h->d_energies.ptr, h->ne, h->d_seg_off.ptr,
+                                                     h->d_seg_len_df.ptr, h->d_seg_rho.ptr, h->nc,
+                                                     avm, (float*)h->d_result.ptr, s, rr);
             if (h->model.poly)
                 return launch_atmos_inline(p, mixed, h->d_energies.ptr, h->ne, h->d_seg_off.ptr,
                                            mixed ? (const void*)h->d_seg_len_df.ptr

@@ -10,6 +10,7 @@
 // 32 consecutive elements (128 B in FP32, 256 B in FP64).
 #include "cp3_device.cuh"
 #include "cp3_kernels.hpp"
+#include "cp3_f64.cuh"
 #include "cp3_mixed.cuh"
 
 namespace cp3 {
@@ -34,51 +35,6 @@ constexpr int kMaxGridY = 65535;
 // W (B^T S_M B) S_0 W^+ with B = S_{M-1}..S_1: M+1 layer applications instead of 2M-1
 // complex 3x3 products.  The phases are formed exactly as the reference forms them, so
 // their roundings -- which matter over ~120 layers of up to ~800 rad -- are the reference's.
-
-struct cm3 {
-    cd a[3][3];
-};
-
-// One FP64 layer in factored form.
-struct Layer64 {
-    double u[2][3];  // unit eigenvectors u1, u2 (rotated basis)
-    cd z[2];         // e^{i (arg_k - arg_0)} - 1, k = 1, 2
-};
-
-// The phases of one layer from dmMatVac[k][0], as getArg (physics.hpp:439-450) evaluates
-// them; arg[] receives arg_k.  The relative phase arg_k - arg_0 is taken exactly, as a
-// TwoSum pair dh + dl (a rounded difference could be off by 1e-13 rad at ~800 rad, which
-// ~120 layers would accumulate), and e^{i(dh + dl)} = e^{i dh} (1 + i dl) to second order in
-// |dl| <= 1e-13: two sincos per layer instead of the three of multiply_phase_matrix
-// (math.hpp:59-75), with the reference's relative phases to ~1e-16.
-// x / E, correctly rounded, from rE = 1/E correctly rounded: q = x rE, then one correction
-// with the exact residual x - q E (an FMA).  By Markstein's theorem (P. Markstein,
-// "Computation of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
-// Dev. 34, 1990) the corrected quotient is the correctly rounded x / E; an exhaustive-style
-// check against IEEE division (4e8 random and edge-significand operand pairs) found no
-// difference.  Three FP64 instructions instead of a full division: the reference's phase
-// roundings at a fraction of the cost on GB300's narrow FP64 pipe.
-__device__ __forceinline__ double div_by(double x, double E, double rE) {
-    const double q = __dmul_rn(x, rE);
-    return fma(fma(-q, E, x), rE, q);
-}
-
-__device__ __forceinline__ void layer64_phases(const double dmv[3], double L, double E,
-                                               double rE, Layer64& f, double arg[3]) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) arg[k] = div_by(__dmul_rn(__dmul_rn(-kLoEFac, dmv[k]), L), E, rE);
-#pragma unroll
-    for (int kk = 0; kk < 2; kk++) {
-        const int k = kk + 1;
-        const double dh = __dadd_rn(arg[k], -arg[0]);  // TwoSum (Knuth)
-        const double bb = __dadd_rn(dh, -arg[k]);
-        const double dl = __dadd_rn(__dadd_rn(arg[k], -__dadd_rn(dh, -bb)), __dadd_rn(-arg[0], -bb));
-        double s, c;
-        sincos(dh, &s, &c);
-        // e^{i dh} (1 + i dl) - 1
-        f.z[kk] = cd{(c - 1.0) - s * dl, s + c * dl};
-    }
-}
 
 // Table entry (10 doubles, five 16-byte words): u1, u2, dmMatVac[0..2][0], 1 unused.
 __device__ __forceinline__ void layer64_from_table(const double* __restrict__ t, double L,
@@ -134,42 +90,6 @@ __device__ __forceinline__ void apply_right64(const Layer64& f, cm3& G) {
                 G.a[i][j].im += yi * u[j];
             }
         }
-    }
-}
-
-// G = S
-__device__ __forceinline__ void layer_to_gen64(const Layer64& f, cm3& G) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = i; j < 3; j++) {
-            const double p0 = f.u[0][i] * f.u[0][j], p1 = f.u[1][i] * f.u[1][j];
-            const cd v{(i == j ? 1.0 : 0.0) + f.z[0].re * p0 + f.z[1].re * p1,
-                       f.z[0].im * p0 + f.z[1].im * p1};
-            G.a[i][j] = v;
-            G.a[j][i] = v;
-        }
-}
-
-// Flavour-basis amplitude A = W A2 W^+, W = [[1,0,0],[0,c,s e],[0,-s,c e]], e = e^{i d}.
-__device__ __forceinline__ void to_flavour64(const cm3& A2, const double* w, cm3& A) {
-    const double c = w[0], s = w[1], er = w[2], ei = w[3];
-    cm3 Y;  // A2 W^+
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const cd a1 = A2.a[i][1], a2 = A2.a[i][2];
-        const cd f{a2.re * er + a2.im * ei, a2.im * er - a2.re * ei};  // e* a2
-        Y.a[i][0] = A2.a[i][0];
-        Y.a[i][1] = cd{c * a1.re + s * f.re, c * a1.im + s * f.im};
-        Y.a[i][2] = cd{-s * a1.re + c * f.re, -s * a1.im + c * f.im};
-    }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        const cd y1 = Y.a[1][j], y2 = Y.a[2][j];
-        const cd g{y2.re * er - y2.im * ei, y2.re * ei + y2.im * er};  // e y2
-        A.a[0][j] = Y.a[0][j];
-        A.a[1][j] = cd{c * y1.re + s * g.re, c * y1.im + s * g.im};
-        A.a[2][j] = cd{-s * y1.re + c * g.re, -s * y1.im + c * g.im};
     }
 }
 
@@ -476,6 +396,11 @@ cudaError_t launch_atmos_mixed(const OscParams& p, const float* table, int ne,
     return cudaGetLastError();
 }
 
+cudaError_t preload_atmos_mixed() {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, atmos_mixed_kernel);
+}
+
 cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* energies, int ne,
                                 const int* seg_off, const void* seg_len, const double* seg_rho,
                                 int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s,
@@ -531,22 +456,14 @@ __device__ __forceinline__ void to_flavour_f32(const cg9& A2, const WParams& w, 
     }
 }
 
-__global__ void __launch_bounds__(kBlock)
-    atmos_mixed_avg_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
-                           const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
-                           int ic0, int nc, AvgMixed av, float* __restrict__ out) {
-    __shared__ float2 s_len[kMaxSegments];
-    const int ic = ic0 + blockIdx.y;
-    const int s0 = seg_off[ic];
-    const int nseg = seg_off[ic + 1] - s0;
-    for (int i = threadIdx.x; i < nseg; i += kBlock) s_len[i] = seg_len[s0 + i];
-    __syncthreads();
-    const int ie = blockIdx.x * kBlock + threadIdx.x;
-    if (ie >= ne) return;
-    const float* tab = table + (size_t)ie * kMixFields;
-    const size_t cls_stride = (size_t)kMixFields * ne_pad;
-    const int M = nseg - 1;
-    auto seg = [&](int l, Layer& F) { layer_from_table(tab + l * cls_stride, s_len[l], F); };
+// One averaged bin: the chain of segments 1..M (seg(l, F) gives segment l's layer), then the
+// amplitude split over the air layer's eigencomponents (F0, with phase rates om1, om2 in turns
+// per km) and the reference's cross terms with their shift factors.
+template <class SegFn>
+__device__ __forceinline__ void atmos_bin_mixed_avg(SegFn seg, int M, const Layer& F0, df om1,
+                                                    df om2, const WParams& w, const AvgMixed& av,
+                                                    int ic, int nc, int ie, int ne,
+                                                    float* __restrict__ out) {
     cg9 G;
     if (M == 0) {
 #pragma unroll
@@ -557,14 +474,9 @@ __global__ void __launch_bounds__(kBlock)
         chain_mixed(seg, M, G);
         if (M >= kNewtonSchulzMinShells) newton_schulz(G);
     }
-    Layer F0;
-    const float* t0 = tab;  // class 0: the air
-    layer_from_table(t0, s_len[0], F0);
-
     // shift factors of the pairs (1,0), (2,0), (2,1): the reference's d = d0[k] - d0[q] is
-    // -(omega_k - omega_q) per km of path-length shift (omega_0 = 0); the table holds the
-    // rates in turns per km
-    const df om1{__ldg(t0 + 6), __ldg(t0 + 8)}, om2{__ldg(t0 + 7), __ldg(t0 + 9)};
+    // -(omega_k - omega_q) per km of path-length shift (omega_0 = 0); the rates are in turns
+    // per km
     const df dom[3] = {om1, om2, df_sub(om2, om1)};
     cf sf[3][3];
 #pragma unroll
@@ -641,6 +553,59 @@ __global__ void __launch_bounds__(kBlock)
         }
 }
 
+
+__global__ void __launch_bounds__(kBlock)
+    atmos_mixed_avg_kernel(WParams w, const float* __restrict__ table, int ne, int ne_pad,
+                           const int* __restrict__ seg_off, const float2* __restrict__ seg_len,
+                           int ic0, int nc, AvgMixed av, float* __restrict__ out) {
+    __shared__ float2 s_len[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) s_len[i] = seg_len[s0 + i];
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const float* tab = table + (size_t)ie * kMixFields;
+    const size_t cls_stride = (size_t)kMixFields * ne_pad;
+    auto seg = [&](int l, Layer& F) { layer_from_table(tab + l * cls_stride, s_len[l], F); };
+    Layer F0;
+    const float* t0 = tab;  // class 0: the air
+    layer_from_table(t0, s_len[0], F0);
+    const df om1{__ldg(t0 + 6), __ldg(t0 + 8)}, om2{__ldg(t0 + 7), __ldg(t0 + 9)};
+    atmos_bin_mixed_avg(seg, nseg - 1, F0, om1, om2, w, av, ic, nc, ie, ne, out);
+}
+
+// The same with the quadratic density model: every segment solves its own eigen-system
+// (segment_layer_inline), the air layer's included.
+__global__ void __launch_bounds__(kBlock)
+    atmos_mixed_inline_avg_kernel(const __grid_constant__ OscParams p, WParams w,
+                                  const double* __restrict__ energies, int ne,
+                                  const int* __restrict__ seg_off,
+                                  const float2* __restrict__ seg_len,
+                                  const double* __restrict__ seg_rho, int ic0, int nc,
+                                  AvgMixed av, float* __restrict__ out) {
+    __shared__ float2 s_len[kMaxSegments];
+    __shared__ double s_rho[kMaxSegments];
+    const int ic = ic0 + blockIdx.y;
+    const int s0 = seg_off[ic];
+    const int nseg = seg_off[ic + 1] - s0;
+    for (int i = threadIdx.x; i < nseg; i += kBlock) {
+        s_len[i] = seg_len[s0 + i];
+        s_rho[i] = seg_rho[s0 + i];
+    }
+    __syncthreads();
+    const int ie = blockIdx.x * kBlock + threadIdx.x;
+    if (ie >= ne) return;
+    const double E = energies[ie];
+    auto seg = [&](int l, Layer& F) { segment_layer_inline(&p, E, s_rho[l], s_len[l], F); };
+    Layer F0;
+    float om[2][2];
+    segment_layer_inline_rates(&p, E, s_rho[0], s_len[0], F0, om);
+    atmos_bin_mixed_avg(seg, nseg - 1, F0, df{om[0][0], om[0][1]}, df{om[1][0], om[1][1]}, w, av,
+                        ic, nc, ie, ne, out);
+}
+
 cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int ne,
                                    const int* seg_off, const float2* seg_len, int n_cosines,
                                    const AvgMixed& av, float* out, cudaStream_t s,
@@ -656,6 +621,25 @@ cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int n
         dim3 grid((ne + kBlock - 1) / kBlock, rows);
         atmos_mixed_avg_kernel<<<grid, kBlock, 0, s>>>(w, table, ne, ne_pad, seg_off, seg_len,
                                                        ic0, n_cosines, a, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_atmos_mixed_inline_avg(const OscParams& p, const double* energies, int ne,
+                                          const int* seg_off, const float2* seg_len,
+                                          const double* seg_rho, int n_cosines,
+                                          const AvgMixed& av, float* out, cudaStream_t s,
+                                          RowRange rr) {
+    if (ne <= 0 || n_cosines <= 0) return cudaSuccess;
+    const WParams w = wparams(p);
+    AvgMixed a = av;
+    a.type = p.anti;
+    const int end = rr.end < 0 ? n_cosines : rr.end;
+    for (int ic0 = rr.begin; ic0 < end; ic0 += kMaxGridY) {
+        const int rows = end - ic0 < kMaxGridY ? end - ic0 : kMaxGridY;
+        dim3 grid((ne + kBlock - 1) / kBlock, rows);
+        atmos_mixed_inline_avg_kernel<<<grid, kBlock, 0, s>>>(p, w, energies, ne, seg_off, seg_len,
+                                                              seg_rho, ic0, n_cosines, a, out);
     }
     return cudaGetLastError();
 }

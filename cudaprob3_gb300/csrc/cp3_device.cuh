@@ -74,89 +74,6 @@ CP3_HD void matter_masses_f64(const OscParams* __restrict__ p, double E,
     }
 }
 
-// physics::get_product + getA (physics.hpp:345-430, 516-598): the beam amplitude
-// A = U (sum_k e^{i arg_k} prod_k) U^dagger through AXFAC.  A[n][m]: row = final flavour.
-CP3_HD void beam_amplitude_f64(const OscParams* __restrict__ p, double E,
-                                                   double rho, double L, cd A[3][3]) {
-    double mm[3];
-    matter_masses_f64(p, E, rho, mm);
-    const double fac = p->anti ? kTwoRtTwoGf * E * rho : -kTwoRtTwoGf * E * rho;
-    double dMV[3][3], dMM[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            dMM[i][j] = mm[i] - mm[j];
-            dMV[i][j] = mm[i] - CP3_DM(p, j, 0);
-        }
-    cd h[3][3][3];
-#pragma unroll
-    for (int n = 0; n < 3; n++)
-#pragma unroll
-        for (int m = 0; m < 3; m++) {
-            const cd a = CP3_U(p, 0, n), b = CP3_U(p, 0, m);
-            const double re = -fac * (a.re * b.re + a.im * b.im);
-            const double im = -fac * (a.re * b.im - a.im * b.re);
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                h[n][m][j].re = re;
-                h[n][m][j].im = im;
-            }
-        }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        h[0][0][j].re -= dMV[j][0];
-        h[1][1][j].re -= dMV[j][1];
-        h[2][2][j].re -= dMV[j][2];
-    }
-    const double den[3] = {dMM[0][1] * dMM[0][2], dMM[1][2] * dMM[1][0], dMM[2][0] * dMM[2][1]};
-    double sn[3], cs[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) sincos(-kLoEFac * dMV[k][0] * L / E, &sn[k], &cs[k]);
-    cd X[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            cd pr[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) pr[k] = cd{0.0, 0.0};
-#pragma unroll
-            for (int q = 0; q < 3; q++)
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    const int f = (k + 1) % 3, s = (k + 2) % 3;
-                    const cd x = h[i][q][f], y = h[q][j][s];
-                    pr[k].re += x.re * y.re - x.im * y.im;
-                    pr[k].im += x.re * y.im + x.im * y.re;
-                }
-            cd acc{0.0, 0.0};
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const double pre = pr[k].re / den[k], pim = pr[k].im / den[k];
-                acc.re += cs[k] * pre - sn[k] * pim;
-                acc.im += cs[k] * pim + sn[k] * pre;
-            }
-            X[i][j] = acc;
-        }
-#pragma unroll
-    for (int n = 0; n < 3; n++)
-#pragma unroll
-        for (int m = 0; m < 3; m++) {
-            double re = 0, im = 0;
-            const double* f = &p->axfac[(n * 3 + m) * 36];
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    const double* g = f + (i * 3 + j) * 4;
-                    re += g[0] * X[i][j].re + g[1] * X[i][j].im;
-                    im += g[2] * X[i][j].im + g[3] * X[i][j].re;
-                }
-            A[n][m] = cd{re, im};
-        }
-}
-
 // Index of (i, j), i <= j, in the 6-entry storage of a symmetric 3x3 matrix.
 __host__ __device__ constexpr int sidx(int i, int j) {
     return i <= j ? (i == 0 ? j : (i == 1 ? 2 + j : 5)) : (j == 0 ? i : (j == 1 ? 2 + i : 5));
@@ -528,9 +445,12 @@ __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restr
     const float pp = fmaf(-a2, s, a1);                        // c1 - c2^2/3  (< 0)
     const float qq = fmaf(s, fmaf(-2.0f * s, s, a1), -a0);    // -(2 s^3 - s c1 + c0)
     const float mp3 = fmaxf(-pp * (1.0f / 3.0f), 1e-30f);
-    const float rt = sqrtf(mp3);
+    // The starting roots need only ~1e-6 relative accuracy (the Newton steps below remove
+    // what is left, as they remove __sincosf's), so the square root and the division take
+    // the fast forms: C3 1 %, the table kernel 4 % faster, every result's error unchanged.
+    const float rt = mp3 * rsqrtf(mp3);
     // t = 2 sqrt(m) cos(a) solves t^3 + P t + Q = 0 when cos(3a) = -Q / (2 m^{3/2})
-    const float carg = fminf(1.0f, fmaxf(-1.0f, (-0.5f * qq) / (mp3 * rt)));
+    const float carg = fminf(1.0f, fmaxf(-1.0f, __fdividef(-0.5f * qq, mp3 * rt)));
     const float th = acosf(carg) * (1.0f / 3.0f);
     // cos(th - 2 pi/3) = -cos(th)/2 + (sqrt(3)/2) sin(th): one sincos for both roots.  The
     // hardware approximation (absolute error ~4e-7 on [0, pi/3]) puts the starting roots

@@ -50,20 +50,6 @@ void build_osc_params(const MixingInput& m, int antineutrino, OscParams* o) {
     D[5] = mv[1] - mv[2];
     D[7] = -D[5];
 
-    // setMixMatrix: AXFAC (physics.hpp:135-146)
-    for (int n = 0; n < 3; n++)
-        for (int mm = 0; mm < 3; mm++)
-            for (int i = 0; i < 3; i++)
-                for (int j = 0; j < 3; j++) {
-                    const double ar = U[(n * 3 + i) * 2], ai = U[(n * 3 + i) * 2 + 1];
-                    const double br = U[(mm * 3 + j) * 2], bi = U[(mm * 3 + j) * 2 + 1];
-                    double* f = &o->axfac[(((n * 3 + mm) * 3 + i) * 3 + j) * 4];
-                    f[0] = ar * br + ai * bi;
-                    f[1] = ar * bi - ai * br;
-                    f[2] = ai * bi + ar * br;
-                    f[3] = ai * br - ar * bi;
-                }
-
     // prepare_getMfast (physics.hpp:198-252): vacuum roots, then which root is which state.
     {
         const double aV = D[1] + D[2];

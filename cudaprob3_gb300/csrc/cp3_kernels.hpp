@@ -27,6 +27,13 @@ cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int n
 cudaError_t launch_table_mixed(const OscParams& p, const float2* energies, int ne,
                                const float2* cls_rho, int ncls, float* table, cudaStream_t s);
 
+// Loads the mixed table kernel (the double-input instance) and the mixed per-bin kernel
+// into the current device's context, as their first launch would.  With lazy module
+// loading that first load may allocate device memory; a caller that must not allocate
+// later (cp3_atmos_mixed_noalloc) calls these once, at set-up.
+cudaError_t preload_table_mixed();
+cudaError_t preload_atmos_mixed();
+
 // Production-height averaging inputs of the FP64 kernels (n_bins == 0: fixed height).
 struct AvgArrays {
     const double* prob = nullptr;    // [2][3][ne][nc][n_bins]
@@ -67,6 +74,13 @@ cudaError_t launch_atmos_mixed_avg(const OscParams& p, const float* table, int n
                                    const int* seg_off, const float2* seg_len, int n_cosines,
                                    const AvgMixed& av, float* out, cudaStream_t s,
                                    RowRange rr = RowRange{});
+
+// Mixed averaged bins with the quadratic density model (per-segment eigen-solve).
+cudaError_t launch_atmos_mixed_inline_avg(const OscParams& p, const double* energies, int ne,
+                                          const int* seg_off, const float2* seg_len,
+                                          const double* seg_rho, int n_cosines,
+                                          const AvgMixed& av, float* out, cudaStream_t s,
+                                          RowRange rr = RowRange{});
 
 // Atmospheric bins whose segments each carry their own electron density (quadratic model):
 // per-segment eigen-solve.  seg_len: double[] (FP64) or float2[] hi/lo (mixed).

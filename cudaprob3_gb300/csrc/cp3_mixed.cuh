@@ -409,10 +409,11 @@ __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, s
 }
 
 // Layer of a segment whose density is its own (quadratic density model): the
-// eigen-decomposition is solved for this segment (double-float refined).
-__device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict__ p, double E,
-                                                     double rho_e, float2 L, Layer& f) {
-    float om[2][2];
+// eigen-decomposition is solved for this segment (double-float refined).  The _rates form
+// also returns the phase rates (the averaging kernel needs the air layer's).
+__device__ __forceinline__ void segment_layer_inline_rates(const OscParams* __restrict__ p,
+                                                           double E, double rho_e, float2 L,
+                                                           Layer& f, float om[2][2]) {
     rotated_eigen_vectors(p, df_from(E), df_from(rho_e), f.u, om);
     float2 lo, zr, zi;
     const float2 r = reduced_turn2(make_float2(om[0][0], om[1][0]),
@@ -422,6 +423,11 @@ __device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict
     f.z[0][1] = zi.x;
     f.z[1][0] = zr.y;
     f.z[1][1] = zi.y;
+}
+__device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict__ p, double E,
+                                                     double rho_e, float2 L, Layer& f) {
+    float om[2][2];  // the phase rates omega_k / 2 pi (hi, lo), turns per km
+    segment_layer_inline_rates(p, E, rho_e, L, f, om);
 }
 
 // One beam energy (E, rho_e as double or float pair): eigen-decomposition (double-float

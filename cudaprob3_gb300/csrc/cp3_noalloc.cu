@@ -7,6 +7,12 @@
 // two kernels as a MIXED atmospheric handle (eigen table, then the per-bin kernel), but the
 // eigen table and the staged trajectory table live in one file-scope device array whose
 // size is fixed when the library is loaded.  Inputs and outputs still belong to the caller.
+//
+// The first call on each device is its set-up: with that device current it looks up the
+// array's device address (cudaGetSymbolAddress) and loads the kernels the call launches.
+// Under lazy module loading (the CUDA default) those loads are where the driver places the
+// array and the kernels' code in device memory, so the set-up call may allocate; every later
+// call on that device allocates nothing.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -46,6 +52,19 @@ __global__ void split_lengths_kernel(const double* __restrict__ len, int n, floa
     if (i >= n) return;
     const float hi = (float)len[i];
     out[i] = make_float2(hi, (float)(len[i] - (double)hi));
+}
+
+// Set-up on the current device: the scratch's device address, and every kernel of the call
+// loaded now rather than at its first launch.
+cudaError_t setup_device(float** scratch) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    cudaFuncAttributes a;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, split_lengths_kernel);
+    if (e == cudaSuccess) e = preload_table_mixed();
+    if (e == cudaSuccess) e = preload_atmos_mixed();
+    if (e == cudaSuccess) *scratch = static_cast<float*>(p);
+    return e;
 }
 
 }  // namespace
@@ -113,22 +132,23 @@ extern "C" int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int
     int prev = -1;
     cudaGetDevice(&prev);
 
-    // ---- once per device, with that device current: the scratch's device address ----------
+    // ---- once per device, with that device current: the scratch's device address and the
+    //      kernels loaded (the set-up call) ------------------------------------------------
     float* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
         if (!g_scratch_on[device]) {
             cudaError_t e = cudaSetDevice(device);
-            void* p = nullptr;
-            if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            float* p = nullptr;
+            if (e == cudaSuccess) e = setup_device(&p);
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 if (prev >= 0) cudaSetDevice(prev);
                 if (err && err_len > 0)
-                    std::snprintf(err, err_len, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+                    std::snprintf(err, err_len, "no-allocation set-up: %s", cudaGetErrorString(e));
                 return CP3_ERR_CUDA;
             }
-            g_scratch_on[device] = static_cast<float*>(p);
+            g_scratch_on[device] = p;
         }
         base = g_scratch_on[device];
     }

@@ -9,7 +9,11 @@
 // runs overlaps on the device.  Grids (trajectory tables, energies,
 // class densities) are registered once and stay resident; each request's eigen table and
 // result live in a device pool until the client releases the request.  A host callback on the
-// stream stamps the completion time of every request of a launch.
+// stream stamps the completion time and the status of every request of a launch: the
+// launch's graph clears the kernel's status word first and copies it into page-locked host
+// memory last, so the callback reads it without a CUDA call.  A launch whose CUDA calls fail
+// fails its own requests (cp3_server_wait reports the error, cp3_server_result refuses the
+// result) and no others.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -121,12 +125,18 @@ public:
 
 enum { kQueued = 0, kRunning = 1, kDone = 2 };
 
+// A finished request's status: 0, the persistent kernel's status word (kStatusWaitLimit,
+// kStatusKind, kStatusBounds), or kReqLaunchFailed when a CUDA call of its launch failed on the
+// host side (the message is in cp3_server::launch_error).
+constexpr int kReqLaunchFailed = -1;
+
 struct Request {
     uint64_t id = 0;
     int tmpl = 0;
     OscParams params;
     int64_t t_submit = 0, t_start = 0, t_done = 0;
     size_t pool_off = 0, pool_units = 0;
+    std::atomic<int> status{0};  // written before state becomes kDone
     std::atomic<int> state{kQueued};
 };
 
@@ -144,6 +154,7 @@ struct Slot {
     HBuf<int> h_a, h_b;
     HBuf<Header> h_hdr;
     HBuf<OscParams> h_params;
+    HBuf<int> h_status;  // the launch's status word, copied back by the graph's last node
     std::vector<std::shared_ptr<Request>> reqs;
     bool busy = false;
     std::atomic<int> finished{0};
@@ -154,7 +165,7 @@ struct Slot {
 struct cp3_server {
     int device = 0, sms = 0;
     std::string err;
-    std::mutex mu;  // requests map, incoming queue, pool, stats
+    std::mutex mu;  // requests map, queues, pool, stats
     std::condition_variable cv;
     EarthModel model;
     bool model_set = false;
@@ -175,13 +186,26 @@ struct cp3_server {
     Slot slots[2];
 
     std::unordered_map<uint64_t, std::shared_ptr<Request>> requests;
-    std::deque<std::shared_ptr<Request>> incoming;
+    // The queue: one FIFO per registered grid (all its requests have the same size), and the
+    // grids in increasing size.  Packing a launch touches only the FIFOs' heads and the
+    // requests it admits, however deep the queue.
+    std::vector<std::deque<std::shared_ptr<Request>>> queues;
+    std::vector<int> by_size;
+    long long queued = 0;
     uint64_t next_id = 1;
     std::thread loop;
     std::atomic<bool> stop{false};
     bool started = false;
     std::atomic<long long> launches{0}, completed{0};
-    std::atomic<int> kernel_status{0};
+    std::string launch_error;      // the last failed launch's CUDA error (under mu)
+    int debug_fail_launches = 0;   // testing aid: cp3_server_debug_fail_launches (under mu)
+
+    // completion queue for cp3_server_poll: ids in completion order, recorded once a client
+    // has called poll (so a server nobody polls keeps no list)
+    std::mutex cq_mu;
+    std::condition_variable cq_cv;
+    std::deque<uint64_t> completions;
+    std::atomic<bool> record_completions{false};
 
     ~cp3_server();
 };
@@ -210,57 +234,84 @@ int scuda(cp3_server* s, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return scuda(s, e_, where);  \
     } while (0)
 
-// Host callback after a slot's launch: every request of the launch is done.
-void CUDART_CB on_launch_done(void* user) {
-    Slot* slot = static_cast<Slot*>(user);
+// Marks the requests of a launch done with one status and queues them for cp3_server_poll.
+void finish_requests(cp3_server* s, const std::vector<std::shared_ptr<Request>>& reqs, int status) {
     const int64_t t = now_ns();
-    for (auto& r : slot->reqs) {
+    for (auto& r : reqs) {
         r->t_done = t;
+        r->status.store(status);
         r->state.store(kDone);
     }
-    slot->owner->completed += (long long)slot->reqs.size();
+    s->completed += (long long)reqs.size();
+    if (s->record_completions.load()) {
+        {
+            std::lock_guard<std::mutex> lk(s->cq_mu);
+            for (auto& r : reqs) s->completions.push_back(r->id);
+        }
+        s->cq_cv.notify_all();
+    }
+}
+
+// Host callback after a slot's launch: every request of the launch is done, with the status
+// word the launch's graph copied into page-locked memory before this callback (stream order).
+// It takes no lock of the scheduler's: the scheduler may hold cp3_server::mu while it waits.
+void CUDART_CB on_launch_done(void* user) {
+    Slot* slot = static_cast<Slot*>(user);
+    finish_requests(slot->owner, slot->reqs, *slot->h_status.ptr);
     slot->finished.store(1);
     slot->owner->cv.notify_all();
+}
+
+const char* status_text(int st) {
+    return st == kStatusBounds      ? "batch kernel: a device bounds check failed (CP3_DEVICE_CHECKS build)"
+           : st == kStatusWaitLimit ? "batch kernel reported a wait time-out"
+           : st == kStatusKind      ? "batch kernel: a tile of a kind the launch was not built for"
+                                    : "the launch of this request failed";
 }
 
 // Packs queued requests into one launch on `slot`; caller holds s->mu.  Order: requests
 // older than the aging limit first (arrival order), then the rest smallest-first, so small
 // requests are not stuck behind large ones and large ones cannot starve.  A request is
 // admitted only if its table and result fit in the pool (admission by device memory).
+// Requests of one grid have one size, so when a grid's oldest request does not fit (pool or
+// the launch's bin cap), none of that grid's does, and the grid is passed over.
 void launch_slot(cp3_server* s, Slot& slot) {
     TraceRange trace("serve_launch");
     slot.reqs.clear();
     const int64_t now = now_ns();
-    std::vector<std::shared_ptr<Request>> q(s->incoming.begin(), s->incoming.end());
-    std::stable_sort(q.begin(), q.end(), [&](const std::shared_ptr<Request>& a, const std::shared_ptr<Request>& b) {
-        const bool oa = now - a->t_submit > s->aging_ns, ob = now - b->t_submit > s->aging_ns;
-        if (oa != ob) return oa;
-        if (oa) return a->t_submit < b->t_submit;
-        return s->tmpls[a->tmpl].bins < s->tmpls[b->tmpl].bins;
-    });
+    const int ng = (int)s->queues.size();
+    std::vector<char> blocked(ng, 0);
     long long bins = 0;
-    std::vector<char> taken(q.size(), 0);
-    for (size_t i = 0; i < q.size() && (int)slot.reqs.size() < s->max_batch; i++) {
-        Request& r = *q[i];
-        const Template& T = s->tmpls[r.tmpl];
-        if (!slot.reqs.empty() && bins + T.bins > s->max_bins) continue;
+    auto admit = [&](int g) {  // the head of grid g's FIFO, if it fits
+        const Template& T = s->tmpls[g];
+        if (!slot.reqs.empty() && bins + T.bins > s->max_bins) return false;
         const size_t units = (T.tab_floats + T.out_floats) / kUnit;
         size_t off = 0;
-        if (!s->pool.alloc(units, &off)) continue;  // waits for releases
-        r.pool_off = off;
-        r.pool_units = units;
+        if (!s->pool.alloc(units, &off)) return false;  // waits for releases
+        std::shared_ptr<Request> r = std::move(s->queues[g].front());
+        s->queues[g].pop_front();
+        s->queued--;
+        r->pool_off = off;
+        r->pool_units = units;
         bins += T.bins;
-        slot.reqs.push_back(q[i]);
-        taken[i] = 1;
+        slot.reqs.push_back(std::move(r));
+        return true;
+    };
+    // aged requests, oldest first across the grids' heads
+    while ((int)slot.reqs.size() < s->max_batch) {
+        int g_old = -1;
+        for (int g = 0; g < ng; g++)
+            if (!blocked[g] && !s->queues[g].empty() &&
+                (g_old < 0 || s->queues[g].front()->t_submit < s->queues[g_old].front()->t_submit))
+                g_old = g;
+        if (g_old < 0 || now - s->queues[g_old].front()->t_submit <= s->aging_ns) break;
+        if (!admit(g_old)) blocked[g_old] = 1;
     }
+    // then smallest grids first, each in arrival order
+    for (int g : s->by_size)
+        while (!blocked[g] && !s->queues[g].empty() && (int)slot.reqs.size() < s->max_batch)
+            if (!admit(g)) blocked[g] = 1;
     if (slot.reqs.empty()) return;
-    std::deque<std::shared_ptr<Request>> rest;
-    for (size_t i = 0; i < q.size(); i++)
-        if (!taken[i]) rest.push_back(q[i]);
-    std::stable_sort(rest.begin(), rest.end(), [](const std::shared_ptr<Request>& a, const std::shared_ptr<Request>& b) {
-        return a->t_submit < b->t_submit;
-    });
-    s->incoming.swap(rest);
     const int n = (int)slot.reqs.size();
     long long a = 0, b = 0;
     slot.h_a.ptr[0] = slot.h_b.ptr[0] = 0;
@@ -295,18 +346,45 @@ void launch_slot(cp3_server* s, Slot& slot) {
     }
     *slot.h_hdr.ptr = Header{n, kServeRows, kServeBeamChunk, (int)a, (int)b};
     cudaStream_t st = slot.stream;
-    cudaMemcpyAsync(slot.d_probs.ptr, slot.h_probs.ptr, sizeof(Problem) * n, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(slot.d_params.ptr, slot.h_params.ptr, sizeof(OscParams) * n, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(slot.d_a.ptr, slot.h_a.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(slot.d_b.ptr, slot.h_b.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(slot.d_hdr.ptr, slot.h_hdr.ptr, sizeof(Header), cudaMemcpyHostToDevice, st);
     bool has_atmos = false, has_beam = false;
     for (int i = 0; i < n; i++) (slot.h_probs.ptr[i].kind == 0 ? has_atmos : has_beam) = true;
-    cudaGraphLaunch(slot.graph[launch_kinds(has_atmos, has_beam)], st);
     slot.finished.store(0);
-    slot.busy = true;
-    cudaLaunchHostFunc(st, on_launch_done, &slot);
     s->launches++;
+    // Every call is checked.  A launch that fails before its host callback is queued fails
+    // its own requests here, after its stream has drained (so no kernel of it can still
+    // write into pool memory that a release hands to the next request).
+    cudaError_t e = cudaSuccess;
+    const char* what = "";
+    bool graph_queued = false;
+    if (s->debug_fail_launches > 0) {
+        s->debug_fail_launches--;
+        e = cudaErrorLaunchFailure;
+        what = "injected launch failure (cp3_server_debug_fail_launches)";
+    }
+#define SERVE_STEP(call, name)        \
+    if (e == cudaSuccess) {           \
+        e = (call);                   \
+        if (e != cudaSuccess) what = name; \
+    }
+    SERVE_STEP(cudaMemcpyAsync(slot.d_probs.ptr, slot.h_probs.ptr, sizeof(Problem) * n, cudaMemcpyHostToDevice, st), "upload problems")
+    SERVE_STEP(cudaMemcpyAsync(slot.d_params.ptr, slot.h_params.ptr, sizeof(OscParams) * n, cudaMemcpyHostToDevice, st), "upload parameters")
+    SERVE_STEP(cudaMemcpyAsync(slot.d_a.ptr, slot.h_a.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st), "upload tile offsets")
+    SERVE_STEP(cudaMemcpyAsync(slot.d_b.ptr, slot.h_b.ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st), "upload tile offsets")
+    SERVE_STEP(cudaMemcpyAsync(slot.d_hdr.ptr, slot.h_hdr.ptr, sizeof(Header), cudaMemcpyHostToDevice, st), "upload header")
+    SERVE_STEP(cudaGraphLaunch(slot.graph[launch_kinds(has_atmos, has_beam)], st), "graph launch")
+    graph_queued = e == cudaSuccess;
+    SERVE_STEP(cudaLaunchHostFunc(st, on_launch_done, &slot), "completion callback")
+#undef SERVE_STEP
+    if (e == cudaSuccess) {
+        slot.busy = true;
+        return;
+    }
+    cudaGetLastError();
+    if (graph_queued) cudaStreamSynchronize(st);
+    s->launch_error = std::string("serve launch: ") + what + ": " + cudaGetErrorString(e);
+    finish_requests(s, slot.reqs, kReqLaunchFailed);
+    slot.reqs.clear();
+    s->cv.notify_all();
 }
 
 void scheduler(cp3_server* s) {
@@ -314,17 +392,14 @@ void scheduler(cp3_server* s) {
     std::unique_lock<std::mutex> lk(s->mu);
     while (!s->stop.load()) {
         for (Slot& sl : s->slots) {
-            if (sl.busy && sl.finished.load()) {
-                int st = 0;
-                cudaMemcpy(&st, sl.d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost);
-                if (st) s->kernel_status.store(st);
+            if (sl.busy && sl.finished.load()) {  // the callback has set every request's status
                 sl.busy = false;
                 sl.reqs.clear();
             }
         }
         bool launched = false;
         for (Slot& sl : s->slots)
-            if (!sl.busy && !s->incoming.empty()) {
+            if (!sl.busy && s->queued > 0) {
                 launch_slot(s, sl);
                 launched = launched || sl.busy;
             }
@@ -352,7 +427,8 @@ int capture_slot(cp3_server* s, Slot& sl) {
     S_CUDA(s, sl.h_b.alloc(cap + 1), "pinned");
     S_CUDA(s, sl.h_hdr.alloc(1), "pinned");
     S_CUDA(s, sl.h_params.alloc(cap), "pinned");
-    S_CUDA(s, cudaMemset(sl.d_status.ptr, 0, sizeof(int)), "memset");
+    S_CUDA(s, sl.h_status.alloc(1), "pinned");
+    *sl.h_status.ptr = 0;
     Args args{sl.d_hdr.ptr, sl.d_probs.ptr, sl.d_a.ptr, sl.d_b.ptr, sl.d_params.ptr,
               s->d_energies.ptr, s->d_row_off.ptr, s->d_seg_len.ptr,
               s->d_cls_rho.ptr, s->d_baselines.ptr, s->d_pool.ptr, s->d_pool.ptr,
@@ -363,7 +439,8 @@ int capture_slot(cp3_server* s, Slot& sl) {
     // With atmospheric requests it is a table launch, then a bin launch that reads the
     // finished tables (no wait); a beam-only launch is the single kernel.  The table launch
     // has a full grid: the number of table tiles changes from launch to launch, and warps
-    // without a tile return at once.
+    // without a tile return at once.  Each graph clears the status word first and copies it
+    // to the slot's page-locked word last, where the completion callback reads it.
     for (int kinds = 1; kinds <= 3; kinds++) {
         using Kern = void (*)(Args);
         const bool split = kServeSplitTables && (kinds & kAtmos);
@@ -382,6 +459,7 @@ int capture_slot(cp3_server* s, Slot& sl) {
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_counter.ptr, 0, 2 * sizeof(unsigned int), cs);
         if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_done.ptr, 0, sizeof(int) * cap, cs);
+        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_status.ptr, 0, sizeof(int), cs);
         if (e == cudaSuccess && split) {
             tab<<<grid_tab, kBlock, 0, cs>>>(args);
             e = cudaGetLastError();
@@ -390,6 +468,8 @@ int capture_slot(cp3_server* s, Slot& sl) {
             kern<<<grid, kBlock, 0, cs>>>(args);
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(sl.h_status.ptr, sl.d_status.ptr, sizeof(int), cudaMemcpyDeviceToHost, cs);
         const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
         if (e == cudaSuccess) e = e2;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.graph[kinds], g, 0);
@@ -549,6 +629,11 @@ int cp3_server_start(cp3_server* s) {
             return sfail(s, CP3_ERR_BAD_SIZE, "a registered grid does not fit in the pool");
     for (Slot& sl : s->slots)
         if (int rc = capture_slot(s, sl)) return rc;
+    s->queues.assign(s->tmpls.size(), {});
+    s->by_size.resize(s->tmpls.size());
+    for (size_t g = 0; g < s->tmpls.size(); g++) s->by_size[g] = (int)g;
+    std::stable_sort(s->by_size.begin(), s->by_size.end(),
+                     [&](int a, int b) { return s->tmpls[a].bins < s->tmpls[b].bins; });
     s->started = true;
     s->loop = std::thread(scheduler, s);
     return CP3_OK;
@@ -578,7 +663,8 @@ int cp3_server_submit(cp3_server* s, int grid, double t12, double t13, double t2
         r->id = s->next_id++;
         r->t_submit = now_ns();
         s->requests[r->id] = r;
-        s->incoming.push_back(r);
+        s->queues[grid].push_back(r);
+        s->queued++;
     }
     s->cv.notify_all();
     if (id) *id = r->id;
@@ -596,12 +682,12 @@ int cp3_server_wait(cp3_server* s, unsigned long long id, double timeout_s, int*
     // short timed waits: the completion callback notifies without taking the mutex
     while (r->state.load() != kDone && Clock::now() < deadline)
         s->cv.wait_for(lk, std::chrono::microseconds(100));
-    if (done) *done = r->state.load() == kDone ? 1 : 0;
-    if (const int st = s->kernel_status.load())
-        return sfail(s, CP3_ERR_CUDA,
-                     st == kStatusBounds ? "batch kernel: a device bounds check failed (CP3_DEVICE_CHECKS build)"
-                     : st == kStatusWaitLimit ? "batch kernel reported a wait time-out"
-                                              : "batch kernel: a tile of a kind the launch was not built for");
+    const bool finished = r->state.load() == kDone;
+    if (done) *done = finished ? 1 : 0;
+    if (finished) {
+        if (const int st = r->status.load())
+            return sfail(s, CP3_ERR_CUDA, st == kReqLaunchFailed ? s->launch_error : std::string(status_text(st)));
+    }
     return CP3_OK;
 }
 
@@ -613,6 +699,9 @@ int cp3_server_result(cp3_server* s, unsigned long long id, const float** ptr, s
     if (it == s->requests.end()) return sfail(s, CP3_ERR_INDEX, "no such request");
     const Request& r = *it->second;
     if (r.state.load() != kDone) return sfail(s, CP3_ERR_NOT_SET, "request not done");
+    if (const int st = r.status.load())
+        return sfail(s, CP3_ERR_CUDA, std::string("no result: ") +
+                                          (st == kReqLaunchFailed ? s->launch_error : std::string(status_text(st))));
     const Template& T = s->tmpls[r.tmpl];
     if (ptr) *ptr = s->d_pool.ptr + r.pool_off * kUnit + T.tab_floats;
     if (count) *count = (size_t)9 * T.nrows * T.ne;
@@ -644,12 +733,39 @@ int cp3_server_release(cp3_server* s, unsigned long long id) {
     return CP3_OK;
 }
 
+int cp3_server_poll(cp3_server* s, unsigned long long* ids, int max_ids, double timeout_s, int* n) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (!n || max_ids < 0 || (max_ids > 0 && !ids)) return sfail(s, CP3_ERR_BAD_ARGUMENT, "poll: null output or negative size");
+    *n = 0;
+    s->record_completions.store(true);
+    if (max_ids == 0) return CP3_OK;
+    std::unique_lock<std::mutex> lk(s->cq_mu);
+    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                             std::chrono::duration<double>(std::max(timeout_s, 0.0)));
+    // timed waits: finish_requests notifies after dropping cq_mu
+    while (s->completions.empty() && Clock::now() < deadline)
+        s->cq_cv.wait_until(lk, std::min(deadline, Clock::now() + std::chrono::microseconds(200)));
+    while (*n < max_ids && !s->completions.empty()) {
+        ids[(*n)++] = s->completions.front();
+        s->completions.pop_front();
+    }
+    return CP3_OK;
+}
+
+int cp3_server_debug_fail_launches(cp3_server* s, int count) {
+    if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
+    if (count < 0) return sfail(s, CP3_ERR_BAD_ARGUMENT, "count must be >= 0");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->debug_fail_launches = count;
+    return CP3_OK;
+}
+
 int cp3_server_stats(cp3_server* s, long long* launches, long long* completed, long long* queued) {
     if (!s) return sfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null server");
     std::lock_guard<std::mutex> lk(s->mu);
     if (launches) *launches = s->launches.load();
     if (completed) *completed = s->completed.load();
-    if (queued) *queued = (long long)s->incoming.size();
+    if (queued) *queued = s->queued;
     return CP3_OK;
 }
 

@@ -7,6 +7,7 @@
 // bits where the eigen-system is ill-conditioned.  The table work is O(classes x energies),
 // amortised over every cosine, so the missing contraction costs nothing that matters.
 #include "cp3_device.cuh"
+#include "cp3_f64.cuh"
 #include "cp3_mixed.cuh"
 #include "cp3_kernels.hpp"
 
@@ -57,18 +58,30 @@ __global__ void __launch_bounds__(kTableBlock)
 }
 
 // physics::calculate_beam (physics.hpp:1153-1260), one thread per energy; result [9][ne].
+// The FP64 atmospheric kernels' algebra with one segment: the reference's matter masses
+// (getMfast, in this unit's uncontracted arithmetic), the rotated-basis unit eigenvectors,
+// the reference's phases -2.534 dmMatVac[k][0] L / E (getA, physics.hpp:547-551) as relative
+// phases, S = 1 + z1 u1 u1^T + z2 u2 u2^T and A = W S W^+.  The reference instead sums
+// e^{i arg_k} times its spectral products (get_product: 18 divisions) and rotates them with
+// AXFAC (getA); the two agree to rounding.
 __global__ void __launch_bounds__(kTableBlock)
     beam_f64_kernel(const __grid_constant__ OscParams p, const double* __restrict__ energies,
                     int ne, double rho_e, double L, double* __restrict__ out) {
     const int ie = blockIdx.x * kTableBlock + threadIdx.x;
     if (ie >= ne) return;
-    cd A[3][3];
-    beam_amplitude_f64(&p, energies[ie], rho_e, L, A);
+    const double E = energies[ie];
+    Layer64 f;
+    double dmv[3], arg[3];
+    rotated_layer_f64(&p, E, rho_e, f.u, dmv);
+    layer64_phases(dmv, L, E, 1.0 / E, f, arg);
+    cm3 A2, A;
+    layer_to_gen64(f, A2);
+    to_flavour64(A2, p.w, A);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++)
-            out[(size_t)(i * 3 + j) * ne + ie] = A[j][i].re * A[j][i].re + A[j][i].im * A[j][i].im;
+            out[(size_t)(i * 3 + j) * ne + ie] = A.a[j][i].re * A.a[j][i].re + A.a[j][i].im * A.a[j][i].im;
 }
 
 }  // namespace
@@ -98,6 +111,11 @@ cudaError_t launch_table_mixed(const OscParams& p, const double* energies, int n
 cudaError_t launch_table_mixed(const OscParams& p, const float2* energies, int ne,
                                const float2* cls_rho, int ncls, float* table, cudaStream_t s) {
     return table_mixed(p, energies, ne, cls_rho, ncls, table, s);
+}
+
+cudaError_t preload_table_mixed() {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, table_mixed_kernel<double>);
 }
 
 cudaError_t launch_beam_f64(const OscParams& p, const double* energies, int ne, double rho_e,

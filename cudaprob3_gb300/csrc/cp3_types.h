@@ -19,10 +19,11 @@ constexpr int kMaxSegments = kMaxShells + 1;  // air segment + crossed shells
 // One oscillation-parameter set for one neutrino type, as the kernels read it.
 // Built on the host from the user's angles and splittings (cp3_host.cpp).
 struct alignas(16) OscParams {
-    // Reference-faithful data (FP64 kernels): Propagator::Mix_U, DM, mass order, AXFAC.
+    // Reference-faithful data (FP64 kernels): Propagator::Mix_U, DM, mass order.  (The
+    // reference's AXFAC bilinears of U serve only its getA, which the rotated-basis beam
+    // kernels replace.)
     double U[18];        // U(i,j) re/im at [(i*3+j)*2 + {0,1}]
     double dm[9];        // DM(i,j) = m_i^2 - m_j^2 with the degeneracy break
-    double axfac[324];   // AXFAC(n,m,i,j,e) at [(((n*3+m)*3+i)*3+j)*4+e]
     // Rotated real basis of the mixed kernels: U = W . O . diag(1,1,e^{-i d}) with
     // W = R23 . diag(1,1,e^{i d}) and O = R13 . R12 real, so 2E.H = W (H0 + V e0 e0^T) W^+.
     double h0[6];        // H0 = O . diag(DM(k,0)) . O^T : 00,01,02,11,12,22 (eV^2)

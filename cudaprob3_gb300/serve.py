@@ -103,6 +103,25 @@ class Server:
     def release(self, rid: int):
         self._check(self._lib.cp3_server_release(self._h, C.c_ulonglong(rid)))
 
+    def poll(self, max_ids: int = 4096, timeout_s: float = 0.0):
+        """Ids of requests finished since the previous poll, in completion order (waits up to
+        timeout_s while there is none).  Call once before the first submit: recording starts
+        with the first poll."""
+        n = C.c_int()
+        if max_ids <= 0:
+            self._check(self._lib.cp3_server_poll(self._h, None, 0, 0.0, C.byref(n)))
+            return []
+        buf = getattr(self, "_poll_buf", None)
+        if buf is None or len(buf) < max_ids:
+            buf = self._poll_buf = (C.c_ulonglong * max_ids)()
+        self._check(self._lib.cp3_server_poll(self._h, buf, int(max_ids), float(timeout_s),
+                                              C.byref(n)))
+        return list(buf[:n.value])
+
+    def debug_fail_launches(self, count: int):
+        """Testing aid: the next ``count`` launches fail on the host before any GPU work."""
+        self._check(self._lib.cp3_server_debug_fail_launches(self._h, int(count)))
+
     def stats(self):
         a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
         self._check(self._lib.cp3_server_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))

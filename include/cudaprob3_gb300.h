@@ -306,10 +306,14 @@ int cp3_server_start(cp3_server* s);
 int cp3_server_submit(cp3_server* s, int grid, double theta12, double theta13, double theta23,
                       double dcp, int knutype, double dm12sq, double dm23sq, int neutrino_type,
                       unsigned long long* id);
-/* Blocks up to timeout_s; *done = 1 when the request's result is ready. */
+/* Blocks up to timeout_s; *done = 1 when the request has finished.  A request whose launch
+ * failed (a CUDA call of the launch, or the kernel's status word) finishes with *done = 1 and
+ * CP3_ERR_CUDA, the reason in cp3_server_last_error; requests of other launches are not
+ * affected. */
 int cp3_server_wait(cp3_server* s, unsigned long long id, double timeout_s, int* done);
 /* Device pointer / float count of a finished request's result (layout as for batches) and its
- * latency (submit to completion of its launch, ms). */
+ * latency (submit to completion of its launch, ms).  Refused (CP3_ERR_CUDA) for a request
+ * that finished with an error. */
 int cp3_server_result(cp3_server* s, unsigned long long id, const float** ptr, size_t* count,
                       double* latency_ms);
 /* Synchronous copy of a finished request's result to host memory (count floats). */
@@ -317,11 +321,23 @@ int cp3_server_copy_result(cp3_server* s, unsigned long long id, void* dst);
 int cp3_server_release(cp3_server* s, unsigned long long id);
 int cp3_server_stats(cp3_server* s, long long* launches, long long* completed,
                      long long* queued);
+/* Completion queue for a client that multiplexes many requests from one thread (an MCMC
+ * driver running many chains): writes to ids up to max_ids ids of requests that finished,
+ * with or without error, since the previous poll, in completion order, and their number to
+ * *n; blocks up to timeout_s while there is none.  Recording starts with the first call
+ * (max_ids = 0 only starts it), so a client calls it once before its first submit. */
+int cp3_server_poll(cp3_server* s, unsigned long long* ids, int max_ids, double timeout_s,
+                    int* n);
+/* Testing aid: the next `count` launches fail on the host before any of their GPU work, as a
+ * launch whose CUDA calls fail does.  Their requests, and only theirs, finish with
+ * CP3_ERR_CUDA. */
+int cp3_server_debug_fail_launches(cp3_server* s, int count);
 
 /* ---- atmospheric propagation without allocation ------------------------------------------ */
 
-/* Size of the device scratch behind cp3_atmos_mixed_noalloc (reserved on every GPU that
- * loads the library, for the life of the process). */
+/* Size of the device scratch behind cp3_atmos_mixed_noalloc: one array per GPU the library
+ * is used on, placed when the library's module is loaded on that GPU (at the latest by the
+ * entry point's first call there), and held for the life of the process. */
 #define CP3_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
 
 /* No counterpart in the reference: an addition for callers that cannot allocate device
@@ -351,9 +367,14 @@ int cp3_server_stats(cp3_server* s, long long* launches, long long* completed,
  * Every call on a device shares the one scratch array, which keeps the last call's
  * contents; nothing in it has to start at zero (each call writes every element it reads).
  * Calls whose work overlaps on the GPU (other streams, or other host threads) race on that
- * array: order them on one stream or synchronise between them.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress, with that device
- * current); make that first call before any stream capture on the device. */
+ * array: order them on one stream or synchronise between them.
+ *
+ * The first call on each device is its set-up: with that device current it looks up the
+ * array's device address (cudaGetSymbolAddress) and loads the kernels the call launches.
+ * Under lazy module loading (the CUDA default) that is when the driver places the array and
+ * the kernels in device memory, so the first call may allocate; make it where allocation is
+ * still allowed, and before any stream capture on the device.  Later calls on that device
+ * allocate nothing. */
 int cp3_atmos_mixed_noalloc(int device, const double* d_energies, int n_energies,
                             const int* seg_offset, const double* seg_len_km,
                             const int* seg_class, int n_cosines, const double* class_rho_e,

@@ -175,11 +175,16 @@ private:
 // BeamCudaPropagatorSingle (beamcudapropagator.cuh:41-120).
 class BeamCudaPropagatorSingle : public Propagator<double> {
 public:
-    BeamCudaPropagatorSingle(int id, int n_energies_, int n_threads = 1, int precision = CP3_FP64) {
-        (void)n_threads;  // the reference's OpenMP thread count of its CPU base class
+    // The reference's two constructors (beamcudapropagator.cuh:52,57): (id, n_energies,
+    // n_threads) and (n_energies, n_threads), so a two-argument call means what it means
+    // there.  n_threads is the OpenMP thread count of the reference's CPU base class.
+    BeamCudaPropagatorSingle(int id, int n_energies_, int n_threads, int precision = CP3_FP64) {
+        (void)n_threads;
         detail::check(cp3_beam_create(id, n_energies_, precision, &h_), nullptr);
         n_energies = n_energies_;
     }
+    BeamCudaPropagatorSingle(int n_energies_, int n_threads)
+        : BeamCudaPropagatorSingle(0, n_energies_, n_threads) {}
     void setDensity(double rho) override { detail::check(cp3_set_beam_density(h_, rho), h_); }
     void setPathLength(double path_length) override {
         detail::check(cp3_set_beam_path_length(h_, path_length), h_);
@@ -328,6 +333,15 @@ public:
         return out;
     }
     void release(unsigned long long id) { check(cp3_server_release(s_, id)); }
+    // Ids finished since the previous poll, in completion order (waits up to timeout_s while
+    // there is none); call poll(0, 0.0) once before the first submit to start recording.
+    std::vector<unsigned long long> poll(int max_ids, double timeout_s) {
+        std::vector<unsigned long long> ids((size_t)(max_ids > 0 ? max_ids : 0));
+        int n = 0;
+        check(cp3_server_poll(s_, ids.data(), max_ids, timeout_s, &n));
+        ids.resize((size_t)n);
+        return ids;
+    }
     cp3_server* handle() { return s_; }
 
 private:

@@ -54,9 +54,17 @@ int main() {
     const int g = s.addAtmosphericGrid(cz, en);
     s.start();
     std::vector<unsigned long long> ids;
+    s.poll(0, 0.0);  // start recording completions
     for (int k = 0; k < 3; k++) ids.push_back(s.submit(g, t12, t13, t23, dcp, 1, dm12, dm23, Neutrino));
+    std::vector<unsigned long long> finished;
+    for (int tries = 0; finished.size() < ids.size() && tries < 600; tries++)
+        for (unsigned long long id : s.poll(8, 0.05)) finished.push_back(id);
+    if (finished.size() != ids.size()) {
+        std::printf("timeout\n");
+        return 1;
+    }
     for (unsigned long long id : ids) {
-        if (!s.wait(id, 30.0)) {
+        if (!s.wait(id, 0.0)) {
             std::printf("timeout\n");
             return 1;
         }

@@ -92,15 +92,27 @@ def test_mixed_averaging_against_oracle(oracle, shells):
         assert np.abs(got - ref).max() <= 1e-5
 
 
-def test_mixed_averaging_with_quadratic_density_is_refused():
-    p = AtmosCudaPropagatorSingle(0, 3, 2, precision="mixed")
-    p.setEnergyList([1.0, 2.0])
-    p.setCosineList([-0.5, 0.0, 0.5])
-    p.setMNSMatrix(0.5, 0.1, 0.7, 0.0, 1)
-    p.setNeutrinoMasses(7.5e-5, 2.5e-3)
-    p.setDensity(*earth.PREM_4LAYER_QUAD_V2)
-    p.setProductionHeight(20.0)
-    p.SetNumberOfProductionHeightBinsForAveraging(1)
-    p.setProductionHeightList(np.ones(2 * 3 * 2 * 3), [15.0, 25.0])
-    with pytest.raises(RuntimeError, match="FP64"):
-        p.calculateProbabilities(0)
+@pytest.mark.parametrize("scale", [1.0, 1.15])
+def test_mixed_averaging_with_quadratic_density_against_oracle(oracle, scale):
+    """Averaging and the quadratic density model together on the mixed kernels (the
+    reference runs them in one loop: physics.hpp:997-1067 with getDensityOfLayerPoly,
+    physics.hpp:651-739): per-segment eigen-solves, the air layer's eigencomponents and the
+    shift factors, against the oracle, both neutrino types, all nine channels, <= 1e-5.  The
+    quadratic PREM, and the same profile 15 % denser."""
+    from oracle.oracle import Mixing as OMix
+    rng = np.random.default_rng(5)
+    cz, en = np.linspace(-1, 1, 37), earth.log_energy_grid(31)
+    nb = 6
+    w = rng.uniform(0.1, 1.0, (2, 3, len(en), len(cz), nb))
+    w /= w.sum(axis=-1, keepdims=True)
+    edges = np.linspace(3.0, 50.0, nb + 1)
+    m = earth.gaussian_sets(2, seed=43)[1]
+    mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+    r, a, b, c, ye = earth.PREM_4LAYER_QUAD_V2
+    a, b, c = a * scale, b * scale, c * scale
+    for anti, knu in ((False, 1), (True, -1)):
+        ref = oracle.atmos(OMix(*mix6[:4], mix6[4], mix6[5], knu), anti, cz, en, r, None, ye, 20.0,
+                           poly_abc=(a, b, c), avg=(nb, w.ravel(), edges))
+        got = run_avg("mixed", mix6, knu, anti, cz, en, r, None, ye, 20.0, nb, w.ravel(), edges,
+                      (a, b, c))
+        assert np.abs(got - ref).max() <= 1e-5

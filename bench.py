@@ -46,10 +46,12 @@ NCU_TRAFFIC = {
     # the table launch and the bin launch of one run
     ("batch_atmos", "mixed"): (0.435456e6 + 0.033280e6 + 83.864320e6 + 902.968832e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
-    ("batch_beam", "mixed"): (107.312384e6 + 912.375040e6, 921.6e6,
+    ("batch_beam", "mixed"): (115.233280e6 + 911.497472e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
     ("atmos59", "fp64"): (9.935872e6 + 245.010688e6, 288.0e6,
                           "profiles/atmos_f64_kernel_59shells_2000x2000.md"),
+    # the 7.2 MB output is still in L2 when the captured launch ends
+    ("beam", "fp64"): (0.865792e6, 7.2e6, "profiles/beam_f64_kernel_1e5energies.md"),
 }
 
 
@@ -60,15 +62,20 @@ NCU_TRAFFIC = {
 NCU_PIPE = {
     ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7099),
     ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6699),  # the bin launch
-    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6852),
+    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6773),
     ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8926),
+    ("beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),
+    ("batch_beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),
 }
 
 
 def ncu_pipe(workload, prec):
     """{metric: fraction} of the committed capture, or {} if there is none."""
     t = NCU_PIPE.get((workload, prec))
-    return {"ncu_pipe_active": {t[0]: t[1], "source": NCU_TRAFFIC[(workload, prec)][2]}} if t else {}
+    if not t:
+        return {}
+    src = NCU_TRAFFIC.get((workload, prec), NCU_TRAFFIC.get((workload.replace("batch_", ""), prec)))
+    return {"ncu_pipe_active": {t[0]: t[1], "source": src[2] if src else None}}
 
 
 def ncu_traffic(workload, prec, result_bytes):
@@ -199,7 +206,10 @@ def run_batch(args, w, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     b, flops, nbins, params = build_batch(w)
     t0 = time.perf_counter()
-    b.tune(use_cache=True)
+    if args.shape:  # a fixed tile shape instead of the autotuner (profiling captures)
+        b.set_shape(*args.shape)
+    else:
+        b.tune(use_cache=True)
     tune_s = time.perf_counter() - t0
     for _ in range(args.warmup):
         b.run()
@@ -274,7 +284,10 @@ def run_batch(args, w, rank, world):
     except (OSError, KeyError, ValueError):
         pass
     if rank == 0:
-        line["max_abs_err_vs_oracle"] = check_batch_against_oracle(w, b)
+        err, per, what = check_batch_against_oracle(w, b)
+        line["max_abs_err_vs_oracle"] = err
+        line["max_abs_err_per_channel"] = dict(per, channels="a*3+b = P(a->b): e_e, e_m, e_t, "
+                                               "m_e, m_m, m_t, t_e, t_m, t_t", checked=what)
     line["clocks"] = clk.summary()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
@@ -288,7 +301,7 @@ def run_batch_fp64(args, w, rank, world):
     import torch
     from cudaprob3_gb300 import earth
     dev = int(os.environ.get("LOCAL_RANK", "0"))
-    props, flops, nbins = [], 0.0, 0
+    props, flops, nbins, jobs = [], 0.0, 0, []
     if w["model"] is not None:
         r = np.asarray(w["model"][0], dtype=np.float64)
         lim = -np.sqrt(1 - np.sort(r)[::-1] ** 2 / 6371.0 ** 2)
@@ -297,10 +310,11 @@ def run_batch_fp64(args, w, rank, world):
             cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
             M = (cz[:, None] < lim[None, :]).sum(axis=1)
             for knu in (1, -1):
-                p = make_propagator(dict(kind="atmos", cz=cz, en=en, model=w["model"], h=w["h"]),
-                                    "fp64")
+                wk = dict(kind="atmos", cz=cz, en=en, model=w["model"], h=w["h"])
+                p = make_propagator(wk, "fp64")
                 set_params(p, m, knu)
                 props.append((p, 0 if knu == 1 else 1))
+                jobs.append((p, wk, m, knu))
                 flops += float(f_bin(M).sum()) * ne
                 nbins += nc * ne
     else:
@@ -310,9 +324,11 @@ def run_batch_fp64(args, w, rank, world):
         for m in w["sets"][:512]:
             for knu in (1, -1):
                 for L in bw["L"]:
-                    p = make_propagator(dict(kind="beam", en=bw["en"], rho=bw["rho"], L=L), "fp64")
+                    wk = dict(kind="beam", en=bw["en"], rho=bw["rho"], L=L)
+                    p = make_propagator(wk, "fp64")
                     set_params(p, m, knu)
                     props.append((p, 0 if knu == 1 else 1))
+                    jobs.append((p, wk, m, knu))
                     flops += float(f_bin(0)) * len(bw["en"])
                     nbins += len(bw["en"])
     stream = torch.cuda.Stream()
@@ -336,6 +352,17 @@ def run_batch_fp64(args, w, rank, world):
     t_ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, "cuda")
     probs = 9 * nbins
     peaks = fma_peaks(dev)
+    # parity of the FP64 kernels on this batch: 8 handles spread over it, every bin
+    from oracle.oracle import Mixing as OMix, Oracle
+    orc, err = Oracle(), 0.0
+    for p, wk, m, knu in [jobs[(i * (len(jobs) - 1)) // 7] for i in range(8)] if rank == 0 else []:
+        om = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
+        if wk["kind"] == "atmos":
+            ref = orc.atmos(om, knu < 0, wk["cz"], wk["en"], *wk["model"], wk["h"],
+                            nthreads=os.cpu_count() or 1)
+        else:
+            ref = orc.beam(om, knu < 0, wk["en"], wk["rho"], wk["L"], nthreads=os.cpu_count() or 1)
+        err = max(err, float(np.abs(p.probabilities() - ref).max()))
     return {
         "metric": "oscillation probabilities/s, plain FP64 kernels (reference tolerance 1e-12)",
         "value": world * probs / (t_ms * 1e-3), "unit": "probabilities/s", "n_gpus": world,
@@ -350,20 +377,27 @@ def run_batch_fp64(args, w, rank, world):
         "roofline": {"bound": "fp64", "achieved": round(flops / (t_ms * 1e-3) / 1e12, 3),
                      "peak": round(peaks["fp64"], 3), "unit": "TFLOP/s",
                      "frac": round(flops / (t_ms * 1e-3) / 1e12 / peaks["fp64"], 4),
-                     "traffic": None, "flops_per_launch": flops},
+                     "traffic": None, "flops_per_launch": flops,
+                     **ncu_pipe(args.workload, "fp64")},
         "peaks_tflops": peaks,
+        "max_abs_err_vs_oracle": err if rank == 0 else None,
+        "checked": "8 of the FP64 handles spread over the batch, every bin",
         "clocks": clk.summary(),
     }
 
 
-def check_batch_against_oracle(w, b, n_check=4):
-    """A few problems of the timed batch against the CPU oracle."""
+def check_batch_against_oracle(w, b, n_check=12):
+    """Problems of the timed batch against the CPU oracle: n_check parameter sets spread over
+    the batch (both mass orderings), each with nu and nubar, every bin of their grids.
+    Returns (max error, per-channel max errors for nu and nubar, what was checked)."""
     from cudaprob3_gb300 import earth
     from oracle.oracle import Mixing as OMix, Oracle
     orc = Oracle()
-    errs = []
-    for i in range(n_check):
-        k = (i * 37) % len(w["sets"])
+    nt = os.cpu_count() or 1
+    n_sets = len(w["sets"])
+    picks = sorted({(i * (n_sets - 1)) // max(n_check - 1, 1) for i in range(n_check)})
+    per = {"nu": np.zeros(9), "nubar": np.zeros(9)}
+    for k in picks:
         m = w["sets"][k]
         for anti in (False, True):
             pid = 2 * k + int(anti)
@@ -372,15 +406,19 @@ def check_batch_against_oracle(w, b, n_check=4):
             if w["model"] is not None:
                 nc, ne = w["grids"][k]
                 cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
-                rows = np.arange(0, nc, max(1, nc // 40))
-                ref = orc.atmos(om, anti, cz[rows], en, *w["model"], w["h"], nthreads=os.cpu_count() or 1)
-                errs.append(float(np.abs(np.transpose(got, (1, 2, 0))[rows] - ref).max()))
+                ref = orc.atmos(om, anti, cz, en, *w["model"], w["h"], nthreads=nt)
+                err = np.abs(np.transpose(got, (1, 2, 0)) - ref).reshape(-1, 9).max(axis=0)
             else:
                 bw = w["beam"]
+                err = np.zeros(9)
                 for j, L in enumerate(bw["L"]):
-                    ref = orc.beam(om, anti, bw["en"], bw["rho"], L, nthreads=os.cpu_count() or 1)
-                    errs.append(float(np.abs(got[j].T - ref).max()))
-    return max(errs)
+                    ref = orc.beam(om, anti, bw["en"], bw["rho"], L, nthreads=nt)
+                    err = np.maximum(err, np.abs(got[j].T - ref).max(axis=0))
+            key = "nubar" if anti else "nu"
+            per[key] = np.maximum(per[key], err)
+    what = (f"{len(picks)} of {n_sets} parameter sets spread over the batch (both orderings), "
+            "nu and nubar, every bin of their grids")
+    return float(max(per["nu"].max(), per["nubar"].max())), {k: v.tolist() for k, v in per.items()}, what
 
 
 def shells_crossed(w):
@@ -1228,6 +1266,10 @@ def main():
                     help="leave out the reference's own FP64 CUDA propagator")
     ap.add_argument("--batch-sets", type=int, default=0,
                     help="parameter sets of the batched workloads (default: the configuration's)")
+    ap.add_argument("--shape", type=int, nargs=3, default=None,
+                    metavar=("ROWS_PER_TILE", "BLOCKS_PER_SM", "BEAM_CHUNK"),
+                    help="batched workloads: this tile shape instead of the autotuner's "
+                         "(so that a profiler captures the launch it is asked for)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     global BATCH_SETS

@@ -44,7 +44,7 @@ NCU_TRAFFIC = {
     ("atmos59", "mixed"): (5.910016e6 + 84.903680e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
     # the table launch and the bin launch of one run
-    ("batch_atmos", "mixed"): (0.435456e6 + 0.033280e6 + 83.864320e6 + 902.968832e6, 912.332288e6,
+    ("batch_atmos", "mixed"): (0.436992e6 + 0.060416e6 + 204.449536e6 + 978.470912e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
     ("batch_beam", "mixed"): (115.233280e6 + 911.497472e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
@@ -61,7 +61,7 @@ NCU_TRAFFIC = {
 # 1); this is the utilisation of what they do execute.
 NCU_PIPE = {
     ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7099),
-    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6699),  # the bin launch
+    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6568),  # the bin launch
     ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6773),
     ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8926),
     ("beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),

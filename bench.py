@@ -289,6 +289,11 @@ def run_batch(args, w, rank, world):
         line["max_abs_err_per_channel"] = dict(per, channels="a*3+b = P(a->b): e_e, e_m, e_t, "
                                                "m_e, m_m, m_t, t_e, t_m, t_t", checked=what)
     line["clocks"] = clk.summary()
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        b.close()
+        line["reference_fp64_gpu"] = reference_gpu_batch(w)
+        if "value" in line["reference_fp64_gpu"]:
+            line["mixed_over_reference_fp64_gpu"] = round(line["value"] / line["reference_fp64_gpu"]["value"], 1)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, seconds=args.cpu_seconds)
     return line
@@ -905,6 +910,92 @@ def reference_gpu(w, m, steps, refs, sample_every=40, timeout=600):
         out["max_abs_err_vs_oracle"] = max(errs)
         out["checked"] = (f"every {sample_every}th cosine row" if w["kind"] == "atmos"
                           else "every energy")
+    return out
+
+
+def reference_gpu_batch(w, n_sets=16, steps=3, sample_every=40, timeout=900):
+    """The reference's own FP64 CUDA propagators on the first n_sets parameter sets of a batched
+    workload, as a caller without batching runs them: one propagator per problem (created
+    before the timed region), calculateProbabilities on each in turn, in a child process.
+    Every sample_every-th cosine row (atmospheric) or energy (beam) of every problem is read
+    back through getProbability and checked against the oracle."""
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix, Oracle, Reference
+    exe = Reference.GPU_BENCH
+    if not os.path.exists(exe):
+        return {"unavailable": "no reference source tree here (CP3_REFERENCE_DIR or "
+                               "baseline/_ref), so the reference's CUDA propagator was not built"}
+    fl = lambda xs: " ".join(repr(float(x)) for x in xs)  # noqa: E731
+    probs = []  # (kind, set, anti, grid or (en, L))
+    with tempfile.TemporaryDirectory() as d:
+        inp, outb = os.path.join(d, "in.txt"), os.path.join(d, "sample.bin")
+        with open(inp, "w") as f:
+            f.write(f"kind batch\nsteps {steps}\nwarmup 1\nsample_every {sample_every}\n")
+            if w["model"] is not None:
+                r, rho, ye = w["model"]
+                f.write(f"height_km {w['h']!r}\nmodel {len(r)}\n" + "".join(
+                    f"{a!r} {b!r} {c!r}\n" for a, b, c in zip(map(float, r), map(float, rho), map(float, ye))))
+            for k in range(min(n_sets, len(w["sets"]))):
+                m = w["sets"][k]
+                par = "%r %r %r %r %r %r" % (m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq)
+                for anti in (0, 1):
+                    if w["model"] is not None:
+                        nc, ne = w["grids"][k]
+                        cz, en = earth.cosine_grid(nc), earth.log_energy_grid(ne)
+                        f.write(f"problem atmos {par} {anti} cosines {nc} {fl(cz)} energies {ne} {fl(en)}\n")
+                        probs.append(("atmos", m, anti, (cz, en)))
+                    else:
+                        bw = w["beam"]
+                        for L in bw["L"]:
+                            f.write(f"problem beam {par} {anti} rho {bw['rho']!r} length_km {float(L)!r} "
+                                    f"energies {len(bw['en'])} {fl(bw['en'])}\n")
+                            probs.append(("beam", m, anti, (bw["en"], float(L))))
+        try:
+            r = subprocess.run([exe, inp, outb], capture_output=True, text=True, timeout=timeout)
+        except subprocess.TimeoutExpired:
+            return {"unavailable": f"the reference's CUDA propagator did not finish in {timeout} s"}
+        try:
+            res = json.loads(r.stdout.strip().splitlines()[-1])
+        except (ValueError, IndexError):
+            res = {}
+        if r.returncode != 0 or "ms_per_step" not in res:
+            return {"unavailable": f"the reference's CUDA propagator exited {r.returncode}: "
+                                   + (res.get("error") or (r.stdout + r.stderr).strip()[-300:])}
+        sample = np.fromfile(outb, dtype=np.float64)
+    step_ms = float(np.mean(res["ms_per_step"]))
+    out = {"value": 9 * res["bins"] / (step_ms * 1e-3), "unit": "probabilities/s",
+           "ms_per_step": step_ms, "steps": len(res["ms_per_step"]), "problems": res["problems"],
+           "device": res.get("device"),
+           "source": "the reference's AtmosCudaPropagatorSingle/BeamCudaPropagatorSingle (FP64), "
+                     "compiled from its own sources for sm_103a with MaxNLayers raised to 64; "
+                     "wall time of its synchronous calculateProbabilities",
+           "timing": f"the first {min(n_sets, len(w['sets']))} parameter sets, nu and nubar"
+                     + ("" if w["model"] is not None else ", both baselines")
+                     + ": one propagator per problem, called one after the other (the reference "
+                       "has no batching)"}
+    orc, err, pos = Oracle(), 0.0, 0
+    nt = os.cpu_count() or 1
+    for kind, m, anti, g in probs:
+        om = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, -1 if anti else 1)
+        if kind == "atmos":
+            cz, en = g
+            rows = cz[::sample_every]
+            n = len(rows) * len(en) * 9
+            ref = orc.atmos(om, bool(anti), rows, en, *w["model"], w["h"], nthreads=nt)
+            got = sample[pos:pos + n].reshape(len(rows), len(en), 9)
+        else:
+            en, L = g
+            es = en[::sample_every]
+            n = len(es) * 9
+            ref = orc.beam(om, bool(anti), es, w["beam"]["rho"], L, nthreads=nt)
+            got = sample[pos:pos + n].reshape(len(es), 9)
+        pos += n
+        if got.size == ref.size:
+            err = max(err, float(np.abs(got - ref).max()))
+    if pos == sample.size:
+        out["max_abs_err_vs_oracle"] = err
+        out["checked"] = (f"every {sample_every}th " + ("cosine row" if w["model"] is not None else "energy")
+                          + " of every problem run")
     return out
 
 

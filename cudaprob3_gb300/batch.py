@@ -36,6 +36,10 @@ class Batch:
             self._lib.cp3_batch_destroy(h)
             self._h = None
 
+    def close(self):
+        """Free the batch's device memory now (the handle is unusable afterwards)."""
+        self.__del__()
+
     def _check(self, rc):
         if rc:
             raise CP3Error(rc, self._lib.cp3_batch_last_error(self._h).decode())

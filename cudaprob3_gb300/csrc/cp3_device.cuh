@@ -447,7 +447,8 @@ __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restr
     const float mp3 = fmaxf(-pp * (1.0f / 3.0f), 1e-30f);
     // The starting roots need only ~1e-6 relative accuracy (the Newton steps below remove
     // what is left, as they remove __sincosf's), so the square root and the division take
-    // the fast forms: C3 1 %, the table kernel 4 % faster, every result's error unchanged.
+    // the fast forms: the batched beam (8192 problems x 1e5 energies) 1 %, the 59-shell
+    // 2000 x 2000 eigen table 4 % faster, every result's error unchanged.
     const float rt = mp3 * rsqrtf(mp3);
     // t = 2 sqrt(m) cos(a) solves t^3 + P t + Q = 0 when cos(3a) = -Q / (2 m^{3/2})
     const float carg = fminf(1.0f, fmaxf(-1.0f, __fdividef(-0.5f * qq, mp3 * rt)));
@@ -587,7 +588,7 @@ __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restr
             return false;
         }
         // projectors P_k = u u^T / |d|^2 (00,01,02,11,12,22), good to a few ulp: the beam's one
-        // layer per baseline needs no more (C3 max error 1.9e-6, against 1.1e-6 with the
+        // layer per baseline needs no more (batched-beam max error 1.9e-6, against 1.1e-6 with the
         // double-float Lagrange projectors, for 15 % less time)
         const float2 inv = make_float2(__fdividef(1.0f, n.x), __fdividef(1.0f, n.y));
         const float2 v0 = __fmul2_rn(u[0], inv), v1 = __fmul2_rn(u[1], inv), v2 = __fmul2_rn(u[2], inv);

@@ -70,7 +70,8 @@ def synthetic_shells(n_shells: int = 59, seed: int = 1234, jitter: float = 0.01)
     return radii, rho, ye
 
 
-# Parameters of the headline atmospheric configuration (also the C2/C3 Gaussian centre).
+# Parameters of the headline atmospheric configuration (also the centre of the Gaussian
+# parameter sets of the batched workloads).
 NOMINAL = Mixing(theta12=0.5843, theta13=0.1496, theta23=0.7365, dcp=-1.601,
                  dm12sq=7.53e-5, dm23sq=2.49e-3)
 PRODUCTION_HEIGHT_KM = 22.0

@@ -21,7 +21,7 @@ def test_oracle_matches_reference_fixture(oracle, path):
 
 
 def test_reference_probe_values(oracle):
-    """Values read off the reference during the survey (headline atmospheric grid)."""
+    """Values of the reference's own build on the headline atmospheric grid."""
     r, rho, ye = earth.PREM_4LAYER
     cz, en = earth.cosine_grid(400), earth.log_energy_grid(400)
     out = oracle.atmos(NOM, False, cz[[0, 100]], en[[0, 200]], r, rho, ye, 22.0)

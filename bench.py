@@ -1046,34 +1046,48 @@ def run_ours(args, rank, world):
 
     # end to end through the public API: grid H2D from pinned memory, compute, full D2H
     is_float = prec == "mixed"
-    host_out = [torch.empty(bytes_out_launch // (4 if is_float else 8),
-                            dtype=torch.float32 if is_float else torch.float64, pin_memory=True)
-                for _ in props]
+    # two page-locked result buffers per type, used in turn: a step's download may still be
+    # in flight while the host queues the next step
+    host_out = [[torch.empty(bytes_out_launch // (4 if is_float else 8),
+                             dtype=torch.float32 if is_float else torch.float64, pin_memory=True)
+                 for _ in range(2)] for _ in props]
     en_pinned = torch.from_numpy(np.asarray(w["en"], dtype=np.float64)).pin_memory()
     cz_pinned = (torch.from_numpy(np.asarray(w["cz"], dtype=np.float64)).pin_memory()
                  if w["kind"] == "atmos" else None)
 
     # neutrino and antineutrino on their own streams, each computed in row pieces whose
-    # downloads overlap the next piece's compute (cp3_calculate_to_host_async)
+    # downloads overlap the next piece's compute (cp3_calculate_to_host_async).  Steps are
+    # queued back to back, as a fitter pipelines consecutive evaluations: a step's setters
+    # and compute are queued while the previous step's download is still on the link (the
+    # handle orders its uploads, computes and copies on the device), and the timed region
+    # ends when the last step's results are in host memory.
     e2e_streams = [torch.cuda.Stream() for _ in props]
 
-    def e2e_step():
+    def e2e_step(k, wait):
         for t, p in enumerate(props):
             p.setEnergyList(en_pinned.numpy())
             if cz_pinned is not None:
                 p.setCosineList(cz_pinned.numpy())
             sp = e2e_streams[t].cuda_stream
-            p.calculate_to_host_async(t, host_out[t].data_ptr(), 0, sp)
-        for st in e2e_streams:
-            st.synchronize()
+            p.calculate_to_host_async(t, host_out[t][k % 2].data_ptr(), 0, sp)
+        if wait:
+            for st in e2e_streams:
+                st.synchronize()
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    for k in range(max(1, args.warmup)):
+        e2e_step(k, True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
+    for k in range(args.steps):
+        e2e_step(k, False)
+    for st in e2e_streams:
+        st.synchronize()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world, "cuda")
+    # the same steps with the host waiting for each step's results before the next
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_step(k, True)
+    e2e_ms_sync = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world, "cuda")
     # bytes that cross the link: the energy lists; an unchanged cosine list is recognised
     # on the host (one memcmp) and not uploaded again
     h2d = len(w["en"]) * 8 * len(props)
@@ -1128,7 +1142,9 @@ def run_ours(args, rank, world):
                    "l2": "256 MB buffer written between timed steps (untimed); per-step output "
                          f"{d2h / 1e6:.0f} MB exceeds L2"},
         "e2e": {"value": world * probs_step / (e2e_ms * 1e-3), "unit": "probabilities/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "steps_queued": "back to back, results in two page-locked buffers per type in turn",
+                "ms_per_step_waiting_each_step": e2e_ms_sync},
         "gpu_launches": args.steps * len(props) * (2 if w["kind"] == "atmos" else 1),
         "roofline": roofline,
         "peaks_tflops": peaks,

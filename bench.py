@@ -231,20 +231,29 @@ def run_batch(args, w, rank, world):
     largest = max(9 * npb for npb in problem_bins(w))
     host = torch.empty(largest, dtype=torch.float32, pin_memory=True)
 
-    def e2e_step():
+    # Steps are queued back to back (set_params waits only until the previous step's
+    # parameter upload has left the staging area); the timed region ends when the last
+    # step's results are in host memory.
+    def e2e_step(wait):
         for pid, m, anti in params:
             b.set_params(pid, m, anti)
         b.run()
         for pid, _, _ in params:
             b.copy_result_async(pid, host.data_ptr())
-        b.synchronize_stream()
+        if wait:
+            b.synchronize_stream()
 
     e2e_steps = min(args.steps, 3)
-    e2e_step()
+    e2e_step(True)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        e2e_step()
+        e2e_step(False)
+    b.synchronize_stream()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, world, "cuda")
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step(True)
+    e2e_ms_sync = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, world, "cuda")
     peaks = fma_peaks(dev)
     achieved = flops / (t_ms * 1e-3) / 1e12
     info = b.info()
@@ -264,7 +273,8 @@ def run_batch(args, w, rank, world):
         "e2e": {"value": world * probs / (e2e_ms * 1e-3), "unit": "probabilities/s",
                 "h2d_bytes_per_step": len(params) * b.parameter_bytes(),
                 "d2h_bytes_per_step": info["result_bytes"], "ms_per_step": e2e_ms,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "steps_queued": "back to back",
+                "ms_per_step_waiting_each_step": e2e_ms_sync},
         "gpu_launches": args.steps * launches,
         "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
                      "peak": round(peaks["fp32"], 3), "unit": "TFLOP/s",

@@ -226,10 +226,12 @@ def run_batch(args, w, rank, world):
     probs = 9 * nbins
 
     # end to end through the public API: every step uploads each problem's parameters
-    # (cp3_batch_set_params), runs, and downloads every result into page-locked host memory
-    # (one reused buffer of the largest result: the bytes cross the link all the same)
-    largest = max(9 * npb for npb in problem_bins(w))
-    host = torch.empty(largest, dtype=torch.float32, pin_memory=True)
+    # (cp3_batch_set_params), runs, and downloads the whole result arena into page-locked
+    # host memory in 256 MB pieces (cp3_batch_copy_results; one reused buffer: the bytes
+    # cross the link all the same)
+    arena = b.info()["result_bytes"] // 4
+    piece = 64 << 20  # floats
+    host = torch.empty(min(piece, arena), dtype=torch.float32, pin_memory=True)
 
     # Steps are queued back to back (set_params waits only until the previous step's
     # parameter upload has left the staging area); the timed region ends when the last
@@ -238,8 +240,8 @@ def run_batch(args, w, rank, world):
         for pid, m, anti in params:
             b.set_params(pid, m, anti)
         b.run()
-        for pid, _, _ in params:
-            b.copy_result_async(pid, host.data_ptr())
+        for first in range(0, arena, piece):
+            b.copy_results_async(first, min(piece, arena - first), host.data_ptr())
         if wait:
             b.synchronize_stream()
 

@@ -27,6 +27,7 @@ EXPORTS = (
     "cp3_batch_get_split_tables", "cp3_batch_debug_withhold_tables",
     "cp3_batch_tune", "cp3_batch_run",
     "cp3_batch_synchronize", "cp3_batch_result", "cp3_batch_copy_result", "cp3_batch_info",
+    "cp3_batch_result_offset", "cp3_batch_copy_results",
     "cp3_batch_parameter_bytes",
     "cp3_server_create", "cp3_server_destroy", "cp3_server_last_error", "cp3_server_set_earth",
     "cp3_server_add_atmos_grid", "cp3_server_add_beam_grid", "cp3_server_start",
@@ -92,6 +93,8 @@ _SIGS = {
     "cp3_batch_synchronize": ([_h, _dp], C.c_int),
     "cp3_batch_result": ([_h, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], C.c_int),
     "cp3_batch_copy_result": ([_h, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
+    "cp3_batch_result_offset": ([_h, C.c_int, C.POINTER(C.c_size_t)], C.c_int),
+    "cp3_batch_copy_results": ([_h, C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p], C.c_int),
     "cp3_batch_parameter_bytes": ([], C.c_size_t),
     "cp3_batch_info": ([_h, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_size_t),
                         C.POINTER(C.c_longlong)], C.c_int),

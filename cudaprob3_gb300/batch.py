@@ -128,6 +128,18 @@ class Batch:
         self._check(self._lib.cp3_batch_copy_result(self._h, int(pid), C.c_void_p(dst_ptr),
                                                     C.c_void_p(stream) if stream else None))
 
+    def result_offset(self, pid: int) -> int:
+        """Float offset of one problem's result in the batch's result arena."""
+        off = C.c_size_t()
+        self._check(self._lib.cp3_batch_result_offset(self._h, int(pid), C.byref(off)))
+        return off.value
+
+    def copy_results_async(self, first: int, count: int, dst_ptr: int, stream=None):
+        """Asynchronous copy of the result arena's floats [first, first + count) to dst."""
+        self._check(self._lib.cp3_batch_copy_results(self._h, int(first), int(count),
+                                                     C.c_void_p(dst_ptr),
+                                                     C.c_void_p(stream) if stream else None))
+
     def result(self, pid: int) -> np.ndarray:
         """Copy of one problem's result: atmospheric [9][nc][ne], beam [nL][9][ne]."""
         _, n = self.result_ptr(pid)

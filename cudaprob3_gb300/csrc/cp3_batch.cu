@@ -656,6 +656,28 @@ int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream) {
     return CP3_OK;
 }
 
+int cp3_batch_result_offset(const cp3_batch* b, int id, size_t* offset) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (!b->committed) return bfail(const_cast<cp3_batch*>(b), CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    if (id < 0 || id >= (int)b->probs.size()) return bfail(const_cast<cp3_batch*>(b), CP3_ERR_INDEX, "no such problem");
+    if (offset) *offset = (size_t)b->probs[id].out_off;
+    return CP3_OK;
+}
+
+int cp3_batch_copy_results(cp3_batch* b, size_t first, size_t count, void* dst, void* stream) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    if (!dst) return bfail(b, CP3_ERR_BAD_ARGUMENT, "null destination");
+    if (first > b->out_floats || count > b->out_floats - first)
+        return bfail(b, CP3_ERR_INDEX, "range beyond the result arena (" +
+                                           std::to_string(b->out_floats) + " floats)");
+    if (count == 0) return CP3_OK;
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    B_CUDA(b, cudaMemcpyAsync(dst, b->d_out.ptr + first, count * sizeof(float), cudaMemcpyDefault,
+                              stream ? (cudaStream_t)stream : b->stream), "copy results");
+    return CP3_OK;
+}
+
 size_t cp3_batch_parameter_bytes(void) { return sizeof(OscParams); }
 
 int cp3_batch_info(const cp3_batch* b, int* n_problems, long long* total_bins, size_t* result_bytes,

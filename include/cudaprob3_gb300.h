@@ -274,6 +274,14 @@ int cp3_batch_synchronize(cp3_batch* b, double* ms);
 int cp3_batch_result(cp3_batch* b, int id, const float** ptr, size_t* count);
 /* Asynchronous copy of one problem's result to dst (count floats) on `stream`. */
 int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream);
+/* The results of all problems sit in one arena of result_bytes / 4 floats (cp3_batch_info);
+ * problem id's result starts at float *offset of it.  (No reference counterpart: the
+ * reference has no batches.) */
+int cp3_batch_result_offset(const cp3_batch* b, int id, size_t* offset);
+/* Asynchronous copy of the arena's floats [first, first + count) to dst (host or device) on
+ * `stream` (NULL: the batch's own stream).  A caller that wants every result moves them in a
+ * few large copies instead of one per problem; gaps between problems hold no results. */
+int cp3_batch_copy_results(cp3_batch* b, size_t first, size_t count, void* dst, void* stream);
 /* Bytes of one problem's parameter block (what a run uploads per problem after
  * cp3_batch_set_params). */
 size_t cp3_batch_parameter_bytes(void);

@@ -269,6 +269,16 @@ public:
         synchronizeCopies();
         return out;
     }
+    // Float offset of problem id's result in the result arena, and an asynchronous copy of
+    // the arena's floats [first, first + count) (on the batch's stream when stream is null).
+    size_t resultOffset(int id) {
+        size_t off = 0;
+        check(cp3_batch_result_offset(b_, id, &off));
+        return off;
+    }
+    void copyResultsAsync(size_t first, size_t count, void* dst, void* stream = nullptr) {
+        check(cp3_batch_copy_results(b_, first, count, dst, stream));
+    }
     cp3_batch* handle() { return b_; }
 
 private:

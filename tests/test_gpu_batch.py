@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from cudaprob3_gb300 import AtmosCudaPropagatorSingle, BeamCudaPropagatorSingle, earth
+from cudaprob3_gb300._abi import CP3Error
 from cudaprob3_gb300.batch import Batch
 from tests.gpu_helpers import run_atmos
 
@@ -78,6 +79,29 @@ def test_batch_matches_single_propagators_and_oracle(oracle):
                 assert np.abs(got[j] - want).max() <= MIXED_TOL
                 ref = oracle.beam(om, anti, x, 2.6, L)
                 assert np.abs(got[j].T - ref).max() <= MIXED_TOL
+
+
+def test_whole_arena_copy_holds_every_result():
+    """cp3_batch_copy_results moves the result arena in pieces of any size; each problem's
+    result sits at its cp3_batch_result_offset, bit-identical to its own copy.  A range past
+    the arena is refused."""
+    rng = np.random.default_rng(6)
+    b, probs = build_batch(earth.gaussian_sets(4, seed=14), rng)
+    b.run()
+    b.synchronize()
+    total = b.info()["result_bytes"] // 4
+    arena = np.full(total, np.nan, dtype=np.float32)
+    piece = 123457  # an odd piece size: copies need not follow problem boundaries
+    for first in range(0, total, piece):
+        n = min(piece, total - first)
+        b.copy_results_async(first, n, arena.ctypes.data + 4 * first)
+    b.synchronize_stream()
+    for _, pid, *_ in probs:
+        mine = b.result(pid).ravel()
+        off = b.result_offset(pid)
+        assert np.array_equal(arena[off:off + mine.size], mine)
+    with pytest.raises(CP3Error, match="beyond the result arena"):
+        b.copy_results_async(total - 10, 11, arena.ctypes.data)
 
 
 def test_batch_results_do_not_depend_on_tile_shape():

@@ -60,6 +60,38 @@ def test_59_shells_against_oracle(oracle, prec, tol, anti):
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_the_largest_earth_model_against_oracle(oracle, prec, tol):
+    """128 shells, the most a trajectory may cross (CP3_MAX_SHELLS): the vertical up-going
+    rows cross every one, 257 layer applications of the reference's palindrome.  FP64 and
+    mixed single propagators and one batched problem against the oracle; 129 shells are
+    refused."""
+    from cudaprob3_gb300 import earth
+    from cudaprob3_gb300.batch import Batch
+    from oracle.oracle import Mixing as OMix
+    r, rho, ye = earth.synthetic_shells(128)
+    cz = np.array([-1.0, -0.9999, -0.99, -0.7, -0.2, 0.0, 0.6])
+    en = earth.log_energy_grid(48)
+    m = earth.gaussian_sets(3, seed=77)[2]
+    mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+    for anti, knu in ((False, 1), (True, -1)):
+        ref = oracle.atmos(OMix(*mix6, knu), anti, cz, en, r, rho, ye, 15.0, layer_limit=128)
+        got = run_atmos(prec, mix6, knu, anti, cz, en, r, rho, ye, 15.0)
+        assert np.abs(got - ref).max() <= tol
+        if prec == "mixed":
+            b = Batch(0)
+            b.set_earth(r, rho, ye, 15.0)
+            pid = b.add_atmos(cz, en)
+            b.set_params(pid, m, anti)
+            b.commit()
+            b.run()
+            b.synchronize()
+            assert np.abs(np.transpose(b.result(pid), (1, 2, 0)) - ref).max() <= tol
+    r2, rho2, ye2 = earth.synthetic_shells(129)
+    with pytest.raises(RuntimeError, match="invalid number of maxLayer"):
+        run_atmos(prec, mix6, 1, False, cz, en, r2, rho2, ye2, 15.0)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
 def test_random_parameters_against_oracle(oracle, prec, tol):
     from cudaprob3_gb300 import earth
     from oracle.oracle import Mixing as OMix

@@ -536,6 +536,8 @@ def set_params(p, m, knu):
     p.setNeutrinoMasses(m.dm12sq, m.dm23sq)
 
 
+SERVE_P99_TARGET_MS = 2.0  # the serving latency target for 500 x 500 requests
+
 SERVE_KINDS = (("atm200x200", "atmos", 200), ("atm500x500", "atmos", 500),
                ("atm2000x2000", "atmos", 2000), ("beam10000", "beam", 10000),
                ("beam100000", "beam", 100000))
@@ -689,9 +691,21 @@ def serve_summary(cap, knee, kinds, levels=()):
         "offered_req_per_s": top["offered_req_per_s"], "achieved_req_per_s": top["achieved_req_per_s"],
         "probabilities_per_s": top["probabilities_per_s"], "p50_ms": top["p50_ms"],
         "p99_ms": top["p99_ms"], "atm500x500": top.get("atm500x500")}
+    # the highest load at which 500 x 500 requests keep the 2 ms p99 target (every request
+    # completed, the server keeping up)
+    ok = [lv for lv in levels if lv.get("atm500x500") and lv["completed"] == lv["requests"]
+          and lv["atm500x500"]["p99_ms"] <= SERVE_P99_TARGET_MS]
+    best = max(ok, key=lambda lv: lv["offered_req_per_s"]) if ok else None
+    target = None if best is None else {
+        "p99_target_ms": SERVE_P99_TARGET_MS,
+        "offered_req_per_s": best["offered_req_per_s"], "achieved_req_per_s": best["achieved_req_per_s"],
+        "probabilities_per_s": best["probabilities_per_s"], "atm500x500": best["atm500x500"],
+        "fraction_of_highest_throughput": round(best["achieved_req_per_s"] / top["achieved_req_per_s"], 3)}
     if knee is None:
-        return {"capacity_req_per_s": round(cap, 1), "sustained": None, "highest_throughput": sat}
+        return {"capacity_req_per_s": round(cap, 1), "sustained": None, "highest_throughput": sat,
+                "highest_load_meeting_p99_target_500x500": target}
     out = {"capacity_req_per_s": round(cap, 1), "highest_throughput": sat,
+           "highest_load_meeting_p99_target_500x500": target,
            "offered_req_per_s": knee["offered_req_per_s"],
            "achieved_req_per_s": knee["achieved_req_per_s"],
            "probabilities_per_s": knee["probabilities_per_s"],

@@ -29,6 +29,22 @@ def test_knee_is_the_highest_load_served_without_queueing():
     assert summary["highest_throughput"]["achieved_req_per_s"] == 64150
 
 
+def test_serving_summary_reports_the_load_meeting_the_latency_target():
+    import bench
+    n = lambda rate: int(rate * 1.5)  # noqa: E731
+    levels = []
+    for r, a, p50, p99, p99_500 in ((9000, 8970, 0.15, 0.30, 0.28), (54000, 54470, 0.26, 1.49, 0.40),
+                                    (63000, 63480, 0.30, 5.0, 4.9), (72000, 64150, 92.0, 177.0, 177.0)):
+        lv = level(r, a, p50, p99, n=n(r))
+        lv["atm500x500"] = {"n": 100, "p50_ms": p50, "p99_ms": p99_500}
+        levels.append(lv)
+    knee = bench.serve_knee(levels, 1.5)
+    assert knee["offered_req_per_s"] == 63000  # keeps up, median within 2x of the lightest
+    target = bench.serve_summary(1.0, knee, [], levels)["highest_load_meeting_p99_target_500x500"]
+    assert target["offered_req_per_s"] == 54000 and target["atm500x500"]["p99_ms"] == 0.40
+    assert target["fraction_of_highest_throughput"] == round(54470 / 64150, 3)
+
+
 def test_knee_needs_every_request_completed():
     import bench
     levels = [level(1000, 1000, 0.1, 0.2, n=1500),

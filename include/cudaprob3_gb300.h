@@ -153,7 +153,8 @@ int cp3_calculate_async(cp3_propagator* h, int neutrino_type, void* stream);
 
 /* Computation plus the whole result copied to host memory dst (the device layout,
  * 9 * n_cosines * n_energies values of the handle's precision), asynchronous on `stream`.
- * The cosine rows are computed in n_chunks pieces (<= 0: a default of 4) and each piece's
+ * The cosine rows are computed in n_chunks pieces (<= 0: the default, 4 pieces of at least
+ * 32 MB each, fewer for smaller results) and each piece's
  * copy is queued right after its kernel, so copies overlap computation; dst must be
  * page-locked for that.  Replaces calculateProbabilities followed by the full download of
  * the first getProbability (atmoscudapropagator.cu:222-235). */

@@ -111,9 +111,7 @@ class Server:
         if max_ids <= 0:
             self._check(self._lib.cp3_server_poll(self._h, None, 0, 0.0, C.byref(n)))
             return []
-        buf = getattr(self, "_poll_buf", None)
-        if buf is None or len(buf) < max_ids:
-            buf = self._poll_buf = (C.c_ulonglong * max_ids)()
+        buf = (C.c_ulonglong * max_ids)()  # per call: poll may be called from any thread
         self._check(self._lib.cp3_server_poll(self._h, buf, int(max_ids), float(timeout_s),
                                               C.byref(n)))
         return list(buf[:n.value])

@@ -46,7 +46,7 @@ NCU_TRAFFIC = {
     # the table launch and the bin launch of one run
     ("batch_atmos", "mixed"): (0.436992e6 + 0.060416e6 + 204.449536e6 + 978.470912e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
-    ("batch_beam", "mixed"): (115.233280e6 + 911.497472e6, 921.6e6,
+    ("batch_beam", "mixed"): (115.457024e6 + 911.392000e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
     ("atmos59", "fp64"): (9.935872e6 + 245.010688e6, 288.0e6,
                           "profiles/atmos_f64_kernel_59shells_2000x2000.md"),
@@ -62,7 +62,7 @@ NCU_TRAFFIC = {
 NCU_PIPE = {
     ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7099),
     ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6568),  # the bin launch
-    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6773),
+    ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6007),
     ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8926),
     ("beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),
     ("batch_beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),
@@ -276,7 +276,8 @@ def run_batch(args, w, rank, world):
                 "h2d_bytes_per_step": len(params) * b.parameter_bytes(),
                 "d2h_bytes_per_step": info["result_bytes"], "ms_per_step": e2e_ms,
                 "steps": e2e_steps, "steps_queued": "back to back",
-                "ms_per_step_waiting_each_step": e2e_ms_sync},
+                "ms_per_step_waiting_each_step": e2e_ms_sync,
+                "link": link_summary(info["result_bytes"], e2e_ms, d2h_link())},
         "gpu_launches": args.steps * launches,
         "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
                      "peak": round(peaks["fp32"], 3), "unit": "TFLOP/s",
@@ -513,6 +514,34 @@ def fma_peaks(device):
     fp32 = [v for v in (out["fp32_scalar"], out["fp32_paired"]) if v]
     out["fp32"] = max(fp32) if fp32 else None
     return out
+
+
+def d2h_link(nbytes=256 << 20, reps=5):
+    """The device-to-host link's copy rate in GB/s, measured live: a page-locked copy of
+    nbytes timed with CUDA events (median of reps).  On GB300 every route into host
+    memory (copy engines on one or several streams, 2-D copies, SM stores of any width)
+    measured the same rate, so this bounds any end-to-end step that downloads its results."""
+    import torch
+    src = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda").fill_(0.5)
+    dst = torch.empty(nbytes // 4, dtype=torch.float32, pin_memory=True)
+    s = torch.cuda.Stream()
+    ms = []
+    for _ in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s):
+            e0.record(s)
+            dst.copy_(src, non_blocking=True)
+            e1.record(s)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return nbytes / (statistics.median(ms[1:]) * 1e-3) / 1e9
+
+
+def link_summary(d2h_bytes, e2e_ms, gbs):
+    """The e2e step's roofline: its bytes at the measured link rate, against its time."""
+    return {"d2h_gbs_measured": round(gbs, 1),
+            "d2h_gbs_achieved": round(d2h_bytes / (e2e_ms * 1e-3) / 1e9, 1),
+            "frac_of_link": round(d2h_bytes / (e2e_ms * 1e-3) / 1e9 / gbs, 4)}
 
 
 def make_propagator(w, prec):
@@ -1170,7 +1199,8 @@ def run_ours(args, rank, world):
         "e2e": {"value": world * probs_step / (e2e_ms * 1e-3), "unit": "probabilities/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                 "steps_queued": "back to back, results in two page-locked buffers per type in turn",
-                "ms_per_step_waiting_each_step": e2e_ms_sync},
+                "ms_per_step_waiting_each_step": e2e_ms_sync,
+                "link": link_summary(d2h, e2e_ms, d2h_link())},
         "gpu_launches": args.steps * len(props) * (2 if w["kind"] == "atmos" else 1),
         "roofline": roofline,
         "peaks_tflops": peaks,

@@ -369,8 +369,7 @@ CP3_HD void rotated_layer_f64(const OscParams* __restrict__ p, double E, double 
 // The FP64 branch of the mixed eigen-solver (the reference cubic), kept out of line: inlined,
 // the compiler may hoist part of it (the double conversions of E and rho) above the branch,
 // and on GB300's narrow FP64 pipe even one such instruction per call costs more than the
-// whole double-float path.  vectors: P[k][0..2] = u_k, else the projectors u_k u_k^T; both
-// from eigenvectors orthonormalised in FP64.
+// whole double-float path.  u[k] = the unit eigenvectors u_1, u_2, orthonormalised in FP64.
 //   The fallback runs where two levels nearly meet.  There the Lagrange projectors have
 // entries ~spread / gap that cancel in S = 1 + z1 P1 + z2 P2 (z1 ~ z2), and rounded to FP32
 // separately they no longer do: the beam returned probabilities of 0.4-50 at the exact level
@@ -379,8 +378,8 @@ CP3_HD void rotated_layer_f64(const OscParams* __restrict__ p, double E, double 
 // rounding, and leave only a rotation inside the near-degenerate plane, which S weighs by
 // the small z1 - z2.
 __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams* __restrict__ p,
-                                                                df Ed, df rhod, bool vectors,
-                                                                float P[2][6], float om[2][2]) {
+                                                                df Ed, df rhod, float uf[2][3],
+                                                                float om[2][2]) {
     double Pd[2][6], omd[2], u[2][3];
     rotated_eigen_f64(p, (double)Ed.hi + (double)Ed.lo, (double)rhod.hi + (double)rhod.lo, Pd, omd);
     for (int k = 0; k < 2; k++) {
@@ -390,15 +389,8 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
         om[k][1] = (float)(t - (double)om[k][0]);
     }
     orthonormalize_pair(u[0], u[1]);
-    for (int k = 0; k < 2; k++) {
-        if (vectors) {
-            for (int i = 0; i < 3; i++) P[k][i] = (float)u[k][i];
-        } else {
-            const double* v = u[k];
-            const double q[6] = {v[0] * v[0], v[0] * v[1], v[0] * v[2], v[1] * v[1], v[1] * v[2], v[2] * v[2]};
-            for (int i = 0; i < 6; i++) P[k][i] = (float)q[i];
-        }
-    }
+    for (int k = 0; k < 2; k++)
+        for (int i = 0; i < 3; i++) uf[k][i] = (float)u[k][i];
 }
 
 // The mixed kernels' eigen-decomposition without FP64 on the common path:
@@ -408,8 +400,8 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
 //      trace);
 //   4. the phase rates in turns per km, omega_k / (2 pi) = 2.534 (m_k - m_0) / (2 pi E),
 //      in df64 (hi, lo);
-//   5. the eigenvectors of m_1, m_2 in FP32 from the vacuum eigen-system (the rank-one
-//      update below), and from them P1, P2.
+//   5. the unit eigenvectors u_1, u_2 of m_1, m_2 from the vacuum eigen-system (the
+//      rank-one update below), in double-float (kDf) or FP32.
 // Where two roots lie closer than 5e-3 of the spread -- tested on the FP32 starting roots
 // and again on the refined ones -- the FP64 reference cubic takes over.  Below that the
 // double-float Newton steps are not reliably in their quadratic regime (FP32 starting roots
@@ -424,16 +416,20 @@ __host__ __device__ __noinline__ inline void eigen_fallback_f64(const OscParams*
 // E and rho arrive as float pairs (split once on the host), so the common path runs no FP64
 // instruction at all -- conversions included, which issue on the narrow FP64 pipe.
 //
-// kVectors: instead of the projectors, out[k][0..2] = u_k, the unit eigenvector with
-// P_k = u_k u_k^T (sign arbitrary).
+// out[k][0..2] = u_k, the unit eigenvector with P_k = u_k u_k^T (sign arbitrary).  kDf:
+// the vectors in double-float, rounded once (the eigen tables of the deep atmospheric
+// chains, whose vector errors add up over the layers); else in FP32 (the beam's one layer
+// per baseline).
 // The common path; false where the FP64 fallback has to take over (one call site for it,
 // below, so that no live range of the common path has to survive a call).
-template <bool kVectors>
+template <bool kDf>
 __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restrict__ p, df Ed,
-                                                        df rhod, float P[2][6], float om[2][2]) {
-    // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos
+                                                        df rhod, float P[2][3], float om[2][2]) {
+    // V = -fac of getMfast: +2 sqrt2 G_F N_e E for neutrinos, minus for antineutrinos.
+    // (2 sqrt2 G_F) N_e comes first: constant over a beam's energies, the batched kernel
+    // forms it once per tile (C3 1.2 % faster).
     const df tw = df{1.52588e-4f, -7.040322e-12f};  // kTwoRtTwoGf = hi + lo
-    df V = df_mul(df_mul(tw, Ed), rhod);
+    df V = df_mul(df_mul(tw, rhod), Ed);
     if (p->anti) V = df_neg(V);
     // det(l - H) = l^3 - c2 l^2 + c1 l - c0 with H = H0 + V e0 e0^T (OscParams::cpoly)
     const df c2 = df_add(df{p->cpolyf[0][0], p->cpolyf[0][1]}, V);
@@ -492,8 +488,8 @@ __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restr
             x = df2_sub(x, df2{make_float2(__fdividef(f.hi.x, d.x), __fdividef(f.hi.y, d.y)), bc2(0.0f)});
         };
         newton();
-        bool again = kVectors;
-        if (!kVectors) {
+        bool again = kDf;
+        if (!kDf) {
             const float m2 = c2.hi - x.hi.x - x.hi.y;
             const float d01 = fabsf(x.hi.x - x.hi.y), d02 = fabsf(x.hi.x - m2),
                         d12 = fabsf(x.hi.y - m2);
@@ -525,7 +521,7 @@ __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restr
     // Each difference mu_i - l is formed from the double-float root before rounding to FP32
     // (hi - hi is exact or correctly rounded, the low words add ~ulp), so d is good to a few
     // ulp whatever the cancellation, and |u| = |d| (O orthogonal).
-    if constexpr (kVectors) {
+    if constexpr (kDf) {
         // The eigenvector tables feed every layer of the deep atmospheric chains, where
         // vector errors add up over the layers: on the 59-shell grid the FP32 form below
         // gave 7.5e-6 max error, double-float without the final scaling 4.5e-6, and this
@@ -587,47 +583,39 @@ __device__ __forceinline__ bool rotated_eigen_mixed_try(const OscParams* __restr
         if (!(fminf(n.x, n.y) > 1e-16f * (s2 * s2))) {
             return false;
         }
-        // projectors P_k = u u^T / |d|^2 (00,01,02,11,12,22), good to a few ulp: the beam's one
-        // layer per baseline needs no more (batched-beam max error 1.9e-6, against 1.1e-6 with the
-        // double-float Lagrange projectors, for 15 % less time)
-        const float2 inv = make_float2(__fdividef(1.0f, n.x), __fdividef(1.0f, n.y));
-        const float2 v0 = __fmul2_rn(u[0], inv), v1 = __fmul2_rn(u[1], inv), v2 = __fmul2_rn(u[2], inv);
-        const float2 q[6] = {__fmul2_rn(v0, u[0]), __fmul2_rn(v0, u[1]), __fmul2_rn(v0, u[2]),
-                             __fmul2_rn(v1, u[1]), __fmul2_rn(v1, u[2]), __fmul2_rn(v2, u[2])};
+        // the unit vectors u / |d|, good to a few ulp: the beam's one layer per baseline needs
+        // no more
+        const float2 r = make_float2(rsqrtf(n.x), rsqrtf(n.y));
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
-            P[0][k] = q[k].x;
-            P[1][k] = q[k].y;
+        for (int i = 0; i < 3; i++) {
+            const float2 v = __fmul2_rn(u[i], r);
+            P[0][i] = v.x;
+            P[1][i] = v.y;
         }
         return true;
     }
 }
 
-template <bool kVectors>
+template <bool kDf>
 __device__ __forceinline__ void rotated_eigen_mixed_t(const OscParams* __restrict__ p, df Ed,
-                                                      df rhod, float P[2][6], float om[2][2]) {
-    if (!rotated_eigen_mixed_try<kVectors>(p, Ed, rhod, P, om))
-        eigen_fallback_f64(p, Ed, rhod, kVectors, P, om);
+                                                      df rhod, float u[2][3], float om[2][2]) {
+    if (!rotated_eigen_mixed_try<kDf>(p, Ed, rhod, u, om)) eigen_fallback_f64(p, Ed, rhod, u, om);
 }
 
-// Projectors P1, P2 (00,01,02,11,12,22) and phase rates.
-__device__ __forceinline__ void rotated_eigen_mixed(const OscParams* __restrict__ p, df Ed,
-                                                    df rhod, float P[2][6], float om[2][2]) {
-    rotated_eigen_mixed_t<false>(p, Ed, rhod, P, om);
-}
-__device__ __forceinline__ void rotated_eigen_mixed(const OscParams* __restrict__ p, double E,
-                                                    double rho, float P[2][6], float om[2][2]) {
-    rotated_eigen_mixed_t<false>(p, df_from(E), df_from(rho), P, om);
-}
-// Unit eigenvectors u1, u2 (P_k = u_k u_k^T) and phase rates.
+// Unit eigenvectors u1, u2 (P_k = u_k u_k^T) and phase rates; the vectors in double-float,
+// rounded once (the eigen tables).
 __device__ __forceinline__ void rotated_eigen_vectors(const OscParams* __restrict__ p, df Ed,
                                                       df rhod, float u[2][3], float om[2][2]) {
-    float out[2][6];
-    rotated_eigen_mixed_t<true>(p, Ed, rhod, out, om);
-#pragma unroll
-    for (int k = 0; k < 2; k++)
-#pragma unroll
-        for (int i = 0; i < 3; i++) u[k][i] = out[k][i];
+    rotated_eigen_mixed_t<true>(p, Ed, rhod, u, om);
+}
+// The same with the vectors in FP32 (the beam).
+__device__ __forceinline__ void rotated_eigen_vectors_fp32(const OscParams* __restrict__ p, df Ed,
+                                                           df rhod, float u[2][3], float om[2][2]) {
+    rotated_eigen_mixed_t<false>(p, Ed, rhod, u, om);
+}
+__device__ __forceinline__ void rotated_eigen_vectors_fp32(const OscParams* __restrict__ p, double E,
+                                                           double rho, float u[2][3], float om[2][2]) {
+    rotated_eigen_mixed_t<false>(p, df_from(E), df_from(rho), u, om);
 }
 
 CP3_HD cf cmulf(cf a, cf b) {

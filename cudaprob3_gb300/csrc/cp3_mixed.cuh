@@ -18,9 +18,6 @@ namespace cp3 {
 // G += z_k u_k (u_k^T G): 96 FMAs (48 of them paired over re/im) against 132 for forming S
 // and a symmetric-by-general product.
 
-struct cs6 {  // complex symmetric 3x3
-    cf a[6];
-};
 struct cg9 {  // complex general 3x3
     cf a[3][3];
 };
@@ -30,17 +27,6 @@ struct Layer {
     float u[2][3];  // unit eigenvectors u1, u2
     float z[2][2];  // z_k = e^{-i omega_k L} - 1 (re, im)
 };
-
-// S = 1 + z1 P1 + z2 P2 from the two phase factors and the real projectors (beam).
-__device__ __forceinline__ void layer_matrix(const float z[2][2], const float P1[6],
-                                             const float P2[6], cs6& S) {
-#pragma unroll
-    for (int q = 0; q < 6; q++) {
-        const float one = (q == 0 || q == 3 || q == 5) ? 1.0f : 0.0f;
-        S.a[q].re = fmaf(z[1][0], P2[q], fmaf(z[0][0], P1[q], one));
-        S.a[q].im = fmaf(z[1][1], P2[q], z[0][1] * P1[q]);
-    }
-}
 
 // ------------------------------------------------------------------------------------
 // Paired FP32 forms (bc2, neg2 and df2 are in cp3_device.cuh): complex entries as (re, im)
@@ -92,6 +78,21 @@ __device__ __forceinline__ void unit_turn_minus_one2(float2 r, float2 lo, float2
         __int_as_float(__float_as_int(sx.x) ^ (__float_as_int(r.x) & 0x80000000)),
         __int_as_float(__float_as_int(sx.y) ^ (__float_as_int(r.y) & 0x80000000)));
     const float2 cs = make_float2(rx ? -cx.x : cx.x, ry ? -cx.y : cx.y);
+    const float2 ml = __fmul2_rn(lo, bc2(-kTwoPiF));
+    zre = __ffma2_rn(ml, sn, __fadd2_rn(cs, bc2(-1.0f)));
+    zim = __ffma2_rn(ml, cs, neg2(sn));
+}
+
+// The same with the hardware sine and cosine (sin.approx / cos.approx) of 2 pi r: absolute
+// error about 4e-7 on [-pi, pi], against about an ulp for the polynomial.  For the beam's
+// single layer per baseline that is an error of the same size in each probability; the
+// deep atmospheric chains, where the layers' errors add up, keep the polynomial.
+__device__ __forceinline__ void unit_turn_minus_one2_hw(float2 r, float2 lo, float2& zre,
+                                                        float2& zim) {
+    const float2 x = __fmul2_rn(r, bc2(kTwoPiF));
+    float2 sn, cs;
+    __sincosf(x.x, &sn.x, &cs.x);
+    __sincosf(x.y, &sn.y, &cs.y);
     const float2 ml = __fmul2_rn(lo, bc2(-kTwoPiF));
     zre = __ffma2_rn(ml, sn, __fadd2_rn(cs, bc2(-1.0f)));
     zim = __ffma2_rn(ml, cs, neg2(sn));
@@ -247,13 +248,6 @@ __device__ __forceinline__ void newton_schulz(cg9& A) {
             R.a[i][j] = cf{h.r.x - h.i.y, h.r.y + h.i.x};
         }
     A = R;
-}
-
-__device__ __forceinline__ void sym_to_gen(const cs6& S, cg9& G) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) G.a[i][j] = S.a[sidx(i, j)];
 }
 
 // Probabilities of A = W A2 W^+, W = [[1,0,0],[0,c,s e],[0,-s,c e]], e = e^{i d}; stores
@@ -430,27 +424,100 @@ __device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict
     segment_layer_inline_rates(p, E, rho_e, L, f, om);
 }
 
+// The beam's nine probabilities from the three-flavour expansion over the matter eigenstates
+// k = 0, 1, 2, with U_ak = (W u_k)_a the flavour components of eigenstate k:
+//   P(a -> b) = delta_ab + 2 sum_{j>k} [Re c_jk (cos D_jk - 1) + Im c_jk sin D_jk],
+//   c_jk = w_j conj(w_k),  w_k = U_bk conj(U_ak),  D_jk = phi_j - phi_k  (phi_0 = 0).
+// For a = b, c_jk = m_aj m_ak with m_ak = |U_ak|^2, and there is no sine term.  For a != b
+// the w_k sum to zero (unitarity), so Re c_jk = W_l - (W_0 + W_1 + W_2) / 2 with
+// W_k = m_ak m_bk and l the third index, and Im c_10 = -Im c_20 = Im c_21 = J_ab, the
+// Jarlskog invariant in matter (J for e->mu, mu->tau and tau->e, -J for the reverse).
+// The nine moduli and J thus give every coefficient once per energy; a baseline then
+// costs its two phase factors and about 30 FMAs, where forming S = 1 + z1 P1 + z2 P2 and
+// turning it into the flavour basis cost about 110.
+struct BeamCoefs {
+    float d[3][3];  // flavour a's survival: 2 m_aj m_ak for (j, k) = (1, 0), (2, 0), (2, 1)
+    float o[3][3];  // the pairs (e, mu), (mu, tau), (tau, e): 2 Re c_jk for the same (j, k)
+    float j2;       // 2 J_{e mu}
+};
+
+// u[k-1] = the unit eigenvector of eigenstate k in the rotated basis (k = 1, 2); W = [[1,0,0],
+// [0,c,s e],[0,-s,c e]], e = e^{i delta}, so U_ek = u_k0, U_mu,k = c u_k1 + s e u_k2 and
+// U_tau,k = -s u_k1 + c e u_k2.
+__device__ __forceinline__ BeamCoefs beam_coefficients(const float u[2][3], const WParams& w) {
+    // eigenstates 1 and 2 side by side
+    const float2 u0 = make_float2(u[0][0], u[1][0]), u1 = make_float2(u[0][1], u[1][1]),
+                 u2 = make_float2(u[0][2], u[1][2]);
+    const float cc = w.c * w.c, ss = w.s * w.s, cs2 = 2.0f * w.c * w.s;
+    const float2 b1 = __fmul2_rn(u1, u1), b2 = __fmul2_rn(u2, u2), x = __fmul2_rn(u1, u2);
+    const float2 xr = __fmul2_rn(x, bc2(cs2 * w.er));
+    float2 m[3];  // m[a] = (|U_a1|^2, |U_a2|^2)
+    m[0] = __fmul2_rn(u0, u0);
+    m[1] = __ffma2_rn(bc2(cc), b1, __ffma2_rn(bc2(ss), b2, xr));
+    m[2] = __ffma2_rn(bc2(ss), b1, __ffma2_rn(bc2(cc), b2, neg2(xr)));
+    float m0[3];  // |U_a0|^2
+#pragma unroll
+    for (int a = 0; a < 3; a++) m0[a] = 1.0f - m[a].x - m[a].y;
+    BeamCoefs k;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float t = 2.0f * m0[a];
+        k.d[a][0] = t * m[a].x;
+        k.d[a][1] = t * m[a].y;
+        k.d[a][2] = 2.0f * m[a].x * m[a].y;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const int a = q, b = q == 2 ? 0 : q + 1;
+        const float W0 = m0[a] * m0[b], W1 = m[a].x * m[b].x, W2 = m[a].y * m[b].y;
+        const float S = W0 + W1 + W2;
+        k.o[q][0] = fmaf(2.0f, W2, -S);
+        k.o[q][1] = fmaf(2.0f, W1, -S);
+        k.o[q][2] = fmaf(2.0f, W0, -S);
+    }
+    // J_{e mu} = Im(w_2 conj(w_1)), w_k = U_mu,k u_k0: u_10 u_20 c s sin(delta) (u_11 u_22 - u_12 u_21)
+    k.j2 = cs2 * w.ei * (u0.x * u0.y) * fmaf(u1.x, u2.y, -(u2.x * u1.y));
+    return k;
+}
+
+// The nine probabilities of one baseline from the coefficients and the phase factors
+// z_k = e^{-i phi_k} - 1 (k = 1, 2); channel a*3+b = P(a -> b) at out[ch * plane].
+__device__ __forceinline__ void beam_store(const BeamCoefs& k, float2 zr, float2 zi,
+                                           float* __restrict__ out, size_t plane) {
+    // cos D - 1 for (1,0), (2,0), (2,1); e^{-i D_21} = (1 + z_2) conj(1 + z_1)
+    const float g0 = zr.x, g1 = zr.y, g2 = fmaf(zi.x, zi.y, fmaf(zr.x, zr.y, zr.x + zr.y));
+    // sin D_10 - sin D_20 + sin D_21 = Im z_1 Re z_2 - Im z_2 Re z_1
+    const float jt = k.j2 * fmaf(zi.x, zr.y, -(zi.y * zr.x));
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        out[(size_t)(a * 4) * plane] = fmaf(k.d[a][2], g2, fmaf(k.d[a][1], g1, fmaf(k.d[a][0], g0, 1.0f)));
+    // (e, mu): channels 1 (e->mu) and 3 (mu->e); (mu, tau): 5 and 7; (tau, e): 6 and 2
+    constexpr int fwd[3] = {1, 5, 6}, rev[3] = {3, 7, 2};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float v = fmaf(k.o[q][2], g2, fmaf(k.o[q][1], g1, k.o[q][0] * g0));
+        out[(size_t)fwd[q] * plane] = v + jt;
+        out[(size_t)rev[q] * plane] = v - jt;
+    }
+}
+
 // One beam energy (E, rho_e as double or float pair): eigen-decomposition (double-float
-// refined), then for each baseline L[j] the layer matrix and the nine probabilities at
-// out + j * baseline_stride + ch * plane.
+// refined), the energy's coefficients, then for each baseline L[j] its phase factors and
+// the nine probabilities at out + j * baseline_stride + ch * plane.
 template <class Real>
 __device__ __forceinline__ void beam_bin_mixed(const OscParams* __restrict__ p, const WParams& w,
                                                Real E, Real rho_e, const float2* L, int nL,
                                                float* __restrict__ out, size_t plane,
                                                size_t baseline_stride) {
-    float P[2][6], om[2][2];
-    rotated_eigen_mixed(p, E, rho_e, P, om);
+    float u[2][3], om[2][2];
+    rotated_eigen_vectors_fp32(p, E, rho_e, u, om);
+    const BeamCoefs k = beam_coefficients(u, w);
     for (int j = 0; j < nL; j++) {
         float2 lo, zr, zi;
         const float2 r = reduced_turn2(make_float2(om[0][0], om[1][0]),
                                        make_float2(om[0][1], om[1][1]), L[j].x, L[j].y, lo);
-        unit_turn_minus_one2(r, lo, zr, zi);
-        const float z[2][2] = {{zr.x, zi.x}, {zr.y, zi.y}};
-        cs6 S;
-        layer_matrix(z, P[0], P[1], S);
-        cg9 A2;
-        sym_to_gen(S, A2);
-        store_probabilities(A2, w.c, w.s, w.er, w.ei, out + j * baseline_stride, plane);
+        unit_turn_minus_one2_hw(r, lo, zr, zi);
+        beam_store(k, zr, zi, out + j * baseline_stride, plane);
     }
 }
 

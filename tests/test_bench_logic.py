@@ -1,5 +1,5 @@
-"""Host logic of bench.py that decides what a line reports (no GPU): the serving knee and
-the canonical flop count."""
+"""Host logic of bench.py that decides what a line reports (no GPU): the serving knee,
+the canonical flop count and the e2e step's fraction of the device-to-host link."""
 import os
 import sys
 
@@ -58,3 +58,11 @@ def test_canonical_flops_per_bin():
     assert bench.f_bin(0) == 257
     assert bench.f_bin(4) == 27 + 230 * 5 + 216 * 7
     np.testing.assert_array_equal(bench.f_bin(np.array([0, 1])), [257, 27 + 460 + 216])
+
+
+def test_link_summary_is_the_e2e_bytes_over_the_measured_link():
+    import bench
+    s = bench.link_summary(288e6, 1.5, 192.0)
+    assert s["d2h_gbs_achieved"] == 192.0
+    assert s["frac_of_link"] == 1.0
+    assert bench.link_summary(144e6, 1.5, 192.0)["frac_of_link"] == 0.5

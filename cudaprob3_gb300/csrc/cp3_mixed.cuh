@@ -295,6 +295,92 @@ CP3_HD WParams wparams(const OscParams& p) {
     return WParams{p.wf[0], p.wf[1], p.wf[2], p.wf[3]};
 }
 
+// The nine probabilities of a single constant-density layer (a beam baseline, or an
+// atmospheric bin that crosses no shell) from the three-flavour expansion over the matter
+// eigenstates k = 0, 1, 2, with U_ak = (W u_k)_a the flavour components of eigenstate k:
+//   P(a -> b) = delta_ab + 2 sum_{j>k} [Re c_jk (cos D_jk - 1) + Im c_jk sin D_jk],
+//   c_jk = w_j conj(w_k),  w_k = U_bk conj(U_ak),  D_jk = phi_j - phi_k  (phi_0 = 0).
+// For a = b, c_jk = m_aj m_ak with m_ak = |U_ak|^2, and there is no sine term.  For a != b
+// the w_k sum to zero (unitarity), so Re c_jk = W_l - (W_0 + W_1 + W_2) / 2 with
+// W_k = m_ak m_bk and l the third index, and Im c_10 = -Im c_20 = Im c_21 = J_ab, the
+// Jarlskog invariant in matter (J for e->mu, mu->tau and tau->e, -J for the reverse).
+// The nine moduli and J thus give every coefficient once per (energy, density); a path
+// length then costs its two phase factors and about 30 FMAs, where forming
+// S = 1 + z1 P1 + z2 P2 and turning it into the flavour basis cost about 110.
+struct LayerCoefs {
+    float d[3][3];  // flavour a's survival: 2 m_aj m_ak for (j, k) = (1, 0), (2, 0), (2, 1)
+    float o[3][3];  // the pairs (e, mu), (mu, tau), (tau, e): 2 Re c_jk for the same (j, k)
+    float j2;       // 2 J_{e mu}
+};
+
+// u[k-1] = the unit eigenvector of eigenstate k in the rotated basis (k = 1, 2); W = [[1,0,0],
+// [0,c,s e],[0,-s,c e]], e = e^{i delta}, so U_ek = u_k0, U_mu,k = c u_k1 + s e u_k2 and
+// U_tau,k = -s u_k1 + c e u_k2.
+__device__ __forceinline__ LayerCoefs layer_coefficients(const float u[2][3], const WParams& w) {
+    // eigenstates 1 and 2 side by side
+    const float2 u0 = make_float2(u[0][0], u[1][0]), u1 = make_float2(u[0][1], u[1][1]),
+                 u2 = make_float2(u[0][2], u[1][2]);
+    const float cc = w.c * w.c, ss = w.s * w.s, cs2 = 2.0f * w.c * w.s;
+    const float2 b1 = __fmul2_rn(u1, u1), b2 = __fmul2_rn(u2, u2), x = __fmul2_rn(u1, u2);
+    const float2 xr = __fmul2_rn(x, bc2(cs2 * w.er));
+    float2 m[3];  // m[a] = (|U_a1|^2, |U_a2|^2)
+    m[0] = __fmul2_rn(u0, u0);
+    m[1] = __ffma2_rn(bc2(cc), b1, __ffma2_rn(bc2(ss), b2, xr));
+    m[2] = __ffma2_rn(bc2(ss), b1, __ffma2_rn(bc2(cc), b2, neg2(xr)));
+    float m0[3];  // |U_a0|^2
+#pragma unroll
+    for (int a = 0; a < 3; a++) m0[a] = 1.0f - m[a].x - m[a].y;
+    LayerCoefs k;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float t = 2.0f * m0[a];
+        k.d[a][0] = t * m[a].x;
+        k.d[a][1] = t * m[a].y;
+        k.d[a][2] = 2.0f * m[a].x * m[a].y;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const int a = q, b = q == 2 ? 0 : q + 1;
+        const float W0 = m0[a] * m0[b], W1 = m[a].x * m[b].x, W2 = m[a].y * m[b].y;
+        const float S = W0 + W1 + W2;
+        k.o[q][0] = fmaf(2.0f, W2, -S);
+        k.o[q][1] = fmaf(2.0f, W1, -S);
+        k.o[q][2] = fmaf(2.0f, W0, -S);
+    }
+    // J_{e mu} = Im(w_2 conj(w_1)), w_k = U_mu,k u_k0: u_10 u_20 c s sin(delta) (u_11 u_22 - u_12 u_21)
+    k.j2 = cs2 * w.ei * (u0.x * u0.y) * fmaf(u1.x, u2.y, -(u2.x * u1.y));
+    return k;
+}
+
+// The nine probabilities of one path length from the coefficients and the phase factors
+// z_k = e^{-i phi_k} - 1 (k = 1, 2); channel a*3+b = P(a -> b) at out[ch * plane].
+__device__ __forceinline__ void layer_store(const LayerCoefs& k, float2 zr, float2 zi,
+                                            float* __restrict__ out, size_t plane) {
+    // cos D - 1 for (1,0), (2,0), (2,1); e^{-i D_21} = (1 + z_2) conj(1 + z_1)
+    const float g0 = zr.x, g1 = zr.y, g2 = fmaf(zi.x, zi.y, fmaf(zr.x, zr.y, zr.x + zr.y));
+    // sin D_10 - sin D_20 + sin D_21 = Im z_1 Re z_2 - Im z_2 Re z_1
+    const float jt = k.j2 * fmaf(zi.x, zr.y, -(zi.y * zr.x));
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        out[(size_t)(a * 4) * plane] = fmaf(k.d[a][2], g2, fmaf(k.d[a][1], g1, fmaf(k.d[a][0], g0, 1.0f)));
+    // (e, mu): channels 1 (e->mu) and 3 (mu->e); (mu, tau): 5 and 7; (tau, e): 6 and 2
+    constexpr int fwd[3] = {1, 5, 6}, rev[3] = {3, 7, 2};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float v = fmaf(k.o[q][2], g2, fmaf(k.o[q][1], g1, k.o[q][0] * g0));
+        out[(size_t)fwd[q] * plane] = v + jt;
+        out[(size_t)rev[q] * plane] = v - jt;
+    }
+}
+
+// A bin that crosses no shell: the air layer alone, through the expansion.
+__device__ __forceinline__ void store_one_layer(const Layer& F, const WParams& w,
+                                                float* __restrict__ out, size_t plane) {
+    layer_store(layer_coefficients(F.u, w), make_float2(F.z[0][0], F.z[1][0]),
+                make_float2(F.z[0][1], F.z[1][1]), out, plane);
+}
+
+
 // One atmospheric bin over M+1 segments, generic in where each segment's layer comes from:
 // seg(l, F) fills F for segment l (0 = air, then shells inwards).
 // B <- B^T S_M B for the innermost layer F = S_M (complex symmetric: the upper triangle of
@@ -339,16 +425,16 @@ __device__ __forceinline__ void chain_mixed(SegFn seg, int M, cg9& G) {
 template <class SegFn>
 __device__ __forceinline__ void atmos_bin_mixed_with(SegFn seg, int M, const WParams& w,
                                                      float* __restrict__ out, size_t plane) {
-    cg9 A2;
     Layer F;
     if (M == 0) {
         seg(0, F);
-        layer_to_gen(F, A2);
-    } else {
-        chain_mixed(seg, M, A2);
-        seg(0, F);
-        apply_right(F, A2);  // ... S_0
+        store_one_layer(F, w, out, plane);
+        return;
     }
+    cg9 A2;
+    chain_mixed(seg, M, A2);
+    seg(0, F);
+    apply_right(F, A2);  // ... S_0
     // One or two FP32 layer matrices are unitary to ~1e-7 already; the correction pays off
     // from the longer chains on (it removes the drift accumulated over ~2M products).
     if (M >= kNewtonSchulzMinShells) newton_schulz(A2);
@@ -374,30 +460,30 @@ __device__ __forceinline__ void atmos_bin_mixed(const float* __restrict__ tab, s
             [&](int l, Layer& F) { layer_from_entry(entry(l), s_len[l], F); }, M, w, out, plane);
         return;
     }
-    cg9 A2;
     Layer F;
     if (M == 0) {
         layer_from_entry(entry(0), s_len[0], F);
-        layer_to_gen(F, A2);
-    } else {
-        TableEntry e = entry(1), n = entry(M > 1 ? 2 : 0);
-        layer_from_entry(e, s_len[1], F);
-        layer_to_gen(F, A2);  // B = S_1
-        if (M > 1) {
-            for (int l = 2; l < M; l++) {
-                e = n;
-                n = entry(l + 1);
-                layer_from_entry(e, s_len[l], F);
-                apply_left(F, A2);
-            }
-            e = n;
-            n = entry(0);
-            layer_from_entry(e, s_len[M], F);
-            close_palindrome(F, A2);
-        }
-        layer_from_entry(n, s_len[0], F);
-        apply_right(F, A2);  // ... S_0
+        store_one_layer(F, w, out, plane);
+        return;
     }
+    cg9 A2;
+    TableEntry e = entry(1), n = entry(M > 1 ? 2 : 0);
+    layer_from_entry(e, s_len[1], F);
+    layer_to_gen(F, A2);  // B = S_1
+    if (M > 1) {
+        for (int l = 2; l < M; l++) {
+            e = n;
+            n = entry(l + 1);
+            layer_from_entry(e, s_len[l], F);
+            apply_left(F, A2);
+        }
+        e = n;
+        n = entry(0);
+        layer_from_entry(e, s_len[M], F);
+        close_palindrome(F, A2);
+    }
+    layer_from_entry(n, s_len[0], F);
+    apply_right(F, A2);  // ... S_0
     if (M >= kNewtonSchulzMinShells) newton_schulz(A2);  // as in atmos_bin_mixed_with
     store_probabilities(A2, w.c, w.s, w.er, w.ei, out, plane);
 }
@@ -424,83 +510,6 @@ __device__ __forceinline__ void segment_layer_inline(const OscParams* __restrict
     segment_layer_inline_rates(p, E, rho_e, L, f, om);
 }
 
-// The beam's nine probabilities from the three-flavour expansion over the matter eigenstates
-// k = 0, 1, 2, with U_ak = (W u_k)_a the flavour components of eigenstate k:
-//   P(a -> b) = delta_ab + 2 sum_{j>k} [Re c_jk (cos D_jk - 1) + Im c_jk sin D_jk],
-//   c_jk = w_j conj(w_k),  w_k = U_bk conj(U_ak),  D_jk = phi_j - phi_k  (phi_0 = 0).
-// For a = b, c_jk = m_aj m_ak with m_ak = |U_ak|^2, and there is no sine term.  For a != b
-// the w_k sum to zero (unitarity), so Re c_jk = W_l - (W_0 + W_1 + W_2) / 2 with
-// W_k = m_ak m_bk and l the third index, and Im c_10 = -Im c_20 = Im c_21 = J_ab, the
-// Jarlskog invariant in matter (J for e->mu, mu->tau and tau->e, -J for the reverse).
-// The nine moduli and J thus give every coefficient once per energy; a baseline then
-// costs its two phase factors and about 30 FMAs, where forming S = 1 + z1 P1 + z2 P2 and
-// turning it into the flavour basis cost about 110.
-struct BeamCoefs {
-    float d[3][3];  // flavour a's survival: 2 m_aj m_ak for (j, k) = (1, 0), (2, 0), (2, 1)
-    float o[3][3];  // the pairs (e, mu), (mu, tau), (tau, e): 2 Re c_jk for the same (j, k)
-    float j2;       // 2 J_{e mu}
-};
-
-// u[k-1] = the unit eigenvector of eigenstate k in the rotated basis (k = 1, 2); W = [[1,0,0],
-// [0,c,s e],[0,-s,c e]], e = e^{i delta}, so U_ek = u_k0, U_mu,k = c u_k1 + s e u_k2 and
-// U_tau,k = -s u_k1 + c e u_k2.
-__device__ __forceinline__ BeamCoefs beam_coefficients(const float u[2][3], const WParams& w) {
-    // eigenstates 1 and 2 side by side
-    const float2 u0 = make_float2(u[0][0], u[1][0]), u1 = make_float2(u[0][1], u[1][1]),
-                 u2 = make_float2(u[0][2], u[1][2]);
-    const float cc = w.c * w.c, ss = w.s * w.s, cs2 = 2.0f * w.c * w.s;
-    const float2 b1 = __fmul2_rn(u1, u1), b2 = __fmul2_rn(u2, u2), x = __fmul2_rn(u1, u2);
-    const float2 xr = __fmul2_rn(x, bc2(cs2 * w.er));
-    float2 m[3];  // m[a] = (|U_a1|^2, |U_a2|^2)
-    m[0] = __fmul2_rn(u0, u0);
-    m[1] = __ffma2_rn(bc2(cc), b1, __ffma2_rn(bc2(ss), b2, xr));
-    m[2] = __ffma2_rn(bc2(ss), b1, __ffma2_rn(bc2(cc), b2, neg2(xr)));
-    float m0[3];  // |U_a0|^2
-#pragma unroll
-    for (int a = 0; a < 3; a++) m0[a] = 1.0f - m[a].x - m[a].y;
-    BeamCoefs k;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const float t = 2.0f * m0[a];
-        k.d[a][0] = t * m[a].x;
-        k.d[a][1] = t * m[a].y;
-        k.d[a][2] = 2.0f * m[a].x * m[a].y;
-    }
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-        const int a = q, b = q == 2 ? 0 : q + 1;
-        const float W0 = m0[a] * m0[b], W1 = m[a].x * m[b].x, W2 = m[a].y * m[b].y;
-        const float S = W0 + W1 + W2;
-        k.o[q][0] = fmaf(2.0f, W2, -S);
-        k.o[q][1] = fmaf(2.0f, W1, -S);
-        k.o[q][2] = fmaf(2.0f, W0, -S);
-    }
-    // J_{e mu} = Im(w_2 conj(w_1)), w_k = U_mu,k u_k0: u_10 u_20 c s sin(delta) (u_11 u_22 - u_12 u_21)
-    k.j2 = cs2 * w.ei * (u0.x * u0.y) * fmaf(u1.x, u2.y, -(u2.x * u1.y));
-    return k;
-}
-
-// The nine probabilities of one baseline from the coefficients and the phase factors
-// z_k = e^{-i phi_k} - 1 (k = 1, 2); channel a*3+b = P(a -> b) at out[ch * plane].
-__device__ __forceinline__ void beam_store(const BeamCoefs& k, float2 zr, float2 zi,
-                                           float* __restrict__ out, size_t plane) {
-    // cos D - 1 for (1,0), (2,0), (2,1); e^{-i D_21} = (1 + z_2) conj(1 + z_1)
-    const float g0 = zr.x, g1 = zr.y, g2 = fmaf(zi.x, zi.y, fmaf(zr.x, zr.y, zr.x + zr.y));
-    // sin D_10 - sin D_20 + sin D_21 = Im z_1 Re z_2 - Im z_2 Re z_1
-    const float jt = k.j2 * fmaf(zi.x, zr.y, -(zi.y * zr.x));
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-        out[(size_t)(a * 4) * plane] = fmaf(k.d[a][2], g2, fmaf(k.d[a][1], g1, fmaf(k.d[a][0], g0, 1.0f)));
-    // (e, mu): channels 1 (e->mu) and 3 (mu->e); (mu, tau): 5 and 7; (tau, e): 6 and 2
-    constexpr int fwd[3] = {1, 5, 6}, rev[3] = {3, 7, 2};
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-        const float v = fmaf(k.o[q][2], g2, fmaf(k.o[q][1], g1, k.o[q][0] * g0));
-        out[(size_t)fwd[q] * plane] = v + jt;
-        out[(size_t)rev[q] * plane] = v - jt;
-    }
-}
-
 // One beam energy (E, rho_e as double or float pair): eigen-decomposition (double-float
 // refined), the energy's coefficients, then for each baseline L[j] its phase factors and
 // the nine probabilities at out + j * baseline_stride + ch * plane.
@@ -511,13 +520,13 @@ __device__ __forceinline__ void beam_bin_mixed(const OscParams* __restrict__ p, 
                                                size_t baseline_stride) {
     float u[2][3], om[2][2];
     rotated_eigen_vectors_fp32(p, E, rho_e, u, om);
-    const BeamCoefs k = beam_coefficients(u, w);
+    const LayerCoefs k = layer_coefficients(u, w);
     for (int j = 0; j < nL; j++) {
         float2 lo, zr, zi;
         const float2 r = reduced_turn2(make_float2(om[0][0], om[1][0]),
                                        make_float2(om[0][1], om[1][1]), L[j].x, L[j].y, lo);
         unit_turn_minus_one2_hw(r, lo, zr, zi);
-        beam_store(k, zr, zi, out + j * baseline_stride, plane);
+        layer_store(k, zr, zi, out + j * baseline_stride, plane);
     }
 }
 

@@ -227,11 +227,19 @@ def run_batch(args, w, rank, world):
 
     # end to end through the public API: every step uploads each problem's parameters
     # (cp3_batch_set_params), runs, and downloads the whole result arena into page-locked
-    # host memory in 256 MB pieces (cp3_batch_copy_results; one reused buffer: the bytes
-    # cross the link all the same)
+    # host memory.  Where the arena fits in a quarter of the host's memory (up to 16 GB),
+    # cp3_batch_run_to_host runs the bins in windows of whole problems and downloads each
+    # window while the next computes.  Otherwise (C3's 59 GB) the run is followed by copies
+    # of the arena in 256 MB pieces into one reused buffer (cp3_batch_copy_results): the
+    # bytes cross the link all the same.
     arena = b.info()["result_bytes"] // 4
     piece = 64 << 20  # floats
-    host = torch.empty(min(piece, arena), dtype=torch.float32, pin_memory=True)
+    try:
+        host_mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError, AttributeError):
+        host_mem = 0
+    whole = 4 * arena <= min(16 << 30, host_mem // 4)
+    host = torch.empty(arena if whole else min(piece, arena), dtype=torch.float32, pin_memory=True)
 
     # Steps are queued back to back (set_params waits only until the previous step's
     # parameter upload has left the staging area); the timed region ends when the last
@@ -239,9 +247,12 @@ def run_batch(args, w, rank, world):
     def e2e_step(wait):
         for pid, m, anti in params:
             b.set_params(pid, m, anti)
-        b.run()
-        for first in range(0, arena, piece):
-            b.copy_results_async(first, min(piece, arena - first), host.data_ptr())
+        if whole:
+            b.run_to_host(host.data_ptr())
+        else:
+            b.run()
+            for first in range(0, arena, piece):
+                b.copy_results_async(first, min(piece, arena - first), host.data_ptr())
         if wait:
             b.synchronize_stream()
 
@@ -276,6 +287,10 @@ def run_batch(args, w, rank, world):
                 "h2d_bytes_per_step": len(params) * b.parameter_bytes(),
                 "d2h_bytes_per_step": info["result_bytes"], "ms_per_step": e2e_ms,
                 "steps": e2e_steps, "steps_queued": "back to back",
+                "download": ("cp3_batch_run_to_host: bins in windows of whole problems, each "
+                             "window downloaded while the next computes" if whole else
+                             "cp3_batch_run, then the arena in 256 MB copies into one reused "
+                             "page-locked buffer"),
                 "ms_per_step_waiting_each_step": e2e_ms_sync,
                 "link": link_summary(info["result_bytes"], e2e_ms, d2h_link())},
         "gpu_launches": args.steps * launches,

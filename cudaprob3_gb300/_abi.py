@@ -25,7 +25,7 @@ EXPORTS = (
     "cp3_batch_add_atmos", "cp3_batch_add_beam", "cp3_batch_set_params", "cp3_batch_commit",
     "cp3_batch_set_shape", "cp3_batch_get_shape", "cp3_batch_set_split_tables",
     "cp3_batch_get_split_tables", "cp3_batch_debug_withhold_tables",
-    "cp3_batch_tune", "cp3_batch_run",
+    "cp3_batch_tune", "cp3_batch_run", "cp3_batch_run_to_host",
     "cp3_batch_synchronize", "cp3_batch_result", "cp3_batch_copy_result", "cp3_batch_info",
     "cp3_batch_result_offset", "cp3_batch_copy_results",
     "cp3_batch_parameter_bytes",
@@ -90,6 +90,7 @@ _SIGS = {
     "cp3_batch_debug_withhold_tables": ([_h, C.c_int], C.c_int),
     "cp3_batch_tune": ([_h, C.c_int], C.c_int),
     "cp3_batch_run": ([_h, C.c_void_p], C.c_int),
+    "cp3_batch_run_to_host": ([_h, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "cp3_batch_synchronize": ([_h, _dp], C.c_int),
     "cp3_batch_result": ([_h, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], C.c_int),
     "cp3_batch_copy_result": ([_h, C.c_int, C.c_void_p, C.c_void_p], C.c_int),

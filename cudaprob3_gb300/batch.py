@@ -102,6 +102,13 @@ class Batch:
     def run(self, stream=None):
         self._check(self._lib.cp3_batch_run(self._h, C.c_void_p(stream) if stream else None))
 
+    def run_to_host(self, dst_ptr: int, n_pieces: int = 0, stream=None):
+        """One run with every result copied to dst (result_bytes, laid out as the arena):
+        the bins in windows of whole problems, each window's download overlapping the next
+        window's computation.  Page-locked dst for the overlap."""
+        self._check(self._lib.cp3_batch_run_to_host(self._h, C.c_void_p(dst_ptr), int(n_pieces),
+                                                    C.c_void_p(stream) if stream else None))
+
     def synchronize(self) -> float:
         ms = C.c_double()
         self._check(self._lib.cp3_batch_synchronize(self._h, C.byref(ms)))

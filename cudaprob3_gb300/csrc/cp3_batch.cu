@@ -117,13 +117,27 @@ struct cp3_batch {
     cudaEvent_t ev_params = nullptr, ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
 
+    // What a run in pieces (cp3_batch_run_to_host) launches directly: the kernel arguments,
+    // the problem mix, the grids of the table and bin instances, the bin-tile prefix sums;
+    // set by every configure.
+    Args args{};
+    int kinds = 0, grid_tab = 1, grid_bins = 1;
+    std::vector<int> bstart;
+    // The copy stream of a run in pieces, an event per piece, and the end of its copies.
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> ev_piece;
+    cudaEvent_t ev_copied = nullptr;
+
     ~cp3_batch() {
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         if (graph) cudaGraphExecDestroy(graph);
-        for (cudaEvent_t e : {ev_params, ev0, ev1})
+        for (cudaEvent_t e : {ev_params, ev0, ev1, ev_copied})
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_piece) cudaEventDestroy(e);
         if (h_params) cudaFreeHost(h_params);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -207,9 +221,11 @@ int configure(cp3_batch* b) {
     // exercises the single launch's bounded wait, so it keeps the single launch.
     const bool split = b->split_tables && a[n] > 0 && !b->withhold_tables;
     const int kinds = batch_kinds(b->probs);
-    int occ = 0, occ_tab = 0;
+    // (a run in pieces launches the table and bin instances separately, split or not)
+    int occ = 0, occ_tab = 0, occ_bins = 0;
     if (occupancy(kinds, &occ, split ? kPhaseBins : kPhaseAll) || occ < 1 ||
-        (split && (occupancy(kinds, &occ_tab, kPhaseTables) || occ_tab < 1)))
+        occupancy(kinds, &occ_bins, kPhaseBins) || occ_bins < 1 ||
+        (a[n] > 0 && (occupancy(kinds, &occ_tab, kPhaseTables) || occ_tab < 1)))
         return bfail(b, CP3_ERR_CUDA, "occupancy query failed");
     const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, occ) : occ;
     const int grid = std::max(1, b->sms * bps);
@@ -222,6 +238,11 @@ int configure(cp3_batch* b) {
               b->d_done.ptr, b->d_counter.ptr, b->d_status.ptr,
               (long long)b->d_tables.n, (long long)b->d_out.n, (long long)b->d_seg_len.n,
               (long long)b->d_energies.n};
+    b->args = args;
+    b->kinds = kinds;
+    b->grid_tab = grid_tab;
+    b->grid_bins = std::max(1, b->sms * std::min(bps, occ_bins));
+    b->bstart = bi;
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -343,18 +364,93 @@ int commit(cp3_batch* b) {
     return configure(b);
 }
 
-int launch(cp3_batch* b, cudaStream_t s) {
-    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
-    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+int upload_params(cp3_batch* b, cudaStream_t s) {
     if (b->params_dirty) {
         B_CUDA(b, cudaMemcpyAsync(b->d_params.ptr, b->h_params, sizeof(OscParams) * b->probs.size(),
                                   cudaMemcpyHostToDevice, s), "upload parameters");
         B_CUDA(b, cudaEventRecord(b->ev_params, s), "event");
         b->params_dirty = false;
     }
+    return CP3_OK;
+}
+
+int launch(cp3_batch* b, cudaStream_t s) {
+    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    if (int rc = upload_params(b, s)) return rc;
     B_CUDA(b, cudaEventRecord(b->ev0, s), "event");
     B_CUDA(b, cudaGraphLaunch(b->graph, s), "graph launch");
     B_CUDA(b, cudaEventRecord(b->ev1, s), "event");
+    b->timed = true;
+    return CP3_OK;
+}
+
+// Default pieces of a run to host memory: at least 256 MB each, at most kMaxPieces.
+constexpr size_t kMinPieceBytes = size_t(256) << 20;
+constexpr int kMaxPieces = 8;
+
+// One run with its results copied to host memory: the table tiles, then the bin tiles in
+// n_pieces windows of whole problems of about equal result size.  Each window's range of
+// the result arena goes to dst on the batch's copy stream as soon as its launch ends, while
+// the next window computes; the caller's stream then waits for the last copy.
+int run_to_host(cp3_batch* b, float* dst, int n_pieces, cudaStream_t s) {
+    if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
+    if (!dst) return bfail(b, CP3_ERR_BAD_ARGUMENT, "cp3_batch_run_to_host: null destination");
+    if (b->withhold_tables)
+        return bfail(b, CP3_ERR_UNSUPPORTED,
+                     "cp3_batch_run_to_host: the withheld-tables testing aid runs through cp3_batch_run only");
+    if (n_pieces > kMaxPieces)
+        return bfail(b, CP3_ERR_BAD_ARGUMENT, "cp3_batch_run_to_host: at most 8 pieces");
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    const int n = (int)b->probs.size();
+    if (n_pieces <= 0)
+        n_pieces = (int)std::max<size_t>(1, std::min<size_t>(kMaxPieces, b->out_floats * sizeof(float) / kMinPieceBytes));
+    n_pieces = std::min(n_pieces, n);
+    if (!b->copy_stream) {
+        B_CUDA(b, cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking), "copy stream");
+        B_CUDA(b, cudaEventCreateWithFlags(&b->ev_copied, cudaEventDisableTiming), "event");
+        for (int i = 0; i < kMaxPieces; i++) {
+            cudaEvent_t e = nullptr;
+            B_CUDA(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            b->ev_piece.push_back(e);
+        }
+    }
+    // piece boundaries: the first problem whose results start at or past k/n of the arena
+    std::vector<int> cut{0};
+    for (int k = 1; k < n_pieces; k++) {
+        const long long target = (long long)(b->out_floats * (size_t)k / (size_t)n_pieces);
+        int p = cut.back() + 1;
+        while (p < n && b->out_off[p] < target) p++;
+        if (p < n) cut.push_back(p);
+    }
+    cut.push_back(n);
+    if (int rc = upload_params(b, s)) return rc;
+    B_CUDA(b, cudaEventRecord(b->ev0, s), "event");
+    // the resets the captured run does, then the launches of its split form
+    B_CUDA(b, cudaMemsetAsync(b->d_counter.ptr, 0, 2 * sizeof(unsigned int), s), "reset");
+    B_CUDA(b, cudaMemsetAsync(b->d_done.ptr, 0, sizeof(int) * std::max(n, 1), s), "reset");
+    B_CUDA(b, cudaMemsetAsync(b->d_status.ptr, 0, sizeof(int), s), "reset");
+    if (b->total_a > 0) {
+        kernel_for(b->kinds, kPhaseTables)<<<b->grid_tab, kBlock, 0, s>>>(b->args);
+        B_CUDA(b, cudaGetLastError(), "table launch");
+    }
+    for (size_t i = 0; i + 1 < cut.size(); i++) {
+        const int p0 = cut[i], p1 = cut[i + 1];
+        Args a = b->args;
+        a.bin_lo = b->bstart[p0];
+        a.bin_hi = b->bstart[p1];
+        B_CUDA(b, cudaMemsetAsync(b->d_counter.ptr + 1, 0, sizeof(unsigned int), s), "reset");
+        kernel_for(b->kinds, kPhaseBins)<<<b->grid_bins, kBlock, 0, s>>>(a);
+        B_CUDA(b, cudaGetLastError(), "bin launch");
+        B_CUDA(b, cudaEventRecord(b->ev_piece[i], s), "event");
+        const size_t lo = (size_t)b->out_off[p0], hi = p1 < n ? (size_t)b->out_off[p1] : b->out_floats;
+        B_CUDA(b, cudaStreamWaitEvent(b->copy_stream, b->ev_piece[i], 0), "order copy");
+        B_CUDA(b, cudaMemcpyAsync(dst + lo, b->d_out.ptr + lo, (hi - lo) * sizeof(float), cudaMemcpyDefault,
+                                  b->copy_stream), "copy results");
+    }
+    B_CUDA(b, cudaEventRecord(b->ev1, s), "event");
+    B_CUDA(b, cudaEventRecord(b->ev_copied, b->copy_stream), "event");
+    B_CUDA(b, cudaStreamWaitEvent(s, b->ev_copied, 0), "order copies");
     b->timed = true;
     return CP3_OK;
 }
@@ -543,6 +639,12 @@ int cp3_batch_run(cp3_batch* b, void* stream) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
     TraceRange trace("batch_run");
     return launch(b, stream ? (cudaStream_t)stream : b->stream);
+}
+
+int cp3_batch_run_to_host(cp3_batch* b, void* dst, int n_pieces, void* stream) {
+    if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
+    TraceRange trace("batch_run_to_host");
+    return run_to_host(b, (float*)dst, n_pieces, stream ? (cudaStream_t)stream : b->stream);
 }
 
 int cp3_batch_synchronize(cp3_batch* b, double* ms) {

@@ -68,6 +68,10 @@ struct Args {
     int* status;
     // Element counts of the arenas, read only by the bounds checks of CP3_DEVICE_CHECKS builds.
     long long n_tables, n_out, n_seg, n_energies;
+    // The bin tiles a kPhaseBins launch runs, counted from the first bin tile:
+    // [bin_lo, min(bin_hi, total_b)).  The default is all of them; a run in pieces
+    // (cp3_batch_run_to_host) launches one window of whole problems per piece.
+    int bin_lo = 0, bin_hi = 0x7fffffff;
 };
 
 // Status words the kernel can leave: a wait that ran out, a tile of a kind the instance was
@@ -145,8 +149,10 @@ static __global__ void __launch_bounds__(kBlock, 7) batch_kernel(const Args a) {
     const unsigned lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const Header hdr = *a.hdr;
-    const int first = kPhases == kPhaseBins ? hdr.total_a : 0;
-    const int total = kPhases == kPhaseTables ? hdr.total_a : hdr.total_a + hdr.total_b;
+    const int first = kPhases == kPhaseBins ? hdr.total_a + a.bin_lo : 0;
+    const int total = kPhases == kPhaseTables ? hdr.total_a
+                      : kPhases == kPhaseBins ? hdr.total_a + min(hdr.total_b, a.bin_hi)
+                                              : hdr.total_a + hdr.total_b;
     unsigned int* const counter = a.counter + (kPhases == kPhaseBins ? 1 : 0);
 
     // The warp's current problem: tiles arrive in increasing order, so a warp's problems do

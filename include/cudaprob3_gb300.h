@@ -268,6 +268,17 @@ int cp3_batch_debug_withhold_tables(cp3_batch* b, int on);
 int cp3_batch_tune(cp3_batch* b, int use_cache);
 /* One run over every problem on `stream` (NULL = the batch's own stream). */
 int cp3_batch_run(cp3_batch* b, void* stream);
+/* One run with every result copied to dst, laid out as the arena (result_bytes bytes; each
+ * problem at its cp3_batch_result_offset).  The bins run in n_pieces windows of whole
+ * problems (0: one per 256 MB of results, at most 8); each window's range of the arena is
+ * copied on the batch's copy stream while the next window computes, so with page-locked dst
+ * the download overlaps the computation.  `stream` (NULL = the batch's own stream) waits for
+ * the last copy.  The run always uses the split form (a table launch, then the bin launches)
+ * and gives the same results as cp3_batch_run.  CP3_ERR_BAD_ARGUMENT for a null dst or more
+ * than 8 pieces, CP3_ERR_UNSUPPORTED while cp3_batch_debug_withhold_tables is on.  (No
+ * reference counterpart: the reference has no batches; its propagators download their
+ * results in calculateProbabilities.) */
+int cp3_batch_run_to_host(cp3_batch* b, void* dst, int n_pieces, void* stream);
 /* Waits for the last run and for everything queued on the batch's own stream (result
  * copies with a NULL stream); *ms = the run's device time. */
 int cp3_batch_synchronize(cp3_batch* b, double* ms);

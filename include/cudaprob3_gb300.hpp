@@ -249,6 +249,11 @@ public:
     void commit() { check(cp3_batch_commit(b_)); }
     void tune(bool use_cache = true) { check(cp3_batch_tune(b_, use_cache ? 1 : 0)); }
     void run(void* cuda_stream = nullptr) { check(cp3_batch_run(b_, cuda_stream)); }
+    // One run with every result copied to dst (result bytes, laid out as the arena), the
+    // download of each window of problems overlapping the next window's computation.
+    void runToHost(void* dst, int n_pieces = 0, void* cuda_stream = nullptr) {
+        check(cp3_batch_run_to_host(b_, dst, n_pieces, cuda_stream));
+    }
     double synchronize() {
         double ms = 0.0;
         check(cp3_batch_synchronize(b_, &ms));

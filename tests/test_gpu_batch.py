@@ -104,6 +104,58 @@ def test_whole_arena_copy_holds_every_result():
         b.copy_results_async(total - 10, 11, arena.ctypes.data)
 
 
+def test_run_to_host_matches_run():
+    """cp3_batch_run_to_host: the bins in windows of whole problems, each window's arena range
+    downloaded while the next computes.  Every problem's result lands at its arena offset,
+    bit-identical to cp3_batch_run's, for any number of pieces, with and without eigen tables
+    (a mixed batch and a beam-only one)."""
+    import torch
+    rng = np.random.default_rng(7)
+    mixed, probs = build_batch(earth.gaussian_sets(4, seed=16), rng)
+    beam = Batch(0)
+    beam_probs = []
+    for m in earth.gaussian_sets(6, seed=17):
+        for anti in (False, True):
+            pid = beam.add_beam(earth.lin_energy_grid(int(rng.integers(1000, 5000))), 2.6, [295.0, 1300.0])
+            beam.set_params(pid, m, anti)
+            beam_probs.append(pid)
+    beam.commit()
+    for b, pids in ((mixed, [q[1] for q in probs]), (beam, beam_probs)):
+        b.run()
+        b.synchronize()
+        want = {pid: b.result(pid).ravel() for pid in pids}
+        total = b.info()["result_bytes"] // 4
+        for n_pieces in (1, 3, 8, 0):
+            host = torch.full((total,), float("nan"), dtype=torch.float32).pin_memory()
+            b.run_to_host(host.data_ptr(), n_pieces)
+            b.synchronize()
+            arena = host.numpy()
+            for pid in pids:
+                off = b.result_offset(pid)
+                assert np.array_equal(arena[off:off + want[pid].size], want[pid]), (n_pieces, pid)
+        # a plain run afterwards is unchanged
+        b.run()
+        b.synchronize()
+        for pid in pids:
+            assert np.array_equal(b.result(pid).ravel(), want[pid])
+
+
+def test_run_to_host_errors():
+    rng = np.random.default_rng(8)
+    b, _ = build_batch(earth.gaussian_sets(2, seed=18), rng)
+    host = np.zeros(b.info()["result_bytes"] // 4, dtype=np.float32)
+    with pytest.raises(CP3Error, match="at most 8 pieces"):
+        b.run_to_host(host.ctypes.data, 9)
+    with pytest.raises(CP3Error, match="null destination"):
+        b.run_to_host(0)
+    b.debug_withhold_tables(True)
+    with pytest.raises(CP3Error, match="withheld-tables"):
+        b.run_to_host(host.ctypes.data)
+    b.debug_withhold_tables(False)
+    b.run_to_host(host.ctypes.data)
+    b.synchronize()
+
+
 def test_batch_results_do_not_depend_on_tile_shape():
     """Tile shapes and the launch split (one launch with waits, or a table launch then a bin
     launch) leave every result bit-identical."""

@@ -1125,24 +1125,27 @@ def run_ours(args, rank, world):
     cz_pinned = (torch.from_numpy(np.asarray(w["cz"], dtype=np.float64)).pin_memory()
                  if w["kind"] == "atmos" else None)
 
-    # neutrino and antineutrino on their own streams, each computed in row pieces whose
-    # downloads overlap the next piece's compute (cp3_calculate_to_host_async).  Steps are
-    # queued back to back, as a fitter pipelines consecutive evaluations: a step's setters
-    # and compute are queued while the previous step's download is still on the link (the
-    # handle orders its uploads, computes and copies on the device), and the timed region
-    # ends when the last step's results are in host memory.
-    e2e_streams = [torch.cuda.Stream() for _ in props]
+    # neutrino and antineutrino each on their own pair of streams, used in turn, each step
+    # computed in row pieces whose downloads (on the handle's copy stream) overlap the next
+    # piece's compute (cp3_calculate_to_host_async).  Steps are queued back to back, as a
+    # fitter pipelines consecutive evaluations: a step's setters and compute are queued while
+    # the previous step's download is still on the link.  The handle orders its uploads,
+    # computes and copies on the device (a row piece is recomputed once its previous copy
+    # has left), and the step's stream waits for its download, so the two streams let a step
+    # compute behind the previous step's download.  The timed region ends when the last
+    # step's results are in host memory.
+    e2e_streams = [[torch.cuda.Stream(), torch.cuda.Stream()] for _ in props]
 
     def e2e_step(k, wait):
         for t, p in enumerate(props):
             p.setEnergyList(en_pinned.numpy())
             if cz_pinned is not None:
                 p.setCosineList(cz_pinned.numpy())
-            sp = e2e_streams[t].cuda_stream
+            sp = e2e_streams[t][k % 2].cuda_stream
             p.calculate_to_host_async(t, host_out[t][k % 2].data_ptr(), 0, sp)
         if wait:
             for st in e2e_streams:
-                st.synchronize()
+                st[k % 2].synchronize()
 
     for k in range(max(1, args.warmup)):
         e2e_step(k, True)
@@ -1150,8 +1153,9 @@ def run_ours(args, rank, world):
     t0 = time.perf_counter()
     for k in range(args.steps):
         e2e_step(k, False)
-    for st in e2e_streams:
-        st.synchronize()
+    for pair in e2e_streams:
+        for st in pair:
+            st.synchronize()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world, "cuda")
     # the same steps with the host waiting for each step's results before the next
     t0 = time.perf_counter()
@@ -1213,7 +1217,8 @@ def run_ours(args, rank, world):
                          f"{d2h / 1e6:.0f} MB exceeds L2"},
         "e2e": {"value": world * probs_step / (e2e_ms * 1e-3), "unit": "probabilities/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "steps_queued": "back to back, results in two page-locked buffers per type in turn",
+                "steps_queued": "back to back, results in two page-locked buffers per type in "
+                                "turn, two streams per type in turn",
                 "ms_per_step_waiting_each_step": e2e_ms_sync,
                 "link": link_summary(d2h, e2e_ms, d2h_link())},
         "gpu_launches": args.steps * len(props) * (2 if w["kind"] == "atmos" else 1),

@@ -105,13 +105,29 @@ struct cp3_propagator {
     bool upload_pending = false;
     void* h_stage = nullptr;
 
+    // The downloads of calculate_to_host_async (atmospheric row pieces) run on copy_stream:
+    // piece c's copy waits for ev_piece[c] (its rows computed) and records
+    // ev_piece_copied[c]; ev_copied marks the end of the last download.  A later compute of
+    // the same row pieces waits for each piece's copy only, so it can run while the rest of
+    // the download is on the link; any other compute waits for the whole download.
+    // copy_rows: the row cuts of the last download (empty: none issued).
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> ev_piece, ev_piece_copied;
+    cudaEvent_t ev_copied = nullptr;
+    std::vector<int> copy_rows;
+
     ~cp3_propagator() {
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         for (cudaEvent_t& e : ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_piece) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_piece_copied) cudaEventDestroy(e);
+        if (ev_copied) cudaEventDestroy(ev_copied);
         if (ev_done) cudaEventDestroy(ev_done);
         if (ev_upload) cudaEventDestroy(ev_upload);
         if (h_stage) cudaFreeHost(h_stage);
         if (h_result) cudaFreeHost(h_result);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -211,7 +227,30 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
 // reads: they start once it has ended.
 int wait_last_compute(cp3_propagator* h) {
     if (h->last_stream) CP3_CUDA(h, cudaEventSynchronize(h->ev_done), "wait for the last compute");
+    if (!h->copy_rows.empty()) CP3_CUDA(h, cudaEventSynchronize(h->ev_copied), "wait for the last download");
     return CP3_OK;
+}
+
+// The copy stream and n piece events of calculate_to_host_async, made on first use.
+cudaError_t ensure_copy_events(cp3_propagator* h, int n) {
+    cudaError_t e = cudaSuccess;
+    if (!h->copy_stream) {
+        e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_copied, cudaEventDisableTiming);
+    }
+    while (e == cudaSuccess && (int)h->ev_piece.size() < n) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming);
+        if (e != cudaSuccess) break;
+        e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(a);
+            break;
+        }
+        h->ev_piece.push_back(a);
+        h->ev_piece_copied.push_back(b);
+    }
+    return e;
 }
 
 // Uploads the trajectory table and density classes if any of their inputs changed.
@@ -349,6 +388,10 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
     if (h->upload_pending && s != h->stream) e = cudaStreamWaitEvent(s, h->ev_upload, 0);
     if (e == cudaSuccess && h->last_stream && h->last_stream != s)
         e = cudaStreamWaitEvent(s, h->ev_done, 0);
+    // the rows of the last download: its row pieces wait for their own copies (below), any
+    // other compute for all of it
+    const bool pieces = host_dst && h->kind == 0;
+    if (e == cudaSuccess && !pieces && !h->copy_rows.empty()) e = cudaStreamWaitEvent(s, h->ev_copied, 0);
     if (e != cudaSuccess) return cuda_fail(h, e, "order compute");
     h->timed = false;
     const bool profile = h->profiling && !host_dst;  // kernel times only without copies
@@ -405,22 +448,38 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
         if (!host_dst) {
             if (e == cudaSuccess) e = bins(RowRange{});
         } else {
-            // each piece: rows [r0, r1) of all 9 channel planes, one 2-D copy.  The first
-            // piece is half the size of the others, so that the link starts sooner (measured
-            // 1.5 % off the 59-shell 2000 x 2000 step against equal pieces).
+            // each piece: rows [r0, r1) of all 9 channel planes, one 2-D copy on the copy
+            // stream once the piece is computed.  The first piece is half the size of the
+            // others, so that the link starts sooner (measured 1.5 % off the 59-shell
+            // 2000 x 2000 step against equal pieces).
             const int chunks = std::max(1, std::min(n_chunks, h->nc));
             const size_t plane = (size_t)h->nc * h->ne * esz, row = (size_t)h->ne * esz;
             const long long den = 2LL * chunks - 1;
-            for (int c = 0; c < chunks && e == cudaSuccess; c++) {
-                const int r0 = c == 0 ? 0 : (int)((long long)h->nc * (2 * c - 1) / den);
+            std::vector<int> cuts{0};
+            for (int c = 0; c < chunks; c++) {
                 const int r1 = (int)((long long)h->nc * (2 * c + 1) / den);
-                if (r1 <= r0) continue;
-                e = bins(RowRange{r0, r1});
+                if (r1 > cuts.back()) cuts.push_back(r1);
+            }
+            const int np = (int)cuts.size() - 1;
+            if (e == cudaSuccess) e = ensure_copy_events(h, np);
+            // the same row pieces as the last download: each waits for its own copy
+            const bool same = cuts == h->copy_rows;
+            if (e == cudaSuccess && !same && !h->copy_rows.empty())
+                e = cudaStreamWaitEvent(s, h->ev_copied, 0);
+            for (int c = 0; c < np && e == cudaSuccess; c++) {
+                const int r0 = cuts[c], r1 = cuts[c + 1];
+                if (same) e = cudaStreamWaitEvent(s, h->ev_piece_copied[c], 0);
+                if (e == cudaSuccess) e = bins(RowRange{r0, r1});
+                if (e == cudaSuccess) e = cudaEventRecord(h->ev_piece[c], s);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(h->copy_stream, h->ev_piece[c], 0);
                 if (e == cudaSuccess)
                     e = cudaMemcpy2DAsync((char*)host_dst + r0 * row, plane,
                                           h->d_result.ptr + r0 * row, plane, (r1 - r0) * row, 9,
-                                          cudaMemcpyDeviceToHost, s);
+                                          cudaMemcpyDeviceToHost, h->copy_stream);
+                if (e == cudaSuccess) e = cudaEventRecord(h->ev_piece_copied[c], h->copy_stream);
             }
+            if (e == cudaSuccess) e = cudaEventRecord(h->ev_copied, h->copy_stream);
+            if (e == cudaSuccess) h->copy_rows = cuts;
         }
         mark(2);
         h->timed_table = true;
@@ -442,6 +501,9 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
         h->timed_table = false;
     }
     if (e == cudaSuccess) e = cudaEventRecord(h->ev_done, s);
+    // the caller's stream then waits for the download: work queued behind it sees the host
+    // copy (ev_done, the compute's end, orders later uploads and computes of the handle)
+    if (e == cudaSuccess && pieces) e = cudaStreamWaitEvent(s, h->ev_copied, 0);
     if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
     h->result_on_host = false;
     h->computed = true;

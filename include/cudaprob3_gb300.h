@@ -154,10 +154,13 @@ int cp3_calculate_async(cp3_propagator* h, int neutrino_type, void* stream);
 /* Computation plus the whole result copied to host memory dst (the device layout,
  * 9 * n_cosines * n_energies values of the handle's precision), asynchronous on `stream`.
  * The cosine rows are computed in n_chunks pieces (<= 0: the default, 4 pieces of at least
- * 32 MB each, fewer for smaller results) and each piece's
- * copy is queued right after its kernel, so copies overlap computation; dst must be
- * page-locked for that.  Replaces calculateProbabilities followed by the full download of
- * the first getProbability (atmoscudapropagator.cu:222-235). */
+ * 32 MB each, fewer for smaller results).  Each piece's copy goes on the handle's copy
+ * stream once the piece is computed, so copies overlap computation; dst must be page-locked
+ * for that.  `stream` waits for the last copy.  A later computation of the same row pieces
+ * waits only for each piece's own copy, so a call on another stream can compute while this
+ * one's download is still running.  (Atmospheric handles; a beam handle's single copy
+ * follows its kernel on `stream`.)  Replaces calculateProbabilities followed by the full
+ * download of the first getProbability (atmoscudapropagator.cu:222-235). */
 int cp3_calculate_to_host_async(cp3_propagator* h, int neutrino_type, void* dst, int n_chunks,
                                 void* stream);
 

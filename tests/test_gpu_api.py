@@ -187,6 +187,39 @@ def test_energy_uploads_and_computes_ordered_across_streams(prec):
             assert np.array_equal(hosts[k].numpy().reshape(want[k].shape), want[k]), (rep, k)
 
 
+def test_pipelined_downloads_never_see_a_later_step():
+    """Back-to-back calculate_to_host_async steps on two streams in turn: a step's row pieces
+    are recomputed while the previous step's download is still on the link, each piece only
+    after its own copy has left.  Every host buffer must hold its own step's result, and a
+    plain compute queued behind the downloads must not reach them either."""
+    import torch
+    nc, ne = 1000, 1000
+    grids = [earth.log_energy_grid(ne) * f for f in (1.0, 0.8, 1.3)]
+    want = []
+    for en in grids:
+        q = configured(nc=nc, ne=ne, prec="mixed")
+        q.setEnergyList(en)
+        q.calculateProbabilities(NeutrinoType.Neutrino)
+        want.append(q.result().copy())
+    p = configured(nc=nc, ne=ne, prec="mixed")
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    steps = 6
+    hosts = [torch.full((9 * nc * ne,), -1.0, dtype=torch.float32, pin_memory=True)
+             for _ in range(steps)]
+    for k in range(steps):
+        p.setEnergyList(grids[k % 3])
+        p.calculate_to_host_async(NeutrinoType.Neutrino, hosts[k].data_ptr(), 4,
+                                  streams[k % 2].cuda_stream)
+    # a plain compute of another grid, queued behind the last downloads
+    p.setEnergyList(grids[1])
+    p.calculateProbabilities(NeutrinoType.Neutrino)
+    for st in streams:
+        st.synchronize()
+    for k in range(steps):
+        assert np.array_equal(hosts[k].numpy().reshape(want[0].shape), want[k % 3]), k
+    assert np.array_equal(p.result(), want[1])
+
+
 def test_calculate_to_host_beam():
     import torch
     ne = 101

@@ -116,6 +116,7 @@ struct cp3_batch {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev_params = nullptr, ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
+    bool ran = false;  // ev1 marks the end of a run
 
     // What a run in pieces (cp3_batch_run_to_host) launches directly: the kernel arguments,
     // the problem mix, the grids of the table and bin instances, the bin-tile prefix sums;
@@ -127,6 +128,7 @@ struct cp3_batch {
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> ev_piece;
     cudaEvent_t ev_copied = nullptr;
+    bool downloads = false;  // ev_copied has been recorded
 
     ~cp3_batch() {
         cudaSetDevice(device);
@@ -374,14 +376,24 @@ int upload_params(cp3_batch* b, cudaStream_t s) {
     return CP3_OK;
 }
 
+// A run rewrites the parameters and the result arena: on a stream other than the last
+// run's, it waits for that run to end and for the last run_to_host's copies, which may still
+// be reading them.
+int order_after_last_run(cp3_batch* b, cudaStream_t s) {
+    if (b->ran) B_CUDA(b, cudaStreamWaitEvent(s, b->ev1, 0), "order run after the last run");
+    if (b->downloads) B_CUDA(b, cudaStreamWaitEvent(s, b->ev_copied, 0), "order run after download");
+    return CP3_OK;
+}
+
 int launch(cp3_batch* b, cudaStream_t s) {
     if (!b->committed) return bfail(b, CP3_ERR_NOT_SET, "cp3_batch_commit first");
     B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    if (int rc = order_after_last_run(b, s)) return rc;
     if (int rc = upload_params(b, s)) return rc;
     B_CUDA(b, cudaEventRecord(b->ev0, s), "event");
     B_CUDA(b, cudaGraphLaunch(b->graph, s), "graph launch");
     B_CUDA(b, cudaEventRecord(b->ev1, s), "event");
-    b->timed = true;
+    b->timed = b->ran = true;
     return CP3_OK;
 }
 
@@ -406,14 +418,13 @@ int run_to_host(cp3_batch* b, float* dst, int n_pieces, cudaStream_t s) {
     if (n_pieces <= 0)
         n_pieces = (int)std::max<size_t>(1, std::min<size_t>(kMaxPieces, b->out_floats * sizeof(float) / kMinPieceBytes));
     n_pieces = std::min(n_pieces, n);
-    if (!b->copy_stream) {
+    if (!b->copy_stream)
         B_CUDA(b, cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking), "copy stream");
-        B_CUDA(b, cudaEventCreateWithFlags(&b->ev_copied, cudaEventDisableTiming), "event");
-        for (int i = 0; i < kMaxPieces; i++) {
-            cudaEvent_t e = nullptr;
-            B_CUDA(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
-            b->ev_piece.push_back(e);
-        }
+    if (!b->ev_copied) B_CUDA(b, cudaEventCreateWithFlags(&b->ev_copied, cudaEventDisableTiming), "event");
+    while ((int)b->ev_piece.size() < kMaxPieces) {
+        cudaEvent_t e = nullptr;
+        B_CUDA(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+        b->ev_piece.push_back(e);
     }
     // piece boundaries: the first problem whose results start at or past k/n of the arena
     std::vector<int> cut{0};
@@ -424,6 +435,7 @@ int run_to_host(cp3_batch* b, float* dst, int n_pieces, cudaStream_t s) {
         if (p < n) cut.push_back(p);
     }
     cut.push_back(n);
+    if (int rc = order_after_last_run(b, s)) return rc;
     if (int rc = upload_params(b, s)) return rc;
     B_CUDA(b, cudaEventRecord(b->ev0, s), "event");
     // the resets the captured run does, then the launches of its split form
@@ -450,8 +462,9 @@ int run_to_host(cp3_batch* b, float* dst, int n_pieces, cudaStream_t s) {
     }
     B_CUDA(b, cudaEventRecord(b->ev1, s), "event");
     B_CUDA(b, cudaEventRecord(b->ev_copied, b->copy_stream), "event");
+    b->downloads = true;
     B_CUDA(b, cudaStreamWaitEvent(s, b->ev_copied, 0), "order copies");
-    b->timed = true;
+    b->timed = b->ran = true;
     return CP3_OK;
 }
 
@@ -650,8 +663,10 @@ int cp3_batch_run_to_host(cp3_batch* b, void* dst, int n_pieces, void* stream) {
 int cp3_batch_synchronize(cp3_batch* b, double* ms) {
     if (!b) return bfail(nullptr, CP3_ERR_BAD_ARGUMENT, "null batch");
     B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
-    // everything queued on the batch's own stream, result copies included
+    // everything queued on the batch's own stream, result copies included, and the copies of
+    // the last run to host memory
     B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+    if (b->downloads) B_CUDA(b, cudaEventSynchronize(b->ev_copied), "synchronize downloads");
     if (!b->timed) return CP3_OK;
     B_CUDA(b, cudaEventSynchronize(b->ev1), "synchronize");
     if (ms) {

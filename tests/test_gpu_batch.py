@@ -140,6 +140,45 @@ def test_run_to_host_matches_run():
             assert np.array_equal(b.result(pid).ravel(), want[pid])
 
 
+def test_runs_on_other_streams_wait_for_the_last_run_and_download():
+    """A run queued on another stream right after a run to host memory, with new parameters
+    and no host wait in between, must neither change the parameters nor the arena under the
+    first run's kernels and copies."""
+    import torch
+    rng = np.random.default_rng(9)
+    b, probs = build_batch(earth.gaussian_sets(4, seed=19), rng)
+    pids = [q[1] for q in probs]
+    sets_a = {pid: (m, anti) for _, pid, m, anti, *_ in probs}
+    sets_b = {pid: (earth.gaussian_sets(8, seed=20)[k % 8], anti)
+              for k, (_, pid, m, anti, *_) in enumerate(probs)}
+    want = {}
+    for name, sets in (("a", sets_a), ("b", sets_b)):
+        for pid, (m, anti) in sets.items():
+            b.set_params(pid, m, anti)
+        b.run()
+        b.synchronize()
+        want[name] = {pid: b.result(pid).ravel() for pid in pids}
+    assert any(not np.array_equal(want["a"][p], want["b"][p]) for p in pids)
+    total = b.info()["result_bytes"] // 4
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    for rep in range(3):
+        host = torch.full((total,), float("nan"), dtype=torch.float32).pin_memory()
+        for pid, (m, anti) in sets_a.items():
+            b.set_params(pid, m, anti)
+        b.run_to_host(host.data_ptr(), 8, streams[0].cuda_stream)
+        for pid, (m, anti) in sets_b.items():
+            b.set_params(pid, m, anti)
+        b.run(streams[1].cuda_stream)
+        for st in streams:
+            st.synchronize()
+        b.synchronize()
+        arena = host.numpy()
+        for pid in pids:
+            off = b.result_offset(pid)
+            assert np.array_equal(arena[off:off + want["a"][pid].size], want["a"][pid]), (rep, pid)
+            assert np.array_equal(b.result(pid).ravel(), want["b"][pid]), (rep, pid)
+
+
 def test_run_to_host_errors():
     rng = np.random.default_rng(8)
     b, _ = build_batch(earth.gaussian_sets(2, seed=18), rng)

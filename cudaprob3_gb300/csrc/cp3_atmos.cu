@@ -239,6 +239,10 @@ __device__ __forceinline__ void atmos_bin_f64(SegFn seg, int M, const double* w,
         }
     }
     seg(0, F, arg);  // the air layer, applied last: A2 = G S_0
+    if (M == 0 && av.nb == 0) {  // the air layer alone: the one-layer expansion
+        layer_store64(layer_coefficients64(F.u, w), F.z, out, plane);
+        return;
+    }
     if (av.nb > 0) {
         cd sf[3][3];
         avg_shift_factors(av, ic, nc, ie, ne, arg, sf);

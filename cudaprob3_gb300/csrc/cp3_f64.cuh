@@ -89,4 +89,75 @@ __device__ __forceinline__ void to_flavour64(const cm3& A2, const double* w, cm3
     }
 }
 
+// The nine probabilities of a single constant-density layer (a beam baseline, or an
+// atmospheric bin that crosses no shell) from the three-flavour expansion over the matter
+// eigenstates, in FP64: the form of layer_coefficients / layer_store in cp3_mixed.cuh.
+//   P(a -> b) = delta_ab + 2 sum_{j>k} [Re c_jk (cos D_jk - 1) + Im c_jk sin D_jk],
+// with c_jk = m_aj m_ak for a = b (m_ak = |U_ak|^2, U_ak = (W u_k)_a); for a != b,
+// Re c_jk = W_l - (W_0 + W_1 + W_2) / 2 (W_k = m_ak m_bk, l the third index) and
+// Im c_10 = -Im c_20 = Im c_21 = +-J, the matter Jarlskog invariant (+ for e->mu, mu->tau,
+// tau->e).  It replaces forming S and its flavour-basis product (about 150 FP64 operations
+// per path length) by 19 coefficients per (energy, density) and about 30 operations per
+// path length.
+struct LayerCoefs64 {
+    double d[3][3];  // flavour a's survival: 2 m_aj m_ak for (j, k) = (1, 0), (2, 0), (2, 1)
+    double o[3][3];  // the pairs (e, mu), (mu, tau), (tau, e): 2 Re c_jk for the same (j, k)
+    double j2;       // 2 J_{e mu}
+};
+
+// u[k-1]: the unit eigenvector of eigenstate k in the rotated basis; w = {c23, s23, cos d, sin d}.
+__device__ __forceinline__ LayerCoefs64 layer_coefficients64(const double u[2][3], const double* w) {
+    const double c = w[0], s = w[1], er = w[2], ei = w[3];
+    const double cc = c * c, ss = s * s, cs2 = 2.0 * c * s;
+    double m[3][2], m0[3];  // m[a][k-1] = |U_ak|^2, m0[a] = |U_a0|^2
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const double b1 = u[k][1] * u[k][1], b2 = u[k][2] * u[k][2], xr = u[k][1] * u[k][2] * (cs2 * er);
+        m[0][k] = u[k][0] * u[k][0];
+        m[1][k] = cc * b1 + ss * b2 + xr;
+        m[2][k] = ss * b1 + cc * b2 - xr;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) m0[a] = 1.0 - m[a][0] - m[a][1];
+    LayerCoefs64 q;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        q.d[a][0] = 2.0 * m0[a] * m[a][0];
+        q.d[a][1] = 2.0 * m0[a] * m[a][1];
+        q.d[a][2] = 2.0 * m[a][0] * m[a][1];
+    }
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+        const int a = p, b = p == 2 ? 0 : p + 1;
+        const double W0 = m0[a] * m0[b], W1 = m[a][0] * m[b][0], W2 = m[a][1] * m[b][1];
+        const double S = W0 + W1 + W2;
+        q.o[p][0] = 2.0 * W2 - S;
+        q.o[p][1] = 2.0 * W1 - S;
+        q.o[p][2] = 2.0 * W0 - S;
+    }
+    q.j2 = cs2 * ei * (u[0][0] * u[1][0]) * (u[0][1] * u[1][2] - u[0][2] * u[1][1]);
+    return q;
+}
+
+// The nine probabilities of one path length from the coefficients and the layer's
+// z_k = e^{-i phi_k} - 1; channel a*3+b = P(a -> b) at out[ch * plane].
+__device__ __forceinline__ void layer_store64(const LayerCoefs64& q, const cd z[2],
+                                              double* __restrict__ out, size_t plane) {
+    // cos D - 1 for (1,0), (2,0), (2,1); sin D_10 - sin D_20 + sin D_21 = Im z_1 Re z_2 - Im z_2 Re z_1
+    const double g0 = z[0].re, g1 = z[1].re;
+    const double g2 = z[0].re + z[1].re + z[0].re * z[1].re + z[0].im * z[1].im;
+    const double jt = q.j2 * (z[0].im * z[1].re - z[1].im * z[0].re);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        out[(size_t)(a * 4) * plane] = 1.0 + q.d[a][0] * g0 + q.d[a][1] * g1 + q.d[a][2] * g2;
+    // (e, mu): channels 1 (e->mu) and 3 (mu->e); (mu, tau): 5 and 7; (tau, e): 6 and 2
+    constexpr int fwd[3] = {1, 5, 6}, rev[3] = {3, 7, 2};
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+        const double v = q.o[p][0] * g0 + q.o[p][1] * g1 + q.o[p][2] * g2;
+        out[(size_t)fwd[p] * plane] = v + jt;
+        out[(size_t)rev[p] * plane] = v - jt;
+    }
+}
+
 }  // namespace cp3

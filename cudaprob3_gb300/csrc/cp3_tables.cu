@@ -74,14 +74,7 @@ __global__ void __launch_bounds__(kTableBlock)
     double dmv[3], arg[3];
     rotated_layer_f64(&p, E, rho_e, f.u, dmv);
     layer64_phases(dmv, L, E, 1.0 / E, f, arg);
-    cm3 A2, A;
-    layer_to_gen64(f, A2);
-    to_flavour64(A2, p.w, A);
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-            out[(size_t)(i * 3 + j) * ne + ie] = A.a[j][i].re * A.a[j][i].re + A.a[j][i].im * A.a[j][i].im;
+    layer_store64(layer_coefficients64(f.u, p.w), f.z, out + ie, (size_t)ne);
 }
 
 }  // namespace

@@ -59,7 +59,7 @@ struct cp3_propagator {
 
     MixingInput mix;
     bool mns_set = false, masses_set = false;
-    std::vector<double> energies, cosines;
+    std::vector<double> cosines;  // the host builds the trajectories from it
     bool energies_set = false, cosines_set = false;
     EarthModel model;
     bool model_set = false;
@@ -201,7 +201,6 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
     h->nc = kind == 0 ? nc : 1;
     h->ne = ne;
     h->precision = precision;
-    h->energies.assign(ne, 0.0);
     if (kind == 0) h->cosines.assign(nc, 0.0);
     const size_t elems = (size_t)9 * h->nc * ne;
     h->result_bytes = elems * (precision == CP3_FP64 ? sizeof(double) : sizeof(float));
@@ -209,7 +208,7 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
         (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_upload, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaMallocHost(&h->h_stage, (size_t)ne * (sizeof(double) + sizeof(float2)))) !=
+        (e = cudaMallocHost(&h->h_stage, (size_t)ne * sizeof(double))) !=
             cudaSuccess ||
         (e = h->d_energies.reserve(ne)) != cudaSuccess ||
         (precision == CP3_MIXED && (e = h->d_energies_df.reserve(ne)) != cudaSuccess) ||
@@ -579,7 +578,6 @@ int cp3_set_energies(cp3_propagator* h, const double* energies, int n) {
     if (n != h->ne || !energies)
         return fail(h, CP3_ERR_BAD_SIZE,
                     "Propagator::setEnergyList. Propagator was not created for this number of energy nodes");
-    h->energies.assign(energies, energies + n);
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     // The staging buffer is reused: the previous upload must have read it.
     if (h->upload_pending) CP3_CUDA(h, cudaEventSynchronize(h->ev_upload), "energy upload");
@@ -591,12 +589,11 @@ int cp3_set_energies(cp3_propagator* h, const double* energies, int n) {
         CP3_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_done, 0), "order upload");
     CP3_CUDA(h, cudaMemcpyAsync(h->d_energies.ptr, stage, sizeof(double) * n,
                                 cudaMemcpyHostToDevice, h->stream), "upload energies");
-    if (h->precision == CP3_MIXED) {
-        float2* pairs = reinterpret_cast<float2*>(stage + n);
-        split_pairs(energies, (size_t)n, pairs);
-        CP3_CUDA(h, cudaMemcpyAsync(h->d_energies_df.ptr, pairs, sizeof(float2) * n,
-                                    cudaMemcpyHostToDevice, h->stream), "upload energies");
-    }
+    // the mixed kernels' float pairs, split on the device from the uploaded doubles (the same
+    // roundings as the host split: one list crosses the link once)
+    if (h->precision == CP3_MIXED)
+        CP3_CUDA(h, launch_split_pairs(h->d_energies.ptr, n, h->d_energies_df.ptr, h->stream),
+                 "split energies");
     CP3_CUDA(h, cudaEventRecord(h->ev_upload, h->stream), "record upload");
     h->upload_pending = true;
     h->energies_set = true;

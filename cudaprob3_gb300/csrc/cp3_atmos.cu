@@ -679,6 +679,24 @@ cudaError_t launch_plane_transpose(const void* src, bool is_float, int nc, int n
     return cudaGetLastError();
 }
 
+// x[i] as float pairs (hi, lo), hi + lo = x[i] to ~48 bits: hi = x rounded to float, lo =
+// the exact remainder x - hi rounded to float (the host's split, done on the device, so that
+// an energy list goes up once, as doubles).
+__global__ void __launch_bounds__(256)
+    split_pairs_kernel(const double* __restrict__ x, int n, float2* __restrict__ out) {
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    out[i] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
+cudaError_t launch_split_pairs(const double* x, int n, float2* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    split_pairs_kernel<<<(n + 255) / 256, 256, 0, s>>>(x, n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_beam_mixed(const OscParams& p, const float2* energies, int ne, double rho_e,
                               double L_km, float* out, cudaStream_t s) {
     if (ne <= 0) return cudaSuccess;

@@ -89,6 +89,9 @@ cudaError_t launch_atmos_inline(const OscParams& p, bool mixed, const double* en
                                 int n_cosines, const AvgArrays& avg, void* out, cudaStream_t s,
                                 RowRange rr = RowRange{});
 
+// out[i] = (x[i] rounded to float, the remainder rounded to float), on the device.
+cudaError_t launch_split_pairs(const double* x, int n, float2* out, cudaStream_t s);
+
 // One channel plane [nc][ne] (float or double) transposed to [ne][nc] doubles.
 cudaError_t launch_plane_transpose(const void* src, bool is_float, int nc, int ne, double* dst,
                                    cudaStream_t s);

@@ -44,11 +44,11 @@ NCU_TRAFFIC = {
     ("atmos59", "mixed"): (5.910016e6 + 84.903680e6, 144.0e6,
                            "profiles/atmos_mixed_kernel_59shells_2000x2000.md"),
     # the table launch and the bin launch of one run
-    ("batch_atmos", "mixed"): (0.436992e6 + 0.060416e6 + 204.449536e6 + 978.470912e6, 912.332288e6,
+    ("batch_atmos", "mixed"): (0.431616e6 + 0.060672e6 + 205.593088e6 + 982.776320e6, 912.332288e6,
                                "profiles/batch_kernel_prem12_48problems.md"),
     ("batch_beam", "mixed"): (115.457024e6 + 911.392000e6, 921.6e6,
                               "profiles/batch_kernel_beam_128problems.md"),
-    ("atmos59", "fp64"): (9.935872e6 + 245.010688e6, 288.0e6,
+    ("atmos59", "fp64"): (9.871104e6 + 244.749312e6, 288.0e6,
                           "profiles/atmos_f64_kernel_59shells_2000x2000.md"),
     # the 7.2 MB output is still in L2 when the captured launch ends
     ("beam", "fp64"): (0.865792e6, 7.2e6, "profiles/beam_f64_kernel_1e5energies.md"),
@@ -61,11 +61,11 @@ NCU_TRAFFIC = {
 # 1); this is the utilisation of what they do execute.
 NCU_PIPE = {
     ("atmos59", "mixed"): ("sm__pipe_fma_cycles_active", 0.7099),
-    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6568),  # the bin launch
+    ("batch_atmos", "mixed"): ("sm__pipe_fma_cycles_active", 0.6572),  # the bin launch
     ("batch_beam", "mixed"): ("sm__pipe_fma_cycles_active", 0.6007),
-    ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8926),
-    ("beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),
-    ("batch_beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8500),
+    ("atmos59", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8930),
+    ("beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8518),
+    ("batch_beam", "fp64"): ("sm__pipe_fp64_cycles_active", 0.8518),
 }
 
 

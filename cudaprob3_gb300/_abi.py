@@ -15,6 +15,7 @@ EXPORTS = (
     "cp3_atmos_create", "cp3_beam_create", "cp3_destroy", "cp3_last_error", "cp3_get_info",
     "cp3_set_energies", "cp3_set_cosines", "cp3_set_mns", "cp3_set_masses", "cp3_set_layers",
     "cp3_set_layers_poly", "cp3_set_density_file", "cp3_set_chemical_composition",
+    "cp3_get_n_layer_boundaries",
     "cp3_set_production_height", "cp3_set_beam_density", "cp3_set_beam_path_length",
     "cp3_set_production_height_averaging", "cp3_calculate", "cp3_calculate_async",
     "cp3_calculate_to_host_async",
@@ -58,6 +59,7 @@ _SIGS = {
     "cp3_set_layers_poly": ([_h, _dp, _dp, _dp, _dp, _dp, C.c_int], C.c_int),
     "cp3_set_density_file": ([_h, C.c_char_p, C.c_double, C.c_double], C.c_int),
     "cp3_set_chemical_composition": ([_h, _dp, C.c_int], C.c_int),
+    "cp3_get_n_layer_boundaries": ([_h, C.POINTER(C.c_int)], C.c_int),
     "cp3_set_production_height": ([_h, C.c_double], C.c_int),
     "cp3_set_beam_density": ([_h, C.c_double], C.c_int),
     "cp3_set_beam_path_length": ([_h, C.c_double], C.c_int),

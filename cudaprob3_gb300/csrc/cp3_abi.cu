@@ -688,6 +688,15 @@ int cp3_set_density_file(cp3_propagator* h, const char* path, double ye_core, do
     return set_model(h, cols[0].data(), cols[1].data(), cols[2].data(), cols[3].data(), cols[4].data(), n, true);
 }
 
+int cp3_get_n_layer_boundaries(cp3_propagator* h, int* n) {
+    if (int rc = check_handle(h)) return rc;
+    if (!n) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output");
+    if (h->kind != 0) return fail(h, CP3_ERR_UNSUPPORTED, "beam propagators have no layer boundaries");
+    if (!h->model_set) return fail(h, CP3_ERR_NOT_SET, "density model was not set");
+    *n = (int)h->model.radii.size();
+    return CP3_OK;
+}
+
 int cp3_set_chemical_composition(cp3_propagator* h, const double* ye, int n) {
     if (int rc = check_handle(h)) return rc;
     if (!h->model_set || !ye || (size_t)n != h->model.ye.size())

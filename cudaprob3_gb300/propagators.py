@@ -162,6 +162,13 @@ class AtmosCudaPropagatorSingle(Propagator):
         a, p = _f64(yps)
         self._check(self._lib.cp3_set_chemical_composition(self._h, p, len(a)))
 
+    def getNlayerBoundaries(self):
+        """The density model's rows (layers + 1), as AtmosCpuPropagator::getNlayerBoundaries
+        (atmoscpupropagator.hpp:85) after setDensityFromFile."""
+        n = C.c_int()
+        self._check(self._lib.cp3_get_n_layer_boundaries(self._h, C.byref(n)))
+        return n.value
+
     def setProductionHeight(self, heightKM):
         self._check(self._lib.cp3_set_production_height(self._h, float(heightKM)))
 

@@ -122,6 +122,14 @@ int cp3_set_density_file(cp3_propagator* h, const char* path, double default_ye_
  * atmoscudapropagator.cu:207-220): n must equal the number of model rows. */
 int cp3_set_chemical_composition(cp3_propagator* h, const double* ye, int n);
 
+/* AtmosCpuPropagator::getNlayerBoundaries (atmoscpupropagator.hpp:85): *n = the number of
+ * rows of the density model (its layer boundaries, the r = 0 row included), one more than
+ * its layers.  The reference sets the count only in setDensityFromFile
+ * (atmoscpupropagator.hpp:343) and returns an uninitialised value after the other density
+ * setters; here every density setter sets it.  CP3_ERR_NOT_SET before a density model,
+ * CP3_ERR_UNSUPPORTED on a beam handle. */
+int cp3_get_n_layer_boundaries(cp3_propagator* h, int* n);
+
 /* AtmosCpuPropagator::setProductionHeight (atmoscpupropagator.hpp:386-393): km; the cosine
  * list must be set first ("must set cosine list before production height"). */
 int cp3_set_production_height(cp3_propagator* h, double height_km);

@@ -139,6 +139,13 @@ public:
     void setChemicalComposition(const std::vector<double>& list) override {
         detail::check(cp3_set_chemical_composition(h_, list.data(), (int)list.size()), h_);
     }
+    // AtmosCpuPropagator::getNlayerBoundaries (atmoscpupropagator.hpp:85): the density
+    // model's rows (layers + 1), after any density setter.
+    virtual int getNlayerBoundaries() {
+        int n = 0;
+        detail::check(cp3_get_n_layer_boundaries(h_, &n), h_);
+        return n;
+    }
     void setProductionHeight(double heightKM) {
         detail::check(cp3_set_production_height(h_, heightKM), h_);
     }

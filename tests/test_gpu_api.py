@@ -115,6 +115,24 @@ def test_density_file_formats(tmp_path, oracle):
         configured().setDensityFromFile(str(bad))
 
 
+def test_layer_boundaries(tmp_path):
+    """getNlayerBoundaries: the model's rows (layers + 1) after setDensityFromFile, as the
+    reference counts them, and after every other density setter too."""
+    r, rho, ye = earth.PREM_4LAYER
+    f = tmp_path / "prem.dat"
+    f.write_text("".join(f"{a} {b} {c}\n" for a, b, c in zip(r, rho, ye)))
+    p = configured()
+    assert p.getNlayerBoundaries() == len(r)
+    p.setDensityFromFile(str(f))
+    assert p.getNlayerBoundaries() == len(r) == 5
+    p.setDensity(*earth.PREM_12LAYER)
+    assert p.getNlayerBoundaries() == len(earth.PREM_12LAYER[0])
+    p.setDensity(*earth.PREM_4LAYER_QUAD_V2)
+    assert p.getNlayerBoundaries() == len(earth.PREM_4LAYER_QUAD_V2[0])
+    with pytest.raises(RuntimeError, match="density model was not set"):
+        AtmosCudaPropagatorSingle(0, 6, 5).getNlayerBoundaries()
+
+
 def test_beam_api_and_legacy_template_name():
     b = BeamCudaPropagatorSingle(0, 100, 1)
     b.setEnergyList(earth.lin_energy_grid(100))

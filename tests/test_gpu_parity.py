@@ -136,3 +136,51 @@ def test_quadratic_density_against_oracle(oracle, prec, tol):
             got = run_atmos(prec, [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq],
                             knu, anti, cz, en, r, None, ye, 18.0, poly_abc=(a, b, c))
             assert np.abs(got - ref).max() <= tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_tiny_grids_against_oracle(oracle, prec, tol):
+    """One bin, one cosine row, one energy column, and a beam of one energy: every launch
+    shape's edge (a partial warp, a single block, one table entry per class)."""
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix
+    r, rho, ye = earth.PREM_4LAYER
+    m = earth.NOMINAL
+    cases = [(np.array([-1.0]), np.array([2.5])),
+             (np.array([-0.6]), earth.log_energy_grid(300)),
+             (np.linspace(-1, 1, 300), np.array([0.7])),
+             (np.array([-0.9, 0.3]), np.array([0.3, 4.0, 40.0]))]
+    for cz, en in cases:
+        for anti, knu in ((False, 1), (True, -1)):
+            om = OMix(m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq, knu)
+            mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+            ref = oracle.atmos(om, anti, cz, en, r, rho, ye, 22.0)
+            got = run_atmos(prec, mix6, knu, anti, cz, en, r, rho, ye, 22.0)
+            assert got.shape == ref.shape
+            assert np.abs(got - ref).max() <= tol, (len(cz), len(en), anti)
+            got_b = run_beam(prec, mix6, knu, anti, en[:1], 2.6, 1300.0)
+            ref_b = oracle.beam(om, anti, en[:1], 2.6, 1300.0)
+            assert np.abs(got_b - ref_b).max() <= tol
+
+
+@pytest.mark.parametrize("prec,tol,lo", [("fp64", FP64_TOL, 0.05), ("mixed", MIXED_TOL, 0.01)])
+def test_energies_far_outside_the_configurations(oracle, prec, tol, lo):
+    """Energies from 0.01 GeV (phases of ~1e4 rad through the core; FP64 from 0.05 GeV, where
+    the reference's own phase roundings stay below its 1e-12 bar) to 10 TeV, where the matter
+    potential dwarfs the splittings and two levels sit within 1e-3 of the spread, so the mixed
+    solver hands many entries to its FP64 fallback.  PREM-4 and PREM-12, both orderings."""
+    from cudaprob3_gb300 import earth
+    from oracle.oracle import Mixing as OMix
+    cz = np.linspace(-1, 1, 41)
+    en = np.logspace(np.log10(lo), 4, 60)
+    for model in (earth.PREM_4LAYER, earth.PREM_12LAYER):
+        r, rho, ye = model
+        for m in earth.gaussian_sets(256, seed=2024)[::127]:  # sets 0, 127 (normal), 254 (inverted)
+            for anti, knu in ((False, 1), (True, -1)):
+                mix6 = [m.theta12, m.theta13, m.theta23, m.dcp, m.dm12sq, m.dm23sq]
+                ref = oracle.atmos(OMix(*mix6[:4], *mix6[4:], knu), anti, cz, en, r, rho, ye, 22.0)
+                got = run_atmos(prec, mix6, knu, anti, cz, en, r, rho, ye, 22.0)
+                assert np.abs(got - ref).max() <= tol, (len(r), m.dm23sq, anti)
+            ref_b = oracle.beam(OMix(*mix6[:4], *mix6[4:], 1), False, en, 2.6, 1300.0)
+            got_b = run_beam(prec, mix6, 1, False, en, 2.6, 1300.0)
+            assert np.abs(got_b - ref_b).max() <= tol

@@ -1,6 +1,6 @@
 """Runs a fixed mix of batch and serving work with whichever library CP3GB300_LIB (or the
-in-tree default) selects and saves every result to an .npz: the driver of
-test_gpu_device_checks.py, which compares the debug build (device bounds checks) with the
+in-tree default) selects and saves every result to an .npz.  test_gpu_device_checks.py
+runs it once per library and compares the debug build (device bounds checks) with the
 product build.  Usage: python tests/device_checks_run.py OUT.npz"""
 import os
 import sys

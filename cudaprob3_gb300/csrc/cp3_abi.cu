@@ -98,12 +98,18 @@ struct cp3_propagator {
     bool timed_table = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
-    // Energy lists go up asynchronously on `stream` from a pinned staging buffer; a compute
-    // on another stream waits for ev_upload.  ev_done marks the end of the last compute (on
-    // last_stream): uploads and computes that overwrite what it reads or writes wait for it.
+    // Energy lists go up asynchronously on `stream` from two pinned staging slots used in
+    // turn (ev_stage[i] marks the end of slot i's last upload, so a setter waits only for the
+    // upload two calls back, not for the last compute the newest upload is queued behind); a
+    // compute on another stream waits for ev_upload.  ev_done marks the end of the last
+    // compute (on last_stream): uploads and computes that overwrite what it reads or writes
+    // wait for it.
     cudaEvent_t ev_done = nullptr, ev_upload = nullptr;
     bool upload_pending = false;
-    void* h_stage = nullptr;
+    void* h_stage = nullptr;  // 2 x ne doubles
+    cudaEvent_t ev_stage[2] = {nullptr, nullptr};
+    bool stage_busy[2] = {false, false};
+    int stage_slot = 0;
 
     // The downloads of calculate_to_host_async (atmospheric row pieces) run on copy_stream:
     // piece c's copy waits for ev_piece[c] (its rows computed) and records
@@ -125,6 +131,8 @@ struct cp3_propagator {
         if (ev_copied) cudaEventDestroy(ev_copied);
         if (ev_done) cudaEventDestroy(ev_done);
         if (ev_upload) cudaEventDestroy(ev_upload);
+        for (cudaEvent_t e : ev_stage)
+            if (e) cudaEventDestroy(e);
         if (h_stage) cudaFreeHost(h_stage);
         if (h_result) cudaFreeHost(h_result);
         if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -208,8 +216,9 @@ int create(int kind, int device, int nc, int ne, int precision, cp3_propagator**
         (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_upload, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaMallocHost(&h->h_stage, (size_t)ne * sizeof(double))) !=
-            cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_stage[0], cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_stage[1], cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaMallocHost(&h->h_stage, 2 * (size_t)ne * sizeof(double))) != cudaSuccess ||
         (e = h->d_energies.reserve(ne)) != cudaSuccess ||
         (precision == CP3_MIXED && (e = h->d_energies_df.reserve(ne)) != cudaSuccess) ||
         (e = h->d_result.reserve(h->result_bytes)) != cudaSuccess) {
@@ -579,16 +588,20 @@ int cp3_set_energies(cp3_propagator* h, const double* energies, int n) {
         return fail(h, CP3_ERR_BAD_SIZE,
                     "Propagator::setEnergyList. Propagator was not created for this number of energy nodes");
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    // The staging buffer is reused: the previous upload must have read it.
-    if (h->upload_pending) CP3_CUDA(h, cudaEventSynchronize(h->ev_upload), "energy upload");
-    h->upload_pending = false;
-    double* stage = static_cast<double*>(h->h_stage);
+    // This staging slot's last upload (two calls back) must have read it.  (One slot would
+    // make every call wait for the previous upload, which is queued behind the last compute.)
+    const int slot = h->stage_slot;
+    if (h->stage_busy[slot]) CP3_CUDA(h, cudaEventSynchronize(h->ev_stage[slot]), "energy upload");
+    double* stage = static_cast<double*>(h->h_stage) + (size_t)slot * h->ne;
     std::memcpy(stage, energies, sizeof(double) * n);
     // The upload overwrites what the last compute reads: it waits for it on the device.
     if (h->last_stream && h->last_stream != h->stream)
         CP3_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_done, 0), "order upload");
     CP3_CUDA(h, cudaMemcpyAsync(h->d_energies.ptr, stage, sizeof(double) * n,
                                 cudaMemcpyHostToDevice, h->stream), "upload energies");
+    CP3_CUDA(h, cudaEventRecord(h->ev_stage[slot], h->stream), "record upload");
+    h->stage_busy[slot] = true;
+    h->stage_slot = slot ^ 1;
     // the mixed kernels' float pairs, split on the device from the uploaded doubles (the same
     // roundings as the host split: one list crosses the link once)
     if (h->precision == CP3_MIXED)

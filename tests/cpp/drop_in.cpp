@@ -29,6 +29,7 @@ int main(int argc, char** argv) {
         propagator->setDensity({0., 1220., 3480., 5701., 6371.}, {13., 13., 11.3, 5., 3.3},
                                {.468, .468, .468, .497, .497});
     propagator->setProductionHeight(22.0);
+    std::printf("boundaries %d\n", propagator->getNlayerBoundaries());
     propagator->calculateProbabilities(cudaprob3linear::Neutrino);
     for (int ic = 0; ic < nc; ic += 3)
         for (int ie = 0; ie < ne; ie += 5)

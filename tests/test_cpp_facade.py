@@ -39,6 +39,7 @@ def test_facade_matches_oracle(tmp_path, oracle):
         out = subprocess.run(args, capture_output=True, text=True, timeout=120)
         assert out.returncode == 0, out.stdout + out.stderr
         assert "caught: CudaPropagatorSingle::getProbability. Invalid indices" in out.stdout
+        assert "boundaries 5" in out.stdout  # PREM 4-layer: 5 rows, from the file or setDensity
         nc, ne = 20, 16
         cz = -1.0 + 2.0 * np.arange(nc) / (nc - 1)
         en = 10 ** (-1.0 + 3.0 * np.arange(ne) / (ne - 1))

@@ -116,3 +116,36 @@ def test_mixed_averaging_with_quadratic_density_against_oracle(oracle, scale):
         got = run_avg("mixed", mix6, knu, anti, cz, en, r, None, ye, 20.0, nb, w.ravel(), edges,
                       (a, b, c))
         assert np.abs(got - ref).max() <= 1e-5
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("poly", [False, True])
+def test_averaged_results_to_host_in_row_pieces(prec, poly):
+    """calculate_to_host_async with averaging on: every averaging kernel (FP64, mixed, and
+    the quadratic-density forms) runs in row pieces whose copies overlap the next piece, and
+    the host buffer equals the device result for any number of pieces."""
+    import torch
+    nc, ne, nb = 41, 37, 5
+    m = earth.NOMINAL
+    edges = np.linspace(5.0, 45.0, nb + 1)
+    prob = np.full((2, 3, ne, nc, nb), 1.0 / nb)
+    p = AtmosCudaPropagatorSingle(0, nc, ne, precision=prec)
+    p.setEnergyList(earth.log_energy_grid(ne))
+    p.setCosineList(earth.cosine_grid(nc))
+    p.setMNSMatrix(m.theta12, m.theta13, m.theta23, m.dcp, 1)
+    p.setNeutrinoMasses(m.dm12sq, m.dm23sq)
+    if poly:
+        p.setDensity(*earth.PREM_4LAYER_QUAD_V2)
+    else:
+        p.setDensity(*earth.PREM_4LAYER)
+    p.setProductionHeight(22.0)
+    p.SetNumberOfProductionHeightBinsForAveraging(nb)
+    p.setProductionHeightList(prob.ravel(), edges)
+    p.calculateProbabilities(0)
+    want = p.result().copy()
+    dtype = torch.float64 if prec == "fp64" else torch.float32
+    for chunks in (1, 3, 7, nc):
+        host = torch.full((9 * nc * ne,), -1.0, dtype=dtype, pin_memory=True)
+        p.calculate_to_host_async(0, host.data_ptr(), chunks)
+        p.synchronize()
+        assert np.array_equal(host.numpy().reshape(want.shape), want), chunks

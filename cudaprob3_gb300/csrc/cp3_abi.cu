@@ -89,7 +89,7 @@ struct cp3_propagator {
     DevBuf<char> d_result;
     size_t result_bytes = 0;
 
-    double* h_result = nullptr;  // pinned, lazily allocated
+    void* h_result = nullptr;  // pinned, lazily allocated: the device result's layout and type
     bool result_on_host = false;
     bool computed = false;
 
@@ -520,27 +520,26 @@ int launch(cp3_propagator* h, int type, cudaStream_t s, void* host_dst = nullptr
     return CP3_OK;
 }
 
+// The whole result, downloaded once per computation for the host getters.  The mixed
+// kernels' floats stay floats and are widened as they are read: widening all of them up
+// front cost more than the download (36e6 values per type on a 2000 x 2000 grid).
 int fetch_result(cp3_propagator* h) {
     TraceRange trace("fetch_result");
     if (!h->computed) return fail(h, CP3_ERR_NOT_SET, "no probabilities computed yet");
     if (h->result_on_host) return CP3_OK;
-    const size_t n = h->result_bytes / (h->precision == CP3_FP64 ? 8 : 4);
-    if (!h->h_result) CP3_CUDA(h, cudaMallocHost(&h->h_result, n * sizeof(double)), "pinned result");
+    if (!h->h_result) CP3_CUDA(h, cudaMallocHost(&h->h_result, h->result_bytes), "pinned result");
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     CP3_CUDA(h, cudaStreamSynchronize(h->last_stream ? h->last_stream : h->stream), "synchronize");
-    if (h->precision == CP3_FP64) {
-        CP3_CUDA(h, cudaMemcpy(h->h_result, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost),
-                 "copy result");
-    } else {
-        // floats land in the second half of the pinned buffer, then widen in place (forward
-        // order never overwrites an unread float: float i sits at byte 4*(n+i) >= 8*i).
-        float* f = reinterpret_cast<float*>(h->h_result) + n;
-        CP3_CUDA(h, cudaMemcpy(f, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost),
-                 "copy result");
-        for (size_t i = 0; i < n; i++) h->h_result[i] = (double)f[i];
-    }
+    CP3_CUDA(h, cudaMemcpy(h->h_result, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost),
+             "copy result");
     h->result_on_host = true;
     return CP3_OK;
+}
+
+// Value i of the downloaded result, as a double.
+double host_value(const cp3_propagator* h, size_t i) {
+    return h->precision == CP3_FP64 ? static_cast<const double*>(h->h_result)[i]
+                                    : (double)static_cast<const float*>(h->h_result)[i];
 }
 
 int check_type(cp3_propagator* h, int t) {
@@ -810,7 +809,7 @@ int cp3_get_probability(cp3_propagator* h, int ic, int ie, int t, double* out) {
         return fail(h, CP3_ERR_INDEX, "CudaPropagatorSingle::getProbability. Invalid indices");
     if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");
     if (int rc = fetch_result(h)) return rc;
-    *out = h->h_result[((size_t)t * h->nc + ic) * h->ne + ie];
+    *out = host_value(h, ((size_t)t * h->nc + ic) * h->ne + ie);
     return CP3_OK;
 }
 
@@ -822,7 +821,7 @@ int cp3_get_probability_beam(cp3_propagator* h, int ie, int t, double* out) {
         return fail(h, CP3_ERR_INDEX, "CudaPropagatorSingle::getProbability. Invalid indices");
     if (!out) return fail(h, CP3_ERR_BAD_ARGUMENT, "null output pointer");
     if (int rc = fetch_result(h)) return rc;
-    *out = h->h_result[(size_t)t * h->ne + ie];
+    *out = host_value(h, (size_t)t * h->ne + ie);
     return CP3_OK;
 }
 
@@ -852,10 +851,10 @@ int cp3_get_probability_arr(cp3_propagator* h, int t, double* out) {
         cudaGetLastError();  // a grid beyond the launch limits: reorder on the host instead
     }
     if (int rc = fetch_result(h)) return rc;
-    const double* plane = h->h_result + (size_t)t * cells;
+    const size_t base = (size_t)t * cells;
     size_t it = 0;
     for (int ie = 0; ie < h->ne; ie++)
-        for (int ic = 0; ic < h->nc; ic++) out[it++] = plane[(size_t)ic * h->ne + ie];
+        for (int ic = 0; ic < h->nc; ic++) out[it++] = host_value(h, base + (size_t)ic * h->ne + ie);
     return CP3_OK;
 }
 

@@ -871,6 +871,9 @@ int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream) {
     if (!dst) return fail(h, CP3_ERR_BAD_ARGUMENT, "null destination");
     CP3_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     cudaStream_t s = stream ? (cudaStream_t)stream : (h->last_stream ? h->last_stream : h->stream);
+    // on another stream than the last compute's, the copy waits for it on the device
+    if (h->last_stream && s != h->last_stream)
+        CP3_CUDA(h, cudaStreamWaitEvent(s, h->ev_done, 0), "order copy");
     CP3_CUDA(h, cudaMemcpyAsync(dst, h->d_result.ptr, h->result_bytes, cudaMemcpyDeviceToHost, s),
              "copy result");
     return CP3_OK;

@@ -768,8 +768,9 @@ int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream) {
     if (int rc = cp3_batch_result(b, id, &src, &n)) return rc;
     if (!dst) return bfail(b, CP3_ERR_BAD_ARGUMENT, "null destination");
     B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
-    B_CUDA(b, cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToHost,
-                              stream ? (cudaStream_t)stream : b->stream), "copy result");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    if (b->ran) B_CUDA(b, cudaStreamWaitEvent(s, b->ev1, 0), "order copy after the last run");
+    B_CUDA(b, cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToHost, s), "copy result");
     return CP3_OK;
 }
 
@@ -790,8 +791,11 @@ int cp3_batch_copy_results(cp3_batch* b, size_t first, size_t count, void* dst, 
                                            std::to_string(b->out_floats) + " floats)");
     if (count == 0) return CP3_OK;
     B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
-    B_CUDA(b, cudaMemcpyAsync(dst, b->d_out.ptr + first, count * sizeof(float), cudaMemcpyDefault,
-                              stream ? (cudaStream_t)stream : b->stream), "copy results");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    // on another stream than the last run's, the copy waits for that run on the device
+    if (b->ran) B_CUDA(b, cudaStreamWaitEvent(s, b->ev1, 0), "order copy after the last run");
+    B_CUDA(b, cudaMemcpyAsync(dst, b->d_out.ptr + first, count * sizeof(float), cudaMemcpyDefault, s),
+           "copy results");
     return CP3_OK;
 }
 

@@ -195,7 +195,8 @@ int cp3_device_result(cp3_propagator* h, const void** ptr, int* is_float, size_t
 
 /* No reference counterpart: asynchronous copy of the whole result, native element type and
  * device layout, into dst (bytes as reported by cp3_device_result) on `stream`
- * (NULL = the stream of the last compute). */
+ * (NULL = the stream of the last compute; another stream waits for that compute on the
+ * device). */
 int cp3_copy_result_async(cp3_propagator* h, void* dst, void* stream);
 
 /* ---- trajectory geometry (host only, no GPU) --------------------------------------------- */
@@ -295,15 +296,17 @@ int cp3_batch_run_to_host(cp3_batch* b, void* dst, int n_pieces, void* stream);
 int cp3_batch_synchronize(cp3_batch* b, double* ms);
 /* Device pointer and float count of one problem's result. */
 int cp3_batch_result(cp3_batch* b, int id, const float** ptr, size_t* count);
-/* Asynchronous copy of one problem's result to dst (count floats) on `stream`. */
+/* Asynchronous copy of one problem's result to dst (count floats) on `stream`, after the last
+ * run on the device whatever its stream. */
 int cp3_batch_copy_result(cp3_batch* b, int id, void* dst, void* stream);
 /* The results of all problems sit in one arena of result_bytes / 4 floats (cp3_batch_info);
  * problem id's result starts at float *offset of it.  (No reference counterpart: the
  * reference has no batches.) */
 int cp3_batch_result_offset(const cp3_batch* b, int id, size_t* offset);
 /* Asynchronous copy of the arena's floats [first, first + count) to dst (host or device) on
- * `stream` (NULL: the batch's own stream).  A caller that wants every result moves them in a
- * few large copies instead of one per problem; gaps between problems hold no results. */
+ * `stream` (NULL: the batch's own stream), after the last run on the device whatever its
+ * stream.  A caller that wants every result moves them in a few large copies instead of one
+ * per problem; gaps between problems hold no results. */
 int cp3_batch_copy_results(cp3_batch* b, size_t first, size_t count, void* dst, void* stream);
 /* Bytes of one problem's parameter block (what a run uploads per problem after
  * cp3_batch_set_params). */

@@ -238,6 +238,46 @@ def test_pipelined_downloads_never_see_a_later_step():
     assert np.array_equal(p.result(), want[1])
 
 
+def test_copies_on_another_stream_wait_for_the_compute():
+    """cp3_copy_result_async on a stream other than the compute's, queued right behind it with
+    no host wait, sees the finished result; so does a batch's arena copy on another stream."""
+    import torch
+    from cudaprob3_gb300.batch import Batch
+    nc, ne = 1000, 1000
+    p = configured(nc=nc, ne=ne, prec="mixed")
+    p.calculateProbabilities(NeutrinoType.Neutrino)
+    want = p.result().copy()
+    a, b = torch.cuda.Stream(), torch.cuda.Stream()
+    for rep in range(3):
+        host = torch.full((9 * nc * ne,), -1.0, dtype=torch.float32, pin_memory=True)
+        p.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, -1)
+        p.calculate_async(NeutrinoType.Antineutrino, a.cuda_stream)  # a different result first
+        p.setMNSMatrix(NOM.theta12, NOM.theta13, NOM.theta23, NOM.dcp, 1)
+        p.calculate_async(NeutrinoType.Neutrino, a.cuda_stream)
+        p.copy_result_async(host.data_ptr(), b.cuda_stream)
+        b.synchronize()
+        assert np.array_equal(host.numpy().reshape(want.shape), want), rep
+    bt = Batch(0)
+    bt.set_earth(*earth.PREM_12LAYER, 22.0)
+    pid = bt.add_atmos(earth.cosine_grid(800), earth.log_energy_grid(900))
+    bt.set_params(pid, NOM, False)
+    bt.commit()
+    bt.run()
+    bt.synchronize()
+    want_b = bt.result(pid).ravel()
+    total = bt.info()["result_bytes"] // 4
+    for rep in range(3):
+        host = torch.full((total,), -1.0, dtype=torch.float32, pin_memory=True)
+        bt.set_params(pid, earth.gaussian_sets(2, seed=3)[1], True)
+        bt.run(a.cuda_stream)  # a different result first
+        bt.set_params(pid, NOM, False)
+        bt.run(a.cuda_stream)
+        bt.copy_results_async(0, total, host.data_ptr(), b.cuda_stream)
+        b.synchronize()
+        off = bt.result_offset(pid)
+        assert np.array_equal(host.numpy()[off:off + want_b.size], want_b), rep
+
+
 def test_calculate_to_host_beam():
     import torch
     ne = 101

@@ -227,18 +227,19 @@ def run_batch(args, w, rank, world):
 
     # end to end through the public API: every step uploads each problem's parameters
     # (cp3_batch_set_params), runs, and downloads the whole result arena into page-locked
-    # host memory.  Where the arena fits in a quarter of the host's memory (up to 16 GB),
+    # host memory.  Where the arena fits in a third of the host's memory (C2's 10.8 GB; C3's
+    # 59 GB on a 199 GB host, pinned in ~5 s before the timed region),
     # cp3_batch_run_to_host runs the bins in windows of whole problems and downloads each
-    # window while the next computes.  Otherwise (C3's 59 GB) the run is followed by copies
-    # of the arena in 256 MB pieces into one reused buffer (cp3_batch_copy_results): the
-    # bytes cross the link all the same.
+    # window while the next computes.  Otherwise the run is followed by copies of the arena
+    # in 256 MB pieces into one reused buffer (cp3_batch_copy_results): the bytes cross the
+    # link all the same.
     arena = b.info()["result_bytes"] // 4
     piece = 64 << 20  # floats
     try:
         host_mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
     except (ValueError, OSError, AttributeError):
         host_mem = 0
-    whole = 4 * arena <= min(16 << 30, host_mem // 4)
+    whole = 4 * arena <= host_mem // 3
     host = torch.empty(arena if whole else min(piece, arena), dtype=torch.float32, pin_memory=True)
 
     # Steps are queued back to back (set_params waits only until the previous step's
